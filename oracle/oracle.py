@@ -1,0 +1,153 @@
+"""ctypes bindings for the C restatement oracle (oracle/race_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py to check or time the reference algorithm. The
+product never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import pathlib
+import subprocess
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+SRC = HERE / "race_oracle.c"
+OUT_DIR = HERE / "_build"
+LIB = OUT_DIR / "librace_oracle.so"
+
+IP = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+DP = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+K_SPMV, K_SPMTV, K_SYMMSPMV, K_GS, K_KACZ = 0, 1, 2, 3, 4
+
+_lib = None
+
+
+def build(force: bool = False) -> pathlib.Path:
+    """Compile the oracle with -O3 -fopenmp and no floating-point contraction
+    (every fused multiply-add in the source is an explicit fma())."""
+    OUT_DIR.mkdir(exist_ok=True)
+    if force or not LIB.exists() or LIB.stat().st_mtime < SRC.stat().st_mtime:
+        tmp = LIB.with_suffix(f".{os.getpid()}.tmp")
+        subprocess.check_call(["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c11",
+                               str(SRC), "-o", str(tmp), "-lm"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        L.orc_bfs.restype = C.c_int
+        L.orc_bfs.argtypes = [C.c_int, IP, IP, IP, IP, C.c_int, C.c_int, C.c_int, IP]
+        L.orc_level_data.argtypes = [IP, IP, IP, C.c_int, C.c_int, C.c_int, IP, IP]
+        L.orc_level_permute.argtypes = [C.c_int, IP, C.c_int, C.c_int, C.c_int, IP, IP]
+        for nm in ["orc_spmv_range", "orc_spmtv_range", "orc_symmspmv_range"]:
+            getattr(L, nm).argtypes = [C.c_int, C.c_int, IP, IP, DP, DP, DP]
+        for nm in ["orc_gs_range", "orc_kacz_range"]:
+            getattr(L, nm).argtypes = [C.c_int, C.c_int, IP, IP, DP, DP, DP]
+        L.orc_exec_tree.argtypes = [C.c_int, IP, IP, IP, IP, IP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    IP, IP, DP, DP, DP]
+        L.orc_mpk_plain.argtypes = [C.c_int, C.c_int, IP, IP, DP, DP]
+        L.orc_mpk_groups.restype = C.c_int
+        L.orc_mpk_groups.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_double, C.c_double, C.c_int, C.c_int,
+                                     IP, IP, IP, IP, IP]
+        L.orc_mpk_unlock_ctr.argtypes = [C.c_int, IP, IP, C.c_int, IP]
+        L.orc_mpk_wavefront.argtypes = [C.c_int, C.c_int, C.c_int, IP, IP, IP, IP, IP, IP, DP, DP]
+        _lib = L
+    return _lib
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def bfs(csr, dist: int, lo: int, hi: int, total_perm=None, total_inv=None):
+    """Distances of rows [lo,hi) in the current permuted space."""
+    n = csr.n
+    tp = _i32(np.arange(n) if total_perm is None else total_perm)
+    ti = _i32(np.arange(n) if total_inv is None else total_inv)
+    d = np.zeros(n, np.int32)
+    L = lib().orc_bfs(n, _i32(csr.row_ptr), _i32(csr.col), tp, ti, dist, lo, hi, d)
+    if L < 0:
+        raise RuntimeError("oracle BFS: some rows went missing")
+    return d, L
+
+
+def traverse(csr, dist: int, lo: int, hi: int, total_perm=None, total_inv=None):
+    """One RACE traversal step: distances, level histograms and the composed
+    permutation (same outputs as the reference's Traverse on [lo,hi))."""
+    n = csr.n
+    tp = _i32(np.arange(n) if total_perm is None else total_perm).copy()
+    ti = _i32(np.arange(n) if total_inv is None else total_inv).copy()
+    d, L = bfs(csr, dist, lo, hi, tp, ti)
+    lr = np.zeros(max(L, 1), np.int32); ln = np.zeros(max(L, 1), np.int32)
+    lib().orc_level_data(_i32(csr.row_ptr), tp, d, lo, hi, L, lr, ln)
+    lib().orc_level_permute(n, d, lo, hi, L, tp, ti)
+    return tp, ti, lr[:L], ln[:L], d
+
+
+def run_kernel(kernel: int, start: int, end: int, csr, x, b):
+    fn = {K_SPMV: "orc_spmv_range", K_SPMTV: "orc_spmtv_range", K_SYMMSPMV: "orc_symmspmv_range",
+          K_GS: "orc_gs_range", K_KACZ: "orc_kacz_range"}[kernel]
+    getattr(lib(), fn)(start, end, _i32(csr.row_ptr), _i32(csr.col), _f64(csr.val), x, b)
+
+
+def tree_arrays(nodes):
+    """Flatten a parsed zone tree (list of dicts with value/children/subblocks)."""
+    vs = np.zeros(len(nodes) + 1, np.int32)
+    cs = np.zeros(len(nodes) + 1, np.int32)
+    for i, z in enumerate(nodes):
+        vs[i + 1] = vs[i] + len(z["value"])
+        cs[i + 1] = cs[i] + len(z["children"])
+    val = np.array([v for z in nodes for v in z["value"]] or [0], np.int32)
+    ch = np.array([c for z in nodes for c in z["children"]] or [0], np.int32)
+    sb = np.array([z["subblocks"] for z in nodes], np.int32)
+    return vs, val, cs, ch, sb
+
+
+def exec_tree(nodes, block_per_thread: int, serial_part, kernel: int, rev: bool, pcsr, x, b):
+    """Run `kernel` over the zone tree sequentially in RACE's execution order."""
+    vs, val, cs, ch, sb = tree_arrays(nodes)
+    lib().orc_exec_tree(len(nodes), vs, val, cs, ch, sb, block_per_thread, int(serial_part[0]),
+                        int(serial_part[1]), kernel, int(rev), _i32(pcsr.row_ptr), _i32(pcsr.col),
+                        _f64(pcsr.val), x, b)
+
+
+def mpk_plain(csr, x0, p: int):
+    x = np.zeros((p + 1) * csr.n)
+    x[: csr.n] = x0
+    lib().orc_mpk_plain(csr.n, p, _i32(csr.row_ptr), _i32(csr.col), _f64(csr.val), x)
+    return x.reshape(p + 1, csr.n)
+
+
+def mpk_groups(p: int, nrow: int, nnz: int, cache_bytes: float, safety: float, cutoff: int, level_ptr, level_nnz):
+    L = len(level_nnz)
+    gp = np.zeros(L + 2, np.int32); ur = np.zeros(L + 2, np.int32); dr = np.zeros(L + 2, np.int32)
+    ng = lib().orc_mpk_groups(p, nrow, nnz, float(cache_bytes), float(safety), cutoff, L, _i32(level_ptr),
+                              _i32(level_nnz), gp, ur, dr)
+    if ng < 0:
+        return None
+    return gp[: ng + 1].copy(), ur[:ng].copy(), dr[:ng].copy()
+
+
+def mpk_wavefront(pcsr, x0, p: int, group_ptr, unlock_row, danger_row, nthreads: int):
+    """Run the reference's level-group wavefront on OpenMP threads (the CPU
+    baseline). The OpenMP team size must equal `nthreads`."""
+    ng = len(group_ptr) - 1
+    uc = np.zeros(ng, np.int32)
+    lib().orc_mpk_unlock_ctr(ng, _i32(group_ptr), _i32(unlock_row), nthreads, uc)
+    x = np.zeros((p + 1) * pcsr.n)
+    x[: pcsr.n] = x0
+    lib().orc_mpk_wavefront(pcsr.n, p, ng, _i32(group_ptr), _i32(unlock_row), _i32(danger_row), uc,
+                            _i32(pcsr.row_ptr), _i32(pcsr.col), _f64(pcsr.val), x)
+    return x.reshape(p + 1, pcsr.n)
