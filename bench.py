@@ -1,0 +1,333 @@
+"""Benchmark of the level-blocked matrix-power kernel (RACE MPK) on GB300.
+
+Workload (one GPU): y_k = A^k x for k = 1..8 on the 27-point stencil of a
+128^3 grid (n = 2,097,152, nnz = 55,742,968; the HPCG-128 shape the reference
+publishes MPK numbers for), FP64 values, permuted with RACE's MPK ordering
+and level groups (cacheSize 100 MB, safety 2). Synthetic data: off-diagonals
+U[-1,0) mirrored, diagonal = sum|off| + 1, x ~ U[-1,1] (seeded).
+
+Metric: effective GB/s = p * (nnz*12 + 4(n+1) + 8n + 8n) bytes per call
+divided by the time (the FP64 CRS SpMV traffic model the reference's
+published GFlop/s convert to). The matrix (669 MB) is larger than the L2,
+so no flush is needed between iterations.
+
+--impl reference times the reference algorithm on the host cores instead:
+the C restatement of RACE's level-group wavefront executor on OpenMP
+threads (oracle/race_oracle.c), since the reference library itself cannot be
+built on the GPU host.
+
+N > 1 GPUs (torchrun): every rank runs an independent replica of the same
+workload (the reference's MPK has no multi-GPU path); value = total effective
+bytes over all ranks / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "MPK/SymmGS effective GB/s & % HBM peak, mixed vs FP64 at 1e-10 rel err"
+GRID = 128
+POWER = 8
+CACHE_BYTES = 100e6
+# Published RACE MPK p=8 on HPCG-128 (the same shape), best CPU result in the
+# reference's perf data: AMD Rome 49.85 GF/s = 317.9 GB/s effective
+# (examples/matrixPower_perf_test/21_Jan_2021_rome1_nps1/mtxPower.csv:2131).
+PUBLISHED_GBS = 317.9
+
+
+def spmv_bytes(n: int, nnz: int, val_bytes: int = 8) -> int:
+    return nnz * (val_bytes + 4) + 4 * (n + 1) + 8 * n + 8 * n
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except OSError:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def build_workload():
+    from race_gb300 import matgen
+    A = matgen.stencil3d_27pt(GRID)
+    return A
+
+
+def run_reference(args, rank, world):
+    """RACE's level-group wavefront on the host cores (oracle port)."""
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+    from race_gb300 import matgen
+    A = build_workload()
+    threads = os.cpu_count() or 1
+    perm, inv, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+    P = A.permuted(perm, inv)
+    lp = np.concatenate([[0], np.cumsum(lr)]).astype(np.int32)
+    gp, ur, dr = orc.mpk_groups(POWER, A.n, A.nnz, CACHE_BYTES, 2.0, 50, lp, ln)
+    x0 = matgen.uniform_vector(A.n, 0)
+    for _ in range(args.warmup):
+        orc.mpk_wavefront(P, x0, POWER, gp, ur, dr, threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        orc.mpk_wavefront(P, x0, POWER, gp, ur, dr, threads)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    eff = POWER * spmv_bytes(A.n, A.nnz)
+    gbs = eff / t / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": gbs / PUBLISHED_GBS, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"MPK p={POWER}, 27-point stencil {GRID}^3, FP64, RACE level groups "
+                               f"(cacheSize {CACHE_BYTES / 1e6:.0f} MB)", "parallelism": "host cores"},
+        "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full MPK calls (median), RACE wavefront restated in C, "
+                                   f"OpenMP {threads} threads"},
+        "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the CPU baseline sample")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from race_gb300 import interface as ri
+    from race_gb300 import matgen
+
+    A = build_workload()
+    n, nnz = A.n, A.nnz
+    stream = torch.cuda.current_stream()
+    rc = ri.Interface(n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True, stream=stream)
+    assert rc.RACEColor(POWER, CACHE_BYTES) == 0
+    perm, inv = rc.getPerm(), rc.getInvPerm()
+    P = A.permuted(perm, inv)
+    x0 = matgen.uniform_vector(n, 0)
+    dm64 = ri.DeviceCsr.from_csr(P, "cuda", torch.float64)
+    dm32 = ri.DeviceCsr(n, dm64.row_ptr, dm64.col, dm64.val.to(torch.float32))
+    x64 = torch.zeros((POWER + 1) * n, dtype=torch.float64, device="cuda")
+    x64[:n] = torch.tensor(x0, device="cuda")
+    x32 = x64.clone()
+    f64 = rc.registerFunction(ri.MPK, ri.Operands(dm64, x64), power=POWER)
+    f32 = rc.registerFunction(ri.MPK, ri.Operands(dm32, x32), power=POWER)
+    assert f64 >= 0 and f32 >= 0
+
+    # correctness on the benchmark inputs: FP64 MPK == plain fma SpMV chain
+    assert rc.executeFunction(f64) == 0
+    y = torch.zeros_like(x64)
+    y[:n] = x64[:n]
+    for k in range(1, POWER + 1):
+        rc.spmv_plain(dm64, y[(k - 1) * n:k * n], y[k * n:(k + 1) * n])
+    assert rc.executeFunction(f32) == 0
+    torch.cuda.synchronize()
+    exact = bool(torch.equal(x64, y))
+    ref_last = y[POWER * n:]
+    rel32 = float(((x32[POWER * n:] - ref_last).abs().max() / ref_last.abs().max()).item())
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn, steps):
+        for _ in range(args.warmup):
+            fn()
+        barrier()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            fn()
+        ev1.record(stream)
+        barrier()
+        ms = ev0.elapsed_time(ev1) / steps
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    def mpk64():
+        rc.executeFunctionAsync(f64)
+
+    def mpk32():
+        rc.executeFunctionAsync(f32)
+
+    def plain64():
+        for k in range(1, POWER + 1):
+            rc.spmv_plain(dm64, x64[(k - 1) * n:k * n], x64[k * n:(k + 1) * n])
+
+    with ClockSampler(local) as clk:
+        ms64 = timed(mpk64, args.steps)
+    clocks = clk.summary()
+    assert rc.getStatus() == 0
+    ms32 = timed(mpk32, args.steps)
+    assert rc.getStatus() == 0
+    ms_plain = timed(plain64, args.steps)
+
+    # end to end through the public API: pinned host x0 -> device, MPK,
+    # all p powers back to pinned host memory, every step
+    h_in = torch.tensor(x0, dtype=torch.float64).pin_memory()
+    h_out = torch.empty(POWER * n, dtype=torch.float64).pin_memory()
+
+    def e2e():
+        x64[:n].copy_(h_in, non_blocking=True)
+        rc.executeFunctionAsync(f64)
+        h_out.copy_(x64[n:], non_blocking=True)
+
+    ms_e2e = timed(e2e, args.steps)
+    assert rc.getStatus() == 0
+
+    eff_bytes = POWER * spmv_bytes(n, nnz)
+    compulsory = (nnz * 12 + 4 * (n + 1)) + 8 * n + POWER * 8 * n
+    gbs = eff_bytes / (ms64 * 1e-3) / 1e9 * world
+    peak, peak_kind = measured_peaks()
+    achieved = compulsory / (ms64 * 1e-3) / 1e9
+
+    traffic = None
+    tpath = ROOT / "profiles" / "mpk_traffic.json"
+    if tpath.exists():
+        traffic = json.loads(tpath.read_text()).get("dram_bytes_per_launch")
+
+    cpu = cpu_baseline(A, P, x0, args.cpu_seconds) if rank == 0 else None
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": gbs / PUBLISHED_GBS, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"MPK p={POWER}, 27-point stencil {GRID}^3 (n={n}, nnz={nnz}), FP64 values, "
+                                   f"RACE level groups (cacheSize {CACHE_BYTES / 1e6:.0f} MB, safety 2)",
+                       "l2": "inputs larger than L2 (669 MB matrix), no flush", "parallelism": f"replicas x{world}"},
+            "e2e": {"value": eff_bytes / (ms_e2e * 1e-3) / 1e9 * world, "unit": "GB/s",
+                    "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": POWER * 8 * n},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "note": f"achieved = compulsory bytes ({compulsory}) per launch / launch time; "
+                                 f"peak {peak_kind}"},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "fp64_bit_exact_vs_plain_chain": exact,
+            "mixed_f32": {"ms_per_step": ms32, "effective_gbs": eff_bytes / (ms32 * 1e-3) / 1e9,
+                          "rel_err_vs_f64": rel32, "meets_1e-10": rel32 <= 1e-10},
+            "plain_f64": {"ms_per_step": ms_plain, "effective_gbs": eff_bytes / (ms_plain * 1e-3) / 1e9,
+                          "hbm_frac": eff_bytes / (ms_plain * 1e-3) / 1e9 / peak},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(A, P, x0, budget_s: float):
+    """The reference algorithm (RACE wavefront, oracle port) on all host
+    cores, on full MPK calls of the same workload until the budget is spent."""
+    from oracle import oracle as orc
+    threads = os.cpu_count() or 1
+    perm, inv, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+    lp = np.concatenate([[0], np.cumsum(lr)]).astype(np.int32)
+    gp, ur, dr = orc.mpk_groups(POWER, A.n, A.nnz, CACHE_BYTES, 2.0, 50, lp, ln)
+    orc.mpk_wavefront(P, x0, POWER, gp, ur, dr, threads)
+    times = []
+    t_start = time.perf_counter()
+    while time.perf_counter() - t_start < budget_s and len(times) < 50:
+        t0 = time.perf_counter()
+        orc.mpk_wavefront(P, x0, POWER, gp, ur, dr, threads)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    return {"value": POWER * spmv_bytes(A.n, A.nnz) / t / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"{len(times)} full MPK p={POWER} calls (median), RACE level-group wavefront "
+                      f"restated in C on {threads} OpenMP threads"}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,165 @@
+/* race_gb300.h -- C ABI of the GB300-native RACE execution engine.
+ *
+ * The entry points mirror RACE::Interface (include/interface.h in the
+ * reference) one to one; every function returns a RACE_error code and no
+ * C++ exception crosses the boundary. Matrices are CRS with int32 indices.
+ * Arrays passed as `host` are read during the call and not retained;
+ * arrays passed as `dev` are device pointers owned by the caller that must
+ * stay valid while a registered function that uses them can run.
+ *
+ * Threading: one host thread drives a handle at a time. Work is enqueued on
+ * the handle's CUDA stream (race_set_stream); calls that return results to
+ * the host synchronise that stream.
+ */
+#ifndef RACE_GB300_H
+#define RACE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* RACE_error, include/error.h:29-41 of the reference, plus engine codes. */
+enum {
+    RACE_SUCCESS = 0,
+    RACE_ERR_INVALID_ARG = 1,
+    RACE_ERR_MATRIX_SYMM = 2,
+    RACE_ERR_D2_COLOR = 3,
+    RACE_ERR_D1_COLOR = 4,
+    RACE_ERR_GRAPH_TRAVERSAL = 5,
+    RACE_ERR_INCOMPATIBILITY = 6,
+    RACE_ERR_HWLOC = 7,
+    RACE_ERR_PIN = 8,
+    RACE_ERR_INTERNAL = 9,
+    RACE_ERR_NOT_IMPLEMENTED = 10,
+    RACE_ERR_CUDA = 100,    /* a CUDA runtime call failed */
+    RACE_ERR_TIMEOUT = 101  /* a device wait hit its iteration limit */
+};
+
+/* RACE::dist, include/type.h:31-35 */
+enum { RACE_DIST_ONE = 1, RACE_DIST_TWO = 2, RACE_DIST_POWER = 3 };
+/* RACE::d2Method, RACE::LBTarget, include/type.h:37-46 */
+enum { RACE_TWO_BLOCK = 0, RACE_THREE_BLOCK = 1 };
+enum { RACE_LB_ROW = 0, RACE_LB_NNZ = 1 };
+
+/* Built-in device kernels (the example kernels of the reference,
+ * examples/src/helpers/kernels.cpp). */
+enum {
+    RACE_K_SPMV = 0,      /* b = A x                                          */
+    RACE_K_SPMTV = 1,     /* b += A^T x (scatter; needs distance-2)           */
+    RACE_K_SYMMSPMV = 2,  /* b += A x from the upper triangle, diag first     */
+    RACE_K_GS = 3,        /* x <- Gauss-Seidel step for A x = b, diag first   */
+    RACE_K_KACZ = 4,      /* x <- Kaczmarz projection step (needs distance-2) */
+    RACE_K_MPK = 5        /* x_k = A x_{k-1}, k = 1..power, power-major x     */
+};
+
+/* Value storage of a registered operand set. */
+enum { RACE_VAL_F64 = 0, RACE_VAL_F32 = 1, RACE_VAL_BF16 = 2 };
+
+typedef struct race_engine race_engine;
+
+/* Device operands of a built-in kernel (the `args` of registerFunction). */
+typedef struct {
+    int n;                  /* rows of the (permuted) matrix */
+    const int *rowPtr;      /* dev, n+1 */
+    const int *col;         /* dev, nnz */
+    const void *val;        /* dev, nnz, type val_type */
+    int val_type;           /* RACE_VAL_* */
+    double *x;              /* dev; MPK: (power+1)*n, power-major */
+    double *b;              /* dev; n (unused by MPK) */
+} race_operands;
+
+/* Pre-processing knobs; the reference reads them from the environment
+ * (RACE_EFFICIENCY, RACE_THREADS, RACE_CACHE_VIOLATION_CUTOFF[_DEFAULT],
+ * RACE_MAX_RECURSION_STAGES). race_params_from_env fills them the same way. */
+typedef struct {
+    int n_eff;
+    double eff[16];          /* eff[0] default threshold (40), eff[k] stage k */
+    int n_lvl_threads;
+    int lvl_threads[16];
+    int cache_violation_cutoff;
+} race_params;
+
+int race_params_from_env(race_params *p);
+
+/* Interface::Interface (interface.h:124, interface.cpp:33-36). rowPtr/col are
+ * host arrays; symm_hint=0 symmetrises the pattern first (graph.cpp:47-142).
+ * initPerm/initInvPerm may be NULL. params may be NULL (read the environment). */
+int race_create(race_engine **out, int nrow, int nthreads, int dist, const int *rowPtr_host, const int *col_host,
+                int symm_hint, const int *initPerm_host, const int *initInvPerm_host, int d2type, int lbtarget,
+                const race_params *params);
+/* Interface::~Interface (interface.cpp:38-60) */
+int race_destroy(race_engine *e);
+
+/* Work is enqueued on this stream (default: the legacy default stream). */
+int race_set_stream(race_engine *e, void *cuda_stream);
+
+/* Interface::RACEColor() (interface.h:128, interface.cpp:260-301) */
+int race_color(race_engine *e);
+/* Interface::RACEColor(highestPower, cacheSize, safetyFactor, mtxType,
+ * highestSubPower) (interface.h:127, interface.cpp:205-257); cacheSize in bytes. */
+int race_power_prepare(race_engine *e, int highestPower, double cacheSize, double safetyFactor, const char *mtxType,
+                       int highestSubPower);
+
+/* Interface::getPerm / getInvPerm (interface.cpp:333-383): copy into
+ * caller-provided host arrays of nrow ints. */
+int race_get_perm(race_engine *e, int *perm_host, int *invPerm_host);
+/* Interface::getNumThreads / getEfficiency / getMaxStageDepth (interface.cpp:304-331, 385) */
+int race_get_num_threads(race_engine *e, int *out);
+int race_get_efficiency(race_engine *e, double *out);
+int race_get_max_stage_depth(race_engine *e, int *out);
+/* Zone tree in the flat layout documented in race_gb300/csrc/coloring.h
+ * (no counterpart in the reference API; printZoneTree prints the same data,
+ * interface.cpp:328-331). *len receives the length; data is written when
+ * cap is large enough. */
+int race_get_zone_tree(race_engine *e, int *buf, int cap, int *len);
+/* Flattened execution phases: phasePtr (numPhases+1) and leaf ranges. */
+int race_get_phases(race_engine *e, int rev, int *phasePtr, int *leafLo, int *leafHi, int cap, int *numPhases,
+                    int *numLeaves);
+/* MPK level groups (consolidated levelPtr of the reference's MPLeaf::lp,
+ * matrixPowerRecursive.h:27-62), *len = groups+1. */
+int race_get_power_groups(race_engine *e, int *buf, int cap, int *len);
+
+/* Interface::registerFunction (interface.h:149-157, interface.cpp:391-485)
+ * with a built-in device kernel in place of a host callback; `power` is used
+ * by RACE_K_MPK. */
+int race_register_function(race_engine *e, int kernel, const race_operands *ops, int power, int *func_id);
+/* Interface::executeFunction (interface.h:167, interface.cpp:541-572):
+ * enqueues the kernel on the engine's stream, waits for it and returns
+ * RACE_ERR_TIMEOUT if a device wait gave up. */
+int race_execute_function(race_engine *e, int func_id, int rev);
+/* Same work without waiting (stream-ordered, like a CUDA library call);
+ * race_get_status later synchronises and reports the device status word of
+ * the last launch. No counterpart in the reference, whose executor is
+ * synchronous. */
+int race_execute_function_async(race_engine *e, int func_id, int rev);
+int race_get_status(race_engine *e);
+/* Interface::setPower / getPower (interface.cpp:574-590) */
+int race_set_power(race_engine *e, int func_id, int power);
+int race_get_power(race_engine *e, int func_id, int *out);
+
+/* Plain FP64 CRS SpMV b = A x (no schedule; the traditional baseline the
+ * reference compares MPK against, kernels.cpp:90-105). */
+int race_spmv_plain(race_engine *e, int n, const int *rowPtr_dev, const int *col_dev, const double *val_dev,
+                    const double *x_dev, double *b_dev);
+
+/* Host-only helpers (no GPU needed), exposed for inspection and tests:
+ * the level load balancer (LB::balance, lb.cpp:188-771) on given level data,
+ * out = [nScale, scale..., totalBlocks, zonePtr(totalBlocks+1)...,
+ *        totalSubBlocks, subZonePtr(totalSubBlocks+1)..., numBlocks(totalBlocks)...];
+ * and the phase flattening of a zone tree given in the flat layout of
+ * race_get_zone_tree. Both return the written length (or the needed length
+ * when cap is too small) through *len. */
+int race_lb_balance(const int *levelRow, const int *levelNnz, int totalLevel, int nthreads, double eff, int dist,
+                    int d2type, int lbtarget, int base, int *out, int cap, int *len);
+int race_flatten_zone_tree(const int *tree, int treeLen, int dist, int d2type, int rev, int serialLo, int serialHi,
+                           int *phasePtr, int *leafLo, int *leafHi, int cap, int *numPhases, int *numLeaves);
+
+/* Last error message of this engine (NUL-terminated, owned by the engine). */
+const char *race_last_error(race_engine *e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

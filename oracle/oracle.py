@@ -58,7 +58,7 @@ def lib():
         L.orc_mpk_groups.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_double, C.c_double, C.c_int, C.c_int,
                                      IP, IP, IP, IP, IP]
         L.orc_mpk_unlock_ctr.argtypes = [C.c_int, IP, IP, C.c_int, IP]
-        L.orc_mpk_wavefront.argtypes = [C.c_int, C.c_int, C.c_int, IP, IP, IP, IP, IP, IP, DP, DP]
+        L.orc_mpk_wavefront.argtypes = [C.c_int, C.c_int, C.c_int, IP, IP, IP, C.c_int, IP, IP, DP, DP]
         _lib = L
     return _lib
 
@@ -141,13 +141,11 @@ def mpk_groups(p: int, nrow: int, nnz: int, cache_bytes: float, safety: float, c
 
 
 def mpk_wavefront(pcsr, x0, p: int, group_ptr, unlock_row, danger_row, nthreads: int):
-    """Run the reference's level-group wavefront on OpenMP threads (the CPU
-    baseline). The OpenMP team size must equal `nthreads`."""
+    """Run the reference's level-group wavefront on `nthreads` OpenMP threads
+    (the CPU baseline)."""
     ng = len(group_ptr) - 1
-    uc = np.zeros(ng, np.int32)
-    lib().orc_mpk_unlock_ctr(ng, _i32(group_ptr), _i32(unlock_row), nthreads, uc)
     x = np.zeros((p + 1) * pcsr.n)
     x[: pcsr.n] = x0
-    lib().orc_mpk_wavefront(pcsr.n, p, ng, _i32(group_ptr), _i32(unlock_row), _i32(danger_row), uc,
+    lib().orc_mpk_wavefront(pcsr.n, p, ng, _i32(group_ptr), _i32(unlock_row), _i32(danger_row), int(nthreads),
                             _i32(pcsr.row_ptr), _i32(pcsr.col), _f64(pcsr.val), x)
     return x.reshape(p + 1, pcsr.n)

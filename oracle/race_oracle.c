@@ -392,16 +392,22 @@ void orc_mpk_unlock_ctr(int ngroups, const int *groupPtr, const int *unlockRow, 
  * rows from dangerRow on) after the next group's first rows at pow-1 are
  * done. Spins use a plain busy wait, as the reference does. */
 void orc_mpk_wavefront(int n, int p, int ngroups, const int *groupPtr, const int *unlockRow, const int *dangerRow,
-                       const int *unlockCtr, const int *rowPtr, const int *col, const double *val, double *x) {
+                       int nthreads, const int *rowPtr, const int *col, const double *val, double *x) {
     volatile int *lockCtr = (volatile int *)calloc((size_t)ngroups, sizeof(int));
     volatile int *lockTable = (volatile int *)calloc((size_t)ngroups * (size_t)p + 1, sizeof(int));
-#pragma omp parallel
+    int *unlockCtr = (int *)malloc(sizeof(int) * (size_t)(ngroups > 0 ? ngroups : 1));
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel num_threads(nthreads)
     {
         int nthr = 1, tid = 0;
 #ifdef _OPENMP
         nthr = omp_get_num_threads();
         tid = omp_get_thread_num();
 #endif
+        /* the unlock counters count the threads of the team that actually
+         * runs (findUnlockCtr uses the live team size, matrixPower.cpp:970) */
+#pragma omp single
+        orc_mpk_unlock_ctr(ngroups, groupPtr, unlockRow, nthr, unlockCtr);
         for (int level = 0; level < ngroups + p - 1; ++level) {
             for (int pow = 0; pow < p; ++pow) {
                 int L = level - pow;
@@ -452,4 +458,5 @@ void orc_mpk_wavefront(int n, int p, int ngroups, const int *groupPtr, const int
     }
     free((void *)lockCtr);
     free((void *)lockTable);
+    free(unlockCtr);
 }

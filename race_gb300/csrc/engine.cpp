@@ -1,0 +1,395 @@
+// Engine driver: pre-processing (coloring, matrix-power partition),
+// function registration and execution, and the C ABI of include/race_gb300.h.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "engine.h"
+
+namespace race {
+
+std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int power);
+void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power);
+int mpkStatus(Engine &e, MpkPlan &plan);
+void uploadPhases(Engine &e, int dir);
+void runSweep(Engine &e, int kernel, const race_operands &ops, bool rev);
+
+// Interface::RACEColor() (interface.cpp:260-301): level recursion over the
+// whole matrix, then the execution phases of both sweep directions.
+void Engine::color() {
+    if (dist == DIST_POWER) throw Error(RACE_ERR_INVALID_ARG, "coloring needs dist ONE or TWO");
+    LevelRecursion lr(
+        n, requested, dist, d2, lbTarget, params, [this](int lo, int hi) { return traverse(lo, hi, dist); },
+        [this](int lo, int hi) { return rangeNnz(lo, hi); });
+    lr.levelBalancing();
+    availableThreads = lr.availableThreads;
+    tree = std::make_unique<ZoneTree>(lr.tree);
+    for (int dir = 0; dir < 2; ++dir) {
+        phases[dir] = flattenZoneTree(*tree, dir == 1, n, n);
+        uploadPhases(*this, dir);
+    }
+    RACE_CUDA(cudaStreamSynchronize(stream));
+    colored = true;
+}
+
+// Interface::RACEColor(p, cacheSize, ...) (interface.cpp:205-257) for the
+// first stage of mtxPowerRecursive (matrixPowerRecursive.cpp:340-436):
+// BFS levels of the whole matrix, cache-violation check, level groups.
+void Engine::powerPrepare(int hp, double cacheSize, double safety, const std::string &mtxType, int subPow) {
+    if (subPow < 1) throw Error(RACE_ERR_INVALID_ARG, "highest sub power must be >= 1");
+    if (dist != DIST_POWER) throw Error(RACE_ERR_INVALID_ARG, "matrix power needs dist POWER");
+    if (mtxType != "N" && mtxType != "L" && mtxType != "U") throw Error(RACE_ERR_INVALID_ARG, "mtxType must be N, L or U");
+    highestPower = hp;
+    highestSubPower = subPow;
+    const int P = hp * subPow;
+    LevelData ld = traverse(0, n, DIST_POWER, mtxType);
+    const int L = ld.totalLevel;
+    levelPtr.assign(L + 1, 0);
+    for (int l = 0; l < L; ++l) levelPtr[l + 1] = levelPtr[l] + ld.levelRow[l];
+    // getBytePerNNZ / getElemUpperLimit (matrixPower.cpp:88-99, 134-140)
+    double nnzr = nnz / (double)n;
+    double bpn = (double)(((1 + P / nnzr) * sizeof(double) + (1 + 1 / nnzr) * sizeof(int)));
+    double cacheElem = cacheSize / bpn;
+    // stage-0 cut-off (matrixPowerRecursive.cpp:37-95)
+    int maxRec = params.maxRecStages >= 0 ? params.maxRecStages
+                                          : std::max(0, (int)(params.cacheViolationCutoff.size() - 1 + 1));
+    int cutoff = 50;
+    if (0 >= maxRec)
+        cutoff = INT_MAX;
+    else
+        cutoff = (0 < (int)params.cacheViolationCutoff.size() - 1) ? params.cacheViolationCutoff[1]
+                                                                    : params.cacheViolationCutoff[0];
+    int violated = 0;
+    for (int l = 0; l < L; ++l) {
+        double e = safety * (P + 1) * ld.levelNnz[l];
+        if (e > cacheElem && static_cast<int>(std::ceil(e / cacheElem)) > cutoff) ++violated;
+    }
+    if (violated > 1 && mtxType == "N")
+        throw Error(RACE_ERR_NOT_IMPLEMENTED,
+                    "levels exceed the cache budget beyond the cut-off (hopeless regions); recursive MPK "
+                    "partitioning is not built: raise cacheSize or RACE_CACHE_VIOLATION_CUTOFF");
+    // consolidatePartition without hopeless regions (matrixPower.cpp:685-883)
+    groupPtr.assign(1, levelPtr[0]);
+    unlockRow.assign(1, L > 0 ? levelPtr[std::min(1, L)] : 0);
+    dangerRow.clear();
+    double sumElem = 0;
+    for (int l = 0; l < L; ++l) {
+        double cur = safety * (P + 1) * ld.levelNnz[l];
+        sumElem += cur;
+        if (l > 0 && sumElem >= cacheElem) {
+            sumElem = cur;
+            groupPtr.push_back(levelPtr[l]);
+            dangerRow.push_back(levelPtr[l - 1]);
+            unlockRow.push_back(levelPtr[l + 1]);
+        }
+    }
+    groupPtr.push_back(levelPtr[L]);
+    dangerRow.push_back(levelPtr[L > 0 ? L - 1 : 0]);
+    powerReady = true;
+}
+
+int Engine::registerFunction(int kernel, const race_operands &ops, int power) {
+    if (ops.n != n) throw Error(RACE_ERR_INVALID_ARG, "operand rows differ from the engine's");
+    if (!ops.rowPtr || !ops.col || !ops.val) throw Error(RACE_ERR_INVALID_ARG, "missing matrix operand");
+    FuncEntry f;
+    f.kernel = kernel;
+    f.ops = ops;
+    f.power = power;
+    if (kernel == RACE_K_MPK) {
+        // interface.cpp:438-458
+        if (dist != DIST_POWER || !powerReady) throw Error(RACE_ERR_INVALID_ARG, "MPK needs RACEColor(power, ...) first");
+        if (power < 1) throw Error(RACE_ERR_INVALID_ARG, "power must be >= 1");
+        if (!ops.x) throw Error(RACE_ERR_INVALID_ARG, "missing x");
+        f.mpk = buildMpkPlan(*this, ops, power);
+    } else {
+        // interface.cpp:397-431
+        if (dist == DIST_POWER) throw Error(RACE_ERR_INVALID_ARG, "coloring kernels need dist ONE or TWO");
+        if (!colored) throw Error(RACE_ERR_INVALID_ARG, "RACEColor() first");
+        if (kernel < RACE_K_SPMV || kernel > RACE_K_KACZ) throw Error(RACE_ERR_INVALID_ARG, "unknown kernel");
+        if (!ops.x || !ops.b) throw Error(RACE_ERR_INVALID_ARG, "missing x or b");
+        if ((kernel == RACE_K_SPMTV || kernel == RACE_K_KACZ || kernel == RACE_K_SYMMSPMV) && dist != DIST_TWO)
+            throw Error(RACE_ERR_D2_COLOR, "scatter kernels need distance-2 coloring");
+    }
+    funcs.push_back(std::move(f));
+    return (int)funcs.size() - 1;
+}
+
+void Engine::launch(int id, bool rev) {
+    if (id < 0 || id >= (int)funcs.size()) throw Error(RACE_ERR_INVALID_ARG, "unknown function id");
+    FuncEntry &f = funcs[id];
+    if (f.kernel == RACE_K_MPK) {
+        runMpk(*this, *f.mpk, f.ops, f.power);
+        lastStatus = f.mpk->status.p;
+    } else {
+        runSweep(*this, f.kernel, f.ops, rev);
+        lastStatus = dStatus.p;
+    }
+}
+
+void Engine::checkStatus() {
+    int st = 0;
+    if (lastStatus) RACE_CUDA(cudaMemcpyAsync(&st, lastStatus, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    RACE_CUDA(cudaStreamSynchronize(stream));
+    if (st != DEV_OK) throw Error(RACE_ERR_TIMEOUT, "a device wait gave up (schedule dependency or grid barrier)");
+}
+
+void Engine::execute(int id, bool rev) {
+    launch(id, rev);
+    checkStatus();
+}
+
+}  // namespace race
+
+using race::Engine;
+using race::Error;
+
+struct race_engine {
+    std::unique_ptr<Engine> eng;
+    std::string err;
+};
+
+namespace {
+template <typename F>
+int guard(race_engine *h, F &&f) {
+    try {
+        f();
+        return RACE_SUCCESS;
+    } catch (const Error &ex) {
+        if (h) h->err = ex.what();
+        return ex.code;
+    } catch (const std::exception &ex) {
+        if (h) h->err = ex.what();
+        return RACE_ERR_INTERNAL;
+    }
+}
+race::Params toParams(const race_params *p) {
+    if (!p) return race::Params::fromEnv();
+    race::Params q;
+    q.effVec.assign(p->eff, p->eff + std::max(1, std::min(p->n_eff, 16)));
+    q.lvlThreads.assign(p->lvl_threads, p->lvl_threads + std::max(0, std::min(p->n_lvl_threads, 16)));
+    q.cacheViolationCutoffDefault = p->cache_violation_cutoff > 0 ? p->cache_violation_cutoff : 50;
+    q.cacheViolationCutoff.assign(1, q.cacheViolationCutoffDefault);
+    return q;
+}
+}  // namespace
+
+extern "C" {
+
+int race_params_from_env(race_params *p) {
+    if (!p) return RACE_ERR_INVALID_ARG;
+    race::Params q = race::Params::fromEnv();
+    memset(p, 0, sizeof(*p));
+    p->n_eff = (int)std::min<size_t>(q.effVec.size(), 16);
+    for (int i = 0; i < p->n_eff; ++i) p->eff[i] = q.effVec[i];
+    p->n_lvl_threads = (int)std::min<size_t>(q.lvlThreads.size(), 16);
+    for (int i = 0; i < p->n_lvl_threads; ++i) p->lvl_threads[i] = q.lvlThreads[i];
+    p->cache_violation_cutoff = q.cacheViolationCutoffDefault;
+    return RACE_SUCCESS;
+}
+
+int race_create(race_engine **out, int nrow, int nthreads, int dist, const int *rowPtr, const int *col, int symm_hint,
+                const int *initPerm, const int *initInvPerm, int d2type, int lbtarget, const race_params *params) {
+    if (!out) return RACE_ERR_INVALID_ARG;
+    *out = nullptr;
+    race_engine *h = new race_engine;
+    int rc = guard(h, [&] {
+        h->eng = std::make_unique<Engine>(nrow, nthreads, dist, rowPtr, col, symm_hint != 0, initPerm, initInvPerm,
+                                          d2type, lbtarget, toParams(params));
+    });
+    if (rc != RACE_SUCCESS) {
+        fprintf(stderr, "[RACE-GB300] race_create: %s\n", h->err.c_str());
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return RACE_SUCCESS;
+}
+
+int race_destroy(race_engine *e) {
+    delete e;
+    return RACE_SUCCESS;
+}
+
+int race_set_stream(race_engine *e, void *s) {
+    if (!e) return RACE_ERR_INVALID_ARG;
+    e->eng->stream = (cudaStream_t)s;
+    return RACE_SUCCESS;
+}
+
+int race_color(race_engine *e) {
+    if (!e) return RACE_ERR_INVALID_ARG;
+    return guard(e, [&] { e->eng->color(); });
+}
+
+int race_power_prepare(race_engine *e, int hp, double cacheSize, double safety, const char *mtxType, int subPow) {
+    if (!e) return RACE_ERR_INVALID_ARG;
+    return guard(e, [&] { e->eng->powerPrepare(hp, cacheSize, safety, mtxType ? mtxType : "N", subPow); });
+}
+
+int race_get_perm(race_engine *e, int *perm, int *invPerm) {
+    if (!e) return RACE_ERR_INVALID_ARG;
+    if (perm) memcpy(perm, e->eng->hPerm.data(), sizeof(int) * e->eng->n);
+    if (invPerm) memcpy(invPerm, e->eng->hInvPerm.data(), sizeof(int) * e->eng->n);
+    return RACE_SUCCESS;
+}
+
+int race_get_num_threads(race_engine *e, int *out) {
+    if (!e || !out) return RACE_ERR_INVALID_ARG;
+    *out = e->eng->availableThreads;
+    return RACE_SUCCESS;
+}
+
+int race_get_efficiency(race_engine *e, double *out) {
+    if (!e || !out) return RACE_ERR_INVALID_ARG;
+    Engine &g = *e->eng;
+    if (g.dist == race::DIST_POWER || !g.tree) return RACE_ERR_INVALID_ARG;
+    // interface.cpp:316-319
+    double effThreads = ((double)g.n / (double)g.tree->nodes[0].effRowZ);
+    *out = effThreads / g.requested;
+    return RACE_SUCCESS;
+}
+
+int race_get_max_stage_depth(race_engine *e, int *out) {
+    if (!e || !out || !e->eng->tree) return RACE_ERR_INVALID_ARG;
+    *out = e->eng->tree->maxStage;
+    return RACE_SUCCESS;
+}
+
+int race_get_zone_tree(race_engine *e, int *buf, int cap, int *len) {
+    if (!e || !len || !e->eng->tree) return RACE_ERR_INVALID_ARG;
+    std::vector<int> v = race::serializeZoneTree(*e->eng->tree);
+    *len = (int)v.size();
+    if (buf && cap >= (int)v.size()) memcpy(buf, v.data(), sizeof(int) * v.size());
+    return RACE_SUCCESS;
+}
+
+int race_get_phases(race_engine *e, int rev, int *phasePtr, int *leafLo, int *leafHi, int cap, int *numPhases,
+                    int *numLeaves) {
+    if (!e || !numPhases || !numLeaves || !e->eng->colored) return RACE_ERR_INVALID_ARG;
+    const race::PhaseTable &pt = e->eng->phases[rev ? 1 : 0];
+    *numPhases = pt.numPhases();
+    *numLeaves = (int)pt.leafLo.size();
+    if (phasePtr && leafLo && leafHi && cap >= *numLeaves && cap >= *numPhases + 1) {
+        memcpy(phasePtr, pt.phasePtr.data(), sizeof(int) * pt.phasePtr.size());
+        memcpy(leafLo, pt.leafLo.data(), sizeof(int) * pt.leafLo.size());
+        memcpy(leafHi, pt.leafHi.data(), sizeof(int) * pt.leafHi.size());
+    }
+    return RACE_SUCCESS;
+}
+
+int race_get_power_groups(race_engine *e, int *buf, int cap, int *len) {
+    if (!e || !len || !e->eng->powerReady) return RACE_ERR_INVALID_ARG;
+    const std::vector<int> &g = e->eng->groupPtr;
+    *len = (int)g.size();
+    if (buf && cap >= (int)g.size()) memcpy(buf, g.data(), sizeof(int) * g.size());
+    return RACE_SUCCESS;
+}
+
+int race_register_function(race_engine *e, int kernel, const race_operands *ops, int power, int *func_id) {
+    if (!e || !ops || !func_id) return RACE_ERR_INVALID_ARG;
+    return guard(e, [&] { *func_id = e->eng->registerFunction(kernel, *ops, power); });
+}
+
+int race_execute_function(race_engine *e, int func_id, int rev) {
+    if (!e) return RACE_ERR_INVALID_ARG;
+    return guard(e, [&] { e->eng->execute(func_id, rev != 0); });
+}
+
+int race_execute_function_async(race_engine *e, int func_id, int rev) {
+    if (!e) return RACE_ERR_INVALID_ARG;
+    return guard(e, [&] { e->eng->launch(func_id, rev != 0); });
+}
+
+int race_get_status(race_engine *e) {
+    if (!e) return RACE_ERR_INVALID_ARG;
+    return guard(e, [&] { e->eng->checkStatus(); });
+}
+
+int race_set_power(race_engine *e, int func_id, int power) {
+    if (!e || func_id < 0 || func_id >= (int)e->eng->funcs.size()) return RACE_ERR_INVALID_ARG;
+    return guard(e, [&] {
+        race::FuncEntry &f = e->eng->funcs[func_id];
+        if (f.kernel == RACE_K_MPK && power != f.power) f.mpk = race::buildMpkPlan(*e->eng, f.ops, power);
+        f.power = power;
+    });
+}
+
+int race_get_power(race_engine *e, int func_id, int *out) {
+    if (!e || !out || func_id < 0 || func_id >= (int)e->eng->funcs.size()) return RACE_ERR_INVALID_ARG;
+    *out = e->eng->funcs[func_id].power;
+    return RACE_SUCCESS;
+}
+
+int race_spmv_plain(race_engine *e, int n, const int *rowPtr, const int *col, const double *val, const double *x,
+                    double *b) {
+    if (!e || !rowPtr || !col || !val || !x || !b || n < 0) return RACE_ERR_INVALID_ARG;
+    return guard(e, [&] { e->eng->spmvPlain(n, rowPtr, col, val, x, b); });
+}
+
+int race_lb_balance(const int *levelRow, const int *levelNnz, int totalLevel, int nthreads, double eff, int dist,
+                    int d2type, int lbtarget, int base, int *out, int cap, int *len) {
+    if (!levelRow || !levelNnz || totalLevel < 0 || !len) return RACE_ERR_INVALID_ARG;
+    return guard(nullptr, [&] {
+        race::LevelData ld;
+        ld.totalLevel = totalLevel;
+        ld.levelRow.assign(levelRow, levelRow + totalLevel);
+        ld.levelNnz.assign(levelNnz, levelNnz + totalLevel);
+        for (int i = 0; i < totalLevel; ++i) {
+            ld.nrow += levelRow[i];
+            ld.nnz += levelNnz[i];
+        }
+        race::LBResult r = race::lbBalance(ld, nthreads, eff, dist, d2type, lbtarget, base);
+        std::vector<int> v;
+        v.push_back((int)r.scale.size());
+        v.insert(v.end(), r.scale.begin(), r.scale.end());
+        v.push_back((int)r.numBlocks.size());
+        v.insert(v.end(), r.zonePtr.begin(), r.zonePtr.end());
+        v.push_back((int)r.subZonePtr.size() - 1);
+        v.insert(v.end(), r.subZonePtr.begin(), r.subZonePtr.end());
+        v.insert(v.end(), r.numBlocks.begin(), r.numBlocks.end());
+        *len = (int)v.size();
+        if (out && cap >= (int)v.size()) memcpy(out, v.data(), sizeof(int) * v.size());
+    });
+}
+
+int race_flatten_zone_tree(const int *tree, int treeLen, int dist, int d2type, int rev, int serialLo, int serialHi,
+                           int *phasePtr, int *leafLo, int *leafHi, int cap, int *numPhases, int *numLeaves) {
+    if (!tree || treeLen < 1 || !numPhases || !numLeaves) return RACE_ERR_INVALID_ARG;
+    return guard(nullptr, [&] {
+        race::ZoneTree t(dist, d2type, race::LB_NNZ);
+        int k = 1;
+        auto take = [&]() {
+            if (k >= treeLen) throw Error(RACE_ERR_INVALID_ARG, "truncated zone tree");
+            return tree[k++];
+        };
+        for (int i = 0, nn = tree[0]; i < nn; ++i) {
+            race::ZoneNode z;
+            z.nthreadsZ = take();
+            z.idealNthreadsZ = take();
+            z.totalSubBlocks = take();
+            z.parentZ = take();
+            z.effRowZ = take();
+            z.stage = take();
+            z.reachedLimit = take() != 0;
+            z.valueZ.resize(take());
+            for (auto &v : z.valueZ) v = take();
+            z.children.resize(take());
+            for (auto &c : z.children) c = take();
+            t.nodes.push_back(z);
+        }
+        race::PhaseTable pt = race::flattenZoneTree(t, rev != 0, serialLo, serialHi);
+        *numPhases = pt.numPhases();
+        *numLeaves = (int)pt.leafLo.size();
+        if (phasePtr && leafLo && leafHi && cap >= *numLeaves && cap >= *numPhases + 1) {
+            memcpy(phasePtr, pt.phasePtr.data(), sizeof(int) * pt.phasePtr.size());
+            memcpy(leafLo, pt.leafLo.data(), sizeof(int) * pt.leafLo.size());
+            memcpy(leafHi, pt.leafHi.data(), sizeof(int) * pt.leafHi.size());
+        }
+    });
+}
+
+const char *race_last_error(race_engine *e) { return e ? e->err.c_str() : "null engine"; }
+
+}  // extern "C"

@@ -1,0 +1,96 @@
+// Engine state behind one race_engine handle.
+#pragma once
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "coloring.h"
+#include "common.cuh"
+#include "lb.h"
+
+namespace race {
+
+// Device copy of a phase table for the persistent sweep kernel.
+struct DevPhases {
+    int numPhases = 0, numLeaves = 0, maxLeaves = 0;
+    DevBuf<int> phasePtr, leafLo, leafHi;
+};
+
+// Tiles of a matrix-power operand set: contiguous row ranges whose
+// non-zeros fit the kernel's shared-memory stage, in RACE's wavefront order,
+// with the last tile each one depends on.
+struct MpkPlan {
+    int numTiles = 0;
+    int power = 0;
+    int numItems = 0;           // power * numTiles
+    DevBuf<int> tileRow;        // numTiles+1 row offsets
+    DevBuf<int> depHi;          // numTiles: highest tile holding a column of the tile
+    DevBuf<int> itemTile;       // numItems: tile of each work item, wavefront order
+    DevBuf<unsigned char> itemPow;  // numItems: power (0-based) of each work item
+    DevBuf<int> flags;          // power * numTiles completion flags
+    DevBuf<int> watermark;      // power: completed prefix of tiles
+    DevBuf<int> ticket;         // 1: next work item
+    DevBuf<int> status;         // 1: device status word
+    int maxTileNnz = 0;
+};
+
+struct FuncEntry {
+    int kernel = 0;
+    race_operands ops{};
+    int power = 1;
+    std::unique_ptr<MpkPlan> mpk;
+};
+
+class Engine {
+  public:
+    Engine(int nrow, int nthreads, int dist, const int *rowPtr, const int *col, bool symmHint, const int *initPerm,
+           const int *initInvPerm, int d2, int lbTarget, const Params &params);
+    ~Engine();
+
+    void color();
+    void powerPrepare(int highestPower, double cacheSize, double safety, const std::string &mtxType, int subPower);
+
+    // One traversal of [lo,hi) of the current permuted space on the GPU.
+    LevelData traverse(int lo, int hi, int mode, const std::string &mtxType = "N");
+    long long rangeNnz(int lo, int hi) const;
+
+    int registerFunction(int kernel, const race_operands &ops, int power);
+    void execute(int id, bool rev);
+    void launch(int id, bool rev);
+    void checkStatus();
+    int *lastStatus = nullptr;  // device status word of the last launch
+    void spmvPlain(int n, const int *rowPtr, const int *col, const double *val, const double *x, double *b);
+
+    int n = 0;
+    long long nnz = 0;          // of the traversal graph (symmetrised pattern)
+    int dist = 1, requested = 1, d2 = 0, lbTarget = 1;
+    Params params;
+    cudaStream_t stream = 0;
+    std::string lastError;
+
+    std::vector<int> hRowPtr, hCol;  // traversal graph (host)
+    std::vector<int> hPerm, hInvPerm;
+    DevBuf<int> dRowPtr, dCol, dPerm, dInvPerm;
+
+    // traversal scratch
+    DevBuf<int> dDist, dStamp, dQ0, dQ1, dCtr, dLevelRow, dLevelNnz, dKeys, dVals, dKeysOut, dValsOut, dTmp;
+    DevBuf<unsigned char> dCubTemp;
+    int stamp = 0;
+
+    // coloring results
+    std::unique_ptr<ZoneTree> tree;
+    int availableThreads = 0;
+    bool colored = false;
+    PhaseTable phases[2];
+    DevPhases dPhases[2];
+
+    // power results
+    bool powerReady = false;
+    int highestPower = 1, highestSubPower = 1;
+    std::vector<int> levelPtr, groupPtr, unlockRow, dangerRow;
+
+    std::vector<FuncEntry> funcs;
+    DevBuf<int> dStatus;
+};
+
+}  // namespace race

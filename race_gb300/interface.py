@@ -1,0 +1,244 @@
+"""Python mirror of RACE::Interface (include/interface.h of the reference)
+over the engine's C ABI.
+
+Names, argument meaning and return codes follow the reference:
+``RACEColor`` returns a RACE_error code, ``registerFunction`` returns a
+function id (or an error code), ``executeFunction`` returns a code. The
+difference is the callback: instead of a host function pointer,
+``registerFunction`` takes a built-in device kernel (``SPMV``, ``SYMMSPMV``,
+``GS``, ``KACZ``, ``SPMTV``, ``MPK``) and its device operands. Device memory
+is managed with torch tensors; the engine never allocates user vectors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import time
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, lib, race_operands, race_params
+
+ONE, TWO, POWER = 1, 2, 3
+TWO_BLOCK, THREE_BLOCK = 0, 1
+ROW, NNZ = 0, 1
+FILL, SCATTER = 0, 1
+SPMV, SPMTV, SYMMSPMV, GS, KACZ, MPK = 0, 1, 2, 3, 4, 5
+VAL_F64, VAL_F32, VAL_BF16 = 0, 1, 2
+_VAL_TYPE = {torch.float64: VAL_F64, torch.float32: VAL_F32, torch.bfloat16: VAL_BF16}
+
+
+def _ptr(t: Optional[torch.Tensor]):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _host_i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+@dataclasses.dataclass
+class DeviceCsr:
+    """A CRS matrix in device memory (torch tensors)."""
+    n: int
+    row_ptr: torch.Tensor
+    col: torch.Tensor
+    val: torch.Tensor
+
+    @staticmethod
+    def from_csr(csr, device="cuda", dtype=torch.float64) -> "DeviceCsr":
+        return DeviceCsr(csr.n, torch.as_tensor(_host_i32(csr.row_ptr), device=device),
+                         torch.as_tensor(_host_i32(csr.col), device=device),
+                         torch.as_tensor(np.asarray(csr.val), device=device).to(dtype))
+
+
+@dataclasses.dataclass
+class Operands:
+    """The ``args`` of registerFunction: a device matrix and vectors.
+    For MPK, ``x`` holds (power+1)*n doubles, power-major."""
+    mat: DeviceCsr
+    x: torch.Tensor
+    b: Optional[torch.Tensor] = None
+
+    def to_c(self) -> race_operands:
+        vt = _VAL_TYPE[self.mat.val.dtype]
+        return race_operands(self.mat.n, self.mat.row_ptr.data_ptr(), self.mat.col.data_ptr(),
+                             self.mat.val.data_ptr(), vt, self.x.data_ptr(),
+                             None if self.b is None else self.b.data_ptr())
+
+
+class Interface:
+    """RACE::Interface(nrow, nthreads, dist, rowPtr, col, symm_hint, SMT,
+    pinMethod, initPerm, initInvPerm, d2Type, lbTarget) (interface.h:124).
+    SMT and pinMethod are accepted for signature parity; thread pinning has no
+    meaning on the GPU."""
+
+    def __init__(self, nrow: int, nthreads: int, dist: int, rowPtr, col, symm_hint: bool = False, SMT: int = 1,
+                 pinMethod: int = SCATTER, initPerm=None, initInvPerm=None, d2Type: int = TWO_BLOCK,
+                 lbTarget: int = NNZ, params: Optional[dict] = None, stream: Optional[torch.cuda.Stream] = None):
+        self.nrow = int(nrow)
+        self.dist = dist
+        self._funcs = {}
+        self._tuned = {}
+        rp, cl = _host_i32(rowPtr), _host_i32(col)
+        ip = _host_i32(initPerm) if initPerm is not None else None
+        iip = _host_i32(initInvPerm) if initInvPerm is not None else None
+        cparams = None
+        if params is not None:
+            cparams = race_params()
+            check(lib().race_params_from_env(C.byref(cparams)))
+            if "efficiency" in params:
+                eff = list(params["efficiency"])
+                cparams.n_eff = len(eff)
+                for i, v in enumerate(eff):
+                    cparams.eff[i] = v
+            if "lvl_threads" in params:
+                lt = list(params["lvl_threads"])
+                cparams.n_lvl_threads = len(lt)
+                for i, v in enumerate(lt):
+                    cparams.lvl_threads[i] = v
+            if "cache_violation_cutoff" in params:
+                cparams.cache_violation_cutoff = int(params["cache_violation_cutoff"])
+        h = C.c_void_p()
+        check(lib().race_create(C.byref(h), self.nrow, int(nthreads), int(dist), rp.ctypes.data, cl.ctypes.data,
+                                int(bool(symm_hint)), None if ip is None else ip.ctypes.data,
+                                None if iip is None else iip.ctypes.data, int(d2Type), int(lbTarget),
+                                None if cparams is None else C.byref(cparams)))
+        self._h = h
+        self.stream = stream
+        if stream is not None:
+            check(lib().race_set_stream(self._h, C.c_void_p(stream.cuda_stream)), self._h)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().race_destroy(h)
+            self._h = None
+
+    close = __del__
+
+    def _check(self, rc):
+        check(rc, self._h)
+
+    # ---- pre-processing (interface.h:127-135)
+    def RACEColor(self, highestPower: Optional[int] = None, cacheSize: Optional[float] = None,
+                  safetyFactor: float = 2.0, mtxType: str = "N", highestSubPower: int = 1) -> int:
+        """RACEColor() for coloring, RACEColor(highestPower, cacheSize [bytes], ...)
+        for the matrix-power partition. Returns a RACE_error code."""
+        if highestPower is None:
+            return lib().race_color(self._h)
+        return lib().race_power_prepare(self._h, int(highestPower), float(cacheSize), float(safetyFactor),
+                                        mtxType.encode(), int(highestSubPower))
+
+    def getPerm(self) -> np.ndarray:
+        p = np.zeros(self.nrow, np.int32)
+        self._check(lib().race_get_perm(self._h, p.ctypes.data, None))
+        return p
+
+    def getInvPerm(self) -> np.ndarray:
+        p = np.zeros(self.nrow, np.int32)
+        self._check(lib().race_get_perm(self._h, None, p.ctypes.data))
+        return p
+
+    def getNumThreads(self) -> int:
+        v = C.c_int()
+        self._check(lib().race_get_num_threads(self._h, C.byref(v)))
+        return v.value
+
+    def getEfficiency(self) -> float:
+        v = C.c_double()
+        self._check(lib().race_get_efficiency(self._h, C.byref(v)))
+        return v.value
+
+    def getMaxStageDepth(self) -> int:
+        v = C.c_int()
+        self._check(lib().race_get_max_stage_depth(self._h, C.byref(v)))
+        return v.value
+
+    def getZoneTreeFlat(self) -> np.ndarray:
+        n = C.c_int()
+        self._check(lib().race_get_zone_tree(self._h, None, 0, C.byref(n)))
+        buf = np.zeros(n.value, np.int32)
+        self._check(lib().race_get_zone_tree(self._h, buf.ctypes.data, n.value, C.byref(n)))
+        return buf
+
+    def getPhases(self, rev: bool = False):
+        npz, nl = C.c_int(), C.c_int()
+        self._check(lib().race_get_phases(self._h, int(rev), None, None, None, 0, C.byref(npz), C.byref(nl)))
+        cap = max(nl.value, npz.value + 1)
+        pp = np.zeros(cap, np.int32); lo = np.zeros(cap, np.int32); hi = np.zeros(cap, np.int32)
+        self._check(lib().race_get_phases(self._h, int(rev), pp.ctypes.data, lo.ctypes.data, hi.ctypes.data, cap,
+                                          C.byref(npz), C.byref(nl)))
+        return pp[: npz.value + 1], lo[: nl.value], hi[: nl.value]
+
+    def getPowerGroups(self) -> np.ndarray:
+        n = C.c_int()
+        self._check(lib().race_get_power_groups(self._h, None, 0, C.byref(n)))
+        buf = np.zeros(n.value, np.int32)
+        self._check(lib().race_get_power_groups(self._h, buf.ctypes.data, n.value, C.byref(n)))
+        return buf
+
+    # ---- execution (interface.h:149-174)
+    def registerFunction(self, kernel: int, args: Operands, power: int = 1) -> int:
+        fid = C.c_int(-1)
+        ops = args.to_c()
+        rc = lib().race_register_function(self._h, int(kernel), C.byref(ops), int(power), C.byref(fid))
+        if rc != _lib.RACE_SUCCESS:
+            return rc  # the reference returns the error code in place of an id (interface.cpp:429)
+        self._funcs[fid.value] = args  # keep operand tensors alive
+        return fid.value
+
+    def executeFunction(self, funcId: int, rev: bool = False) -> int:
+        return lib().race_execute_function(self._h, int(funcId), int(bool(rev)))
+
+    def executeFunctionAsync(self, funcId: int, rev: bool = False) -> int:
+        """Enqueue without waiting; getStatus() reports device-side waits."""
+        return lib().race_execute_function_async(self._h, int(funcId), int(bool(rev)))
+
+    def getStatus(self) -> int:
+        return lib().race_get_status(self._h)
+
+    def setStream(self, stream: torch.cuda.Stream):
+        self.stream = stream
+        self._check(lib().race_set_stream(self._h, C.c_void_p(stream.cuda_stream)))
+
+    def setPower(self, funcId: int, pow: int):
+        self._check(lib().race_set_power(self._h, int(funcId), int(pow)))
+
+    def getPower(self, funcId: int) -> int:
+        v = C.c_int()
+        self._check(lib().race_get_power(self._h, int(funcId), C.byref(v)))
+        return v.value
+
+    def tuneFunction(self, funcId: int, rev: bool = False, highestPower: Optional[int] = None) -> int:
+        """Interface::tuneFunction (interface.cpp:605-647): time powers
+        1..highestPower for >= 0.2 s each, keep the fastest time per power."""
+        if funcId in self._tuned:
+            self.setPower(funcId, self._tuned[funcId])
+            return self._tuned[funcId]
+        hp = highestPower or self.getPower(funcId)
+        times = []
+        for p in range(1, hp + 1):
+            self.setPower(funcId, p)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            it = 0
+            while True:
+                self._check(self.executeFunction(funcId, rev))
+                torch.cuda.synchronize()
+                it += 1
+                el = time.perf_counter() - t0
+                if el >= 0.2:
+                    break
+            times.append(el / (it * p))
+        best = int(np.argmin(times)) + 1
+        self._tuned[funcId] = best
+        self.setPower(funcId, best)
+        return best
+
+    # ---- convenience
+    def spmv_plain(self, mat: DeviceCsr, x: torch.Tensor, b: torch.Tensor):
+        self._check(lib().race_spmv_plain(self._h, mat.n, _ptr(mat.row_ptr), _ptr(mat.col), _ptr(mat.val), _ptr(x),
+                                          _ptr(b)))

@@ -1,0 +1,145 @@
+"""Generates tests/golden/golden.npz from the RACE reference compiled in
+place (oracle/build_ref.sh -> oracle/_ref/librace_ref.so).
+
+Run on the build host (where the reference sources are):
+    ./oracle/build_ref.sh && python tests/golden/make_golden.py
+
+Stored per case: matrix digest, permutation and inverse, zone tree (flat),
+threads/efficiency/stage depth, MPK level groups and the reference's sweep
+and MPK outputs for a few small cases. The reference's executor runs on
+OpenMP threads; its outputs are deterministic for valid colorings.
+Full-size configurations are stored as digests only.
+"""
+from __future__ import annotations
+
+import os
+import pathlib
+import sys
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+os.environ.setdefault("ORACLE_QUIET", "1")
+os.environ.setdefault("OMP_NUM_THREADS", "8")
+
+from cases import (COLOR_CASES, EXEC_CASES, MATRICES, POWER_CASES, TRAVERSE_CASES, arr_digest, digest, key_color,  # noqa: E402
+                   key_power, key_trav)
+from oracle import refpy  # noqa: E402
+from race_gb300 import matgen  # noqa: E402
+
+OUT = pathlib.Path(__file__).resolve().parent / "golden.npz"
+
+# full-size MPK configuration: 128^3 27-point stencil, p=8, 100 MB cache budget
+FULL_POWER = ("st27_128", 8, 100e6)
+
+
+def main():
+    g = {}
+    mats = {}
+
+    def M(name):
+        if name not in mats:
+            mats[name] = MATRICES[name]()
+        return mats[name]
+
+    for m, d in TRAVERSE_CASES:
+        A = M(m)
+        p, ip, lr, ln = refpy.traverse(A, d, 0, A.n)
+        k = key_trav(m, d)
+        g[k + "__digest"] = np.array(digest(A))
+        g[k + "__perm"] = p
+        g[k + "__levelRow"] = lr
+        g[k + "__levelNnz"] = ln
+        print(k, len(lr), "levels")
+
+    # load balancer on the level data of each traversal case
+    lb_rows = []
+    for m, d in TRAVERSE_CASES:
+        if d == 3:
+            continue
+        lr = g[key_trav(m, d) + "__levelRow"]
+        ln = g[key_trav(m, d) + "__levelNnz"]
+        for nt in (2, 5, 8, 33, 128):
+            for eff in (40.0, 10.0, 80.0):
+                for tgt in (0, 1):
+                    r = refpy.lb(lr, ln, nt, eff, d, 0, tgt, 7)
+                    flat = [len(r["scale"])] + r["scale"] + [len(r["numBlocks"])] + r["zonePtr"] + \
+                           [len(r["subZonePtr"]) - 1] + r["subZonePtr"] + r["numBlocks"]
+                    lb_rows.append((m, d, nt, eff, tgt, flat))
+    g["lb__index"] = np.array([f"{m}|{d}|{nt}|{eff}|{tgt}" for m, d, nt, eff, tgt, _ in lb_rows])
+    lens = np.array([len(f) for *_, f in lb_rows], np.int32)
+    g["lb__offsets"] = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    g["lb__data"] = np.concatenate([np.array(f, np.int32) for *_, f in lb_rows])
+    print("lb cases", len(lb_rows))
+
+    for m, d, t in COLOR_CASES:
+        A = M(m)
+        rc = refpy.RefColor(A, d, t)
+        k = key_color(m, d, t)
+        p, ip = rc.perm()
+        g[k + "__digest"] = np.array(digest(A))
+        g[k + "__perm"] = p
+        g[k + "__tree"] = rc.tree_flat()
+        g[k + "__threads"] = np.array(rc.threads())
+        g[k + "__eff"] = np.array(rc.efficiency())
+        g[k + "__stage"] = np.array(rc.max_stage())
+        g[k + "__serial"] = rc.serial_part()
+        if (m, d, t) in EXEC_CASES:
+            P = A.permuted(p, ip)
+            U = P.upper()
+            x0 = matgen.uniform_vector(A.n, 0)
+            b0 = matgen.uniform_vector(A.n, 1)
+            for kern, name, mat, rev in [(2, "symmspmv", U, False), (3, "gs", P, False), (3, "gsrev", P, True),
+                                         (4, "kacz", P, False), (0, "spmv", P, False)]:
+                if kern in (2, 4) and d != 2:
+                    continue
+                x = x0.copy()
+                b = np.zeros(A.n) if kern in (0, 2) else b0.copy()
+                rc.execute(kern, rev, mat, x, b)
+                g[k + f"__out_{name}"] = b if kern in (0, 2) else x
+        rc.close()
+        print(k, "threads", int(g[k + "__threads"]), "eff %.3f" % float(g[k + "__eff"]))
+
+    for m, p, c in POWER_CASES:
+        A = M(m)
+        rp = refpy.RefPower(A, p, c)
+        k = key_power(m, p, c)
+        perm, ip = rp.perm()
+        tr = rp.tree()
+        g[k + "__digest"] = np.array(digest(A))
+        g[k + "__perm"] = perm
+        g[k + "__lp"] = np.array(tr[0]["lp"], np.int32)
+        g[k + "__leaves"] = np.array(len(tr))
+        g[k + "__hid"] = np.array(tr[0]["hid"] + [-1], np.int32)
+        cov = rp.coverage()
+        assert (cov == 1).all()
+        if m in ("st27_24", "aniso5_120x90"):
+            P = A.permuted(perm, ip)
+            x0 = matgen.uniform_vector(A.n, 0)
+            g[k + "__out"] = rp.execute(P, x0)[1:]
+        rp.close()
+        print(k, "groups", len(tr[0]["lp"]) - 1, "leaves", len(tr))
+
+    # full-size MPK configuration: digests only
+    A = matgen.stencil3d_27pt(128)
+    m, p, c = FULL_POWER
+    rp = refpy.RefPower(A, p, c)
+    perm, ip = rp.perm()
+    tr = rp.tree()
+    k = key_power(m, p, c)
+    g[k + "__digest"] = np.array(digest(A))
+    g[k + "__perm_digest"] = np.array(arr_digest(perm))
+    g[k + "__lp"] = np.array(tr[0]["lp"], np.int32)
+    g[k + "__leaves"] = np.array(len(tr))
+    rp.close()
+    print(k, "groups", len(tr[0]["lp"]) - 1)
+
+    np.savez_compressed(OUT, **g)
+    print("wrote", OUT, OUT.stat().st_size // 1024, "KB")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,196 @@
+"""GPU engine parity: structure bit-exact against the reference (golden
+fixtures), numerics against the C oracle. Needs a GB300."""
+import numpy as np
+import pytest
+
+from cases import COLOR_CASES, POWER_CASES, arr_digest, digest, key_color, key_power
+from oracle import oracle as orc
+from oracle.refpy import parse_zone_tree
+from race_gb300 import matgen
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from race_gb300 import interface as ri  # noqa: E402
+
+
+def _rel_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize("m,d,t", COLOR_CASES)
+def test_coloring_matches_reference(golden, mats, m, d, t):
+    A = mats[m]
+    k = key_color(m, d, t)
+    assert str(golden[k + "__digest"]) == digest(A)
+    rc = ri.Interface(A.n, t, d, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor() == 0
+    np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
+    inv = rc.getInvPerm()
+    np.testing.assert_array_equal(inv[rc.getPerm()], np.arange(A.n))
+    np.testing.assert_array_equal(rc.getZoneTreeFlat(), golden[k + "__tree"])
+    assert rc.getNumThreads() == int(golden[k + "__threads"])
+    assert rc.getEfficiency() == float(golden[k + "__eff"])
+    assert rc.getMaxStageDepth() == int(golden[k + "__stage"])
+
+
+@pytest.mark.parametrize("m,p,c", POWER_CASES)
+def test_power_partition_matches_reference(golden, mats, m, p, c):
+    A = mats[m]
+    k = key_power(m, p, c)
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, c) == 0
+    np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
+    np.testing.assert_array_equal(rc.getPowerGroups(), golden[k + "__lp"])
+
+
+def _upload(P, dtype=torch.float64):
+    return ri.DeviceCsr.from_csr(P, "cuda", dtype)
+
+
+SWEEP_CASES = [("lap7_16", 2, 16), ("lap7_32", 2, 1024), ("lap7_32", 1, 256), ("aniso9_100x80", 1, 16),
+               ("plaw_3k", 1, 32), ("band_5k", 2, 32), ("st27_16", 2, 128), ("aniso5_120x90", 2, 48)]
+
+
+@pytest.mark.parametrize("m,d,t", SWEEP_CASES)
+def test_sweeps_match_oracle(golden, mats, m, d, t):
+    """Every built-in kernel through the persistent colored sweep, forward
+    and reverse, against the oracle's sequential walk of the reference zone
+    tree. FP64; warp reductions reorder the row sums, tolerance 1e-12."""
+    A = mats[m]
+    k = key_color(m, d, t)
+    rc = ri.Interface(A.n, t, d, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor() == 0
+    perm, inv = rc.getPerm(), rc.getInvPerm()
+    P = A.permuted(perm, inv)
+    U = P.upper()
+    nodes = parse_zone_tree(golden[k + "__tree"])
+    x0 = matgen.uniform_vector(A.n, 0)
+    b0 = matgen.uniform_vector(A.n, 1)
+    kernels = [(ri.GS, P, False), (ri.GS, P, True), (ri.SPMV, P, False)]
+    if d == 2:
+        kernels += [(ri.SYMMSPMV, U, False), (ri.KACZ, P, False), (ri.KACZ, P, True), (ri.SPMTV, P, False)]
+    for kern, mat, rev in kernels:
+        zero_b = kern in (ri.SPMV, ri.SYMMSPMV, ri.SPMTV)
+        xr, br = x0.copy(), (np.zeros(A.n) if zero_b else b0.copy())
+        orc.exec_tree(nodes, 2, golden[k + "__serial"], kern, rev, mat, xr, br)
+        dm = _upload(mat)
+        x = torch.tensor(x0, device="cuda")
+        b = torch.zeros(A.n, dtype=torch.float64, device="cuda") if zero_b else torch.tensor(b0, device="cuda")
+        fid = rc.registerFunction(kern, ri.Operands(dm, x, b))
+        assert fid >= 0
+        assert rc.executeFunction(fid, rev) == 0
+        torch.cuda.synchronize()
+        out_ref = br if zero_b else xr
+        out = (b if zero_b else x).cpu().numpy()
+        assert _rel_err(out, out_ref) <= 1e-12, (kern, rev, _rel_err(out, out_ref))
+
+
+@pytest.mark.parametrize("m,p,c", POWER_CASES)
+def test_mpk_fp64_bit_exact(golden, mats, m, p, c):
+    """Level-blocked MPK in FP64 equals p sequential fma SpMVs bit for bit."""
+    A = mats[m]
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, c) == 0
+    perm, inv = rc.getPerm(), rc.getInvPerm()
+    P = A.permuted(perm, inv)
+    x0 = matgen.uniform_vector(A.n, 0)
+    Y = orc.mpk_plain(P, x0, p)
+    dm = _upload(P)
+    x = torch.zeros((p + 1) * A.n, dtype=torch.float64, device="cuda")
+    x[: A.n] = torch.tensor(x0, device="cuda")
+    fid = rc.registerFunction(ri.MPK, ri.Operands(dm, x), power=p)
+    assert fid >= 0
+    for _ in range(2):  # repeated calls reuse the plan
+        assert rc.executeFunction(fid) == 0
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(x.cpu().numpy().reshape(p + 1, A.n), Y)
+
+
+def test_mpk_full_size_c2(golden):
+    """128^3 27-point stencil, p=8: permutation and level groups equal the
+    reference's (digests), and the GPU MPK equals the GPU plain SpMV chain bit
+    for bit (both are sequential fma row sums)."""
+    A = matgen.stencil3d_27pt(128)
+    k = key_power("st27_128", 8, 100e6)
+    assert str(golden[k + "__digest"]) == digest(A)
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(8, 100e6) == 0
+    perm, inv = rc.getPerm(), rc.getInvPerm()
+    assert arr_digest(perm) == str(golden[k + "__perm_digest"])
+    np.testing.assert_array_equal(rc.getPowerGroups(), golden[k + "__lp"])
+    P = A.permuted(perm, inv)
+    dm = _upload(P)
+    x = torch.zeros(9 * A.n, dtype=torch.float64, device="cuda")
+    x[: A.n] = torch.tensor(matgen.uniform_vector(A.n, 0), device="cuda")
+    fid = rc.registerFunction(ri.MPK, ri.Operands(dm, x), power=8)
+    assert rc.executeFunction(fid) == 0
+    y = torch.zeros_like(x)
+    y[: A.n] = x[: A.n]
+    for kk in range(1, 9):
+        rc.spmv_plain(dm, y[(kk - 1) * A.n: kk * A.n], y[kk * A.n:(kk + 1) * A.n])
+    torch.cuda.synchronize()
+    assert torch.equal(x, y)
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-5), (torch.bfloat16, 5e-2)])
+def test_mpk_reduced_precision_error(mats, dtype, tol):
+    """FP32/BF16 value storage with FP32 accumulation: error against the FP64
+    oracle stays within the storage precision (reported, not hidden)."""
+    A = mats["st27_24"]
+    p = 4
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, 2e6) == 0
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    x0 = matgen.uniform_vector(A.n, 0)
+    Y = orc.mpk_plain(P, x0, p)
+    dm = _upload(P, dtype)
+    x = torch.zeros((p + 1) * A.n, dtype=torch.float64, device="cuda")
+    x[: A.n] = torch.tensor(x0, device="cuda")
+    fid = rc.registerFunction(ri.MPK, ri.Operands(dm, x), power=p)
+    assert rc.executeFunction(fid) == 0
+    out = x.cpu().numpy().reshape(p + 1, A.n)
+    for kk in range(1, p + 1):
+        assert _rel_err(out[kk], Y[kk]) < tol
+
+
+def test_error_codes(mats):
+    A = mats["lap7_16"]
+    rc = ri.Interface(A.n, 8, ri.TWO, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(4, 1e6) == 1  # power partition needs dist POWER (interface.cpp:218-221)
+    assert rc.RACEColor() == 0
+    dm = _upload(A)
+    x = torch.zeros((5) * A.n, dtype=torch.float64, device="cuda")
+    assert rc.registerFunction(ri.MPK, ri.Operands(dm, x), power=4) == 1
+    assert rc.executeFunction(12345) == 1
+    rp = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rp.RACEColor() == 1  # coloring needs dist ONE/TWO (interface.cpp:264-267)
+    assert rp.RACEColor(4, 1e6, 2.0, "N", 0) == 1  # sub power < 1
+    d1 = ri.Interface(A.n, 8, ri.ONE, A.row_ptr, A.col, symm_hint=True)
+    assert d1.RACEColor() == 0
+    b = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+    assert d1.registerFunction(ri.KACZ, ri.Operands(dm, x[: A.n], b)) == 3  # needs distance-2
+
+
+def test_unsymmetric_pattern_is_symmetrised(mats):
+    """symm_hint=False on a matrix with one-sided entries: the traversal graph
+    gains the transposed pattern (graph.cpp:47-142) and levels match the
+    oracle on the symmetrised pattern."""
+    A = mats["band_5k"]
+    rows = np.repeat(np.arange(A.n), np.diff(A.row_ptr))
+    keep = (A.col >= rows) | (np.arange(A.nnz) % 3 == 0)  # drop two thirds of the lower triangle
+    counts = np.bincount(rows[keep], minlength=A.n)
+    rp = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    B = matgen.Csr(A.n, rp, A.col[keep].astype(np.int32), A.val[keep])
+    rc = ri.Interface(B.n, 1, ri.POWER, B.row_ptr, B.col, symm_hint=False)
+    assert rc.RACEColor(4, 3e5) == 0
+    # oracle on the explicitly symmetrised pattern
+    r2 = np.concatenate([rows[keep], B.col]); c2 = np.concatenate([B.col, rows[keep]])
+    S = matgen._assemble(B.n, r2[r2 != c2], c2[r2 != c2].astype(np.int32), np.ones((r2 != c2).sum()), np.ones(B.n), "s")
+    key = np.unique(S.col.astype(np.int64) + np.repeat(np.arange(S.n), np.diff(S.row_ptr)).astype(np.int64) * S.n)
+    rr, cc = key // S.n, key % S.n
+    off = rr != cc
+    S2 = matgen._assemble(S.n, rr[off], cc[off].astype(np.int32), np.ones(off.sum()), np.ones(S.n), "s2")
+    perm, _, _, _, _ = orc.traverse(S2, 3, 0, S2.n)
+    np.testing.assert_array_equal(rc.getPerm(), perm)

@@ -1,0 +1,115 @@
+"""Host-side engine logic without a GPU: the library loads and exports the
+C ABI, the load balancer matches the reference's, and the phase flattening
+of reference zone trees reproduces the reference execution order."""
+import ctypes as C
+import pathlib
+import re
+
+import numpy as np
+import pytest
+
+from cases import COLOR_CASES, EXEC_CASES, key_color
+from oracle import oracle as orc
+from oracle.refpy import parse_zone_tree
+from race_gb300 import _lib, matgen
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+
+
+def _header_functions():
+    text = (ROOT / "include" / "race_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(race_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    declared = _header_functions()
+    assert declared, "no functions parsed from the header"
+    for name in declared:
+        assert hasattr(L, name), name
+    assert sorted(_lib.EXPORTS) == declared
+
+
+def _lb(levelRow, levelNnz, nt, eff, dist, tgt, base=7):
+    L = _lib.lib()
+    lr = np.ascontiguousarray(levelRow, np.int32)
+    ln = np.ascontiguousarray(levelNnz, np.int32)
+    n = C.c_int()
+    _lib.check(L.race_lb_balance(lr.ctypes.data, ln.ctypes.data, lr.size, nt, eff, dist, 0, tgt, base, None, 0,
+                                 C.byref(n)))
+    out = np.zeros(n.value, np.int32)
+    _lib.check(L.race_lb_balance(lr.ctypes.data, ln.ctypes.data, lr.size, nt, eff, dist, 0, tgt, base,
+                                 out.ctypes.data, n.value, C.byref(n)))
+    return out
+
+
+def test_load_balancer_matches_reference(golden):
+    idx = golden["lb__index"]
+    off = golden["lb__offsets"]
+    data = golden["lb__data"]
+    for i, key in enumerate(idx):
+        m, d, nt, eff, tgt = str(key).split("|")
+        k = f"trav__{m}__d{d}"
+        got = _lb(golden[k + "__levelRow"], golden[k + "__levelNnz"], int(nt), float(eff), int(d), int(tgt))
+        np.testing.assert_array_equal(got, data[off[i]:off[i + 1]], err_msg=str(key))
+
+
+def _flatten(tree_flat, dist, rev, n):
+    L = _lib.lib()
+    t = np.ascontiguousarray(tree_flat, np.int32)
+    npz, nl = C.c_int(), C.c_int()
+    _lib.check(L.race_flatten_zone_tree(t.ctypes.data, t.size, dist, 0, int(rev), n, n, None, None, None, 0,
+                                        C.byref(npz), C.byref(nl)))
+    cap = max(nl.value, npz.value + 1)
+    pp = np.zeros(cap, np.int32); lo = np.zeros(cap, np.int32); hi = np.zeros(cap, np.int32)
+    _lib.check(L.race_flatten_zone_tree(t.ctypes.data, t.size, dist, 0, int(rev), n, n, pp.ctypes.data,
+                                        lo.ctypes.data, hi.ctypes.data, cap, C.byref(npz), C.byref(nl)))
+    return pp[:npz.value + 1], lo[:nl.value], hi[:nl.value]
+
+
+@pytest.mark.parametrize("m,d,t", COLOR_CASES)
+def test_phases_cover_every_row_once(golden, mats, m, d, t):
+    A = mats[m]
+    k = key_color(m, d, t)
+    for rev in (False, True):
+        pp, lo, hi = _flatten(golden[k + "__tree"], d, rev, A.n)
+        seen = np.zeros(A.n, np.int32)
+        for a, b in zip(lo, hi):
+            if a <= b:
+                seen[a:b] += 1
+            else:
+                seen[b + 1:a + 1] += 1
+        assert (seen == 1).all()
+
+
+def _run_phases(pp, lo, hi, kern, mat, x, b):
+    for p in range(len(pp) - 1):
+        for l in range(pp[p], pp[p + 1]):
+            orc.run_kernel(kern, int(lo[l]), int(hi[l]), mat, x, b)
+
+
+@pytest.mark.parametrize("m,d,t", sorted(EXEC_CASES) + [("lap7_32", 2, 1024), ("lap7_32", 1, 256)])
+def test_phases_reproduce_reference_order(golden, mats, m, d, t):
+    """Running the kernels phase by phase over the flattened phases gives the
+    same bits as the reference's recursive execution order."""
+    A = mats[m]
+    k = key_color(m, d, t)
+    perm = golden[k + "__perm"]
+    inv = np.empty_like(perm); inv[perm] = np.arange(A.n, dtype=np.int32)
+    P = A.permuted(perm, inv)
+    U = P.upper()
+    nodes = parse_zone_tree(golden[k + "__tree"])
+    x0 = matgen.uniform_vector(A.n, 0)
+    b0 = matgen.uniform_vector(A.n, 1)
+    kernels = [(orc.K_GS, P, False), (orc.K_GS, P, True)]
+    if d == 2:
+        kernels += [(orc.K_SYMMSPMV, U, False), (orc.K_KACZ, P, False), (orc.K_KACZ, P, True)]
+    for kern, mat, rev in kernels:
+        x1, b1 = x0.copy(), (np.zeros(A.n) if kern == orc.K_SYMMSPMV else b0.copy())
+        x2, b2 = x1.copy(), b1.copy()
+        orc.exec_tree(nodes, 2, golden[k + "__serial"], kern, rev, mat, x1, b1)
+        pp, lo, hi = _flatten(golden[k + "__tree"], d, rev, A.n)
+        _run_phases(pp, lo, hi, kern, mat, x2, b2)
+        np.testing.assert_array_equal(x1, x2)
+        np.testing.assert_array_equal(b1, b2)

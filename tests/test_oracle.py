@@ -1,0 +1,97 @@
+"""The C restatement oracle against golden data produced by the reference
+(tests/golden/make_golden.py). CPU only."""
+import numpy as np
+import pytest
+
+from cases import EXEC_CASES, POWER_CASES, TRAVERSE_CASES, digest, key_color, key_power, key_trav
+from oracle import oracle as orc
+from race_gb300 import matgen
+
+
+@pytest.mark.parametrize("m,d", TRAVERSE_CASES)
+def test_traverse_matches_reference(golden, mats, m, d):
+    A = mats[m]
+    k = key_trav(m, d)
+    assert str(golden[k + "__digest"]) == digest(A)
+    perm, inv, lr, ln, _ = orc.traverse(A, d, 0, A.n)
+    np.testing.assert_array_equal(perm, golden[k + "__perm"])
+    np.testing.assert_array_equal(lr, golden[k + "__levelRow"])
+    np.testing.assert_array_equal(ln, golden[k + "__levelNnz"])
+    np.testing.assert_array_equal(inv[perm], np.arange(A.n))
+
+
+def _tree(golden, k):
+    from oracle.refpy import parse_zone_tree
+    return parse_zone_tree(golden[k + "__tree"])
+
+
+@pytest.mark.parametrize("m,d,t", sorted(EXEC_CASES))
+def test_executor_walk_matches_reference(golden, mats, m, d, t):
+    """The sequential zone-tree walk reproduces the reference's threaded
+    executor bit for bit on its own schedule."""
+    A = mats[m]
+    k = key_color(m, d, t)
+    perm = golden[k + "__perm"]
+    inv = np.empty_like(perm); inv[perm] = np.arange(A.n, dtype=np.int32)
+    P = A.permuted(perm, inv)
+    U = P.upper()
+    nodes = _tree(golden, k)
+    x0 = matgen.uniform_vector(A.n, 0)
+    b0 = matgen.uniform_vector(A.n, 1)
+    for kern, name, mat, rev in [(orc.K_SYMMSPMV, "symmspmv", U, False), (orc.K_GS, "gs", P, False),
+                                 (orc.K_GS, "gsrev", P, True), (orc.K_KACZ, "kacz", P, False),
+                                 (orc.K_SPMV, "spmv", P, False)]:
+        key = k + f"__out_{name}"
+        if key not in golden:
+            continue
+        x = x0.copy()
+        b = np.zeros(A.n) if kern in (orc.K_SPMV, orc.K_SYMMSPMV) else b0.copy()
+        orc.exec_tree(nodes, 2, golden[k + "__serial"], kern, rev, mat, x, b)
+        out = b if kern in (orc.K_SPMV, orc.K_SYMMSPMV) else x
+        np.testing.assert_array_equal(out, golden[key], err_msg=name)
+
+
+@pytest.mark.parametrize("m,p,c", POWER_CASES)
+def test_mpk_partition_matches_reference(golden, mats, m, p, c):
+    A = mats[m]
+    k = key_power(m, p, c)
+    assert str(golden[k + "__digest"]) == digest(A)
+    perm, inv, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+    np.testing.assert_array_equal(perm, golden[k + "__perm"])
+    lp = np.concatenate([[0], np.cumsum(lr)]).astype(np.int32)
+    g = orc.mpk_groups(p, A.n, A.nnz, c, 2.0, 50, lp, ln)
+    assert g is not None
+    np.testing.assert_array_equal(g[0], golden[k + "__lp"])
+
+
+@pytest.mark.parametrize("m,p,c", [pc for pc in POWER_CASES if pc[0] in ("st27_24", "aniso5_120x90")])
+def test_mpk_output_matches_reference(golden, mats, m, p, c):
+    """The reference MPK executor's output equals p sequential fma SpMVs, and
+    the oracle's threaded wavefront port gives the same bits."""
+    A = mats[m]
+    k = key_power(m, p, c)
+    perm = golden[k + "__perm"]
+    inv = np.empty_like(perm); inv[perm] = np.arange(A.n, dtype=np.int32)
+    P = A.permuted(perm, inv)
+    x0 = matgen.uniform_vector(A.n, 0)
+    Y = orc.mpk_plain(P, x0, p)
+    np.testing.assert_array_equal(Y[1:], golden[k + "__out"])
+    perm2, inv2, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+    lp = np.concatenate([[0], np.cumsum(lr)]).astype(np.int32)
+    gp, ur, dr = orc.mpk_groups(p, A.n, A.nnz, c, 2.0, 50, lp, ln)
+    Z = orc.mpk_wavefront(P, x0, p, gp, ur, dr, int(__import__("os").environ.get("OMP_NUM_THREADS", "4")))
+    np.testing.assert_array_equal(Z, Y)
+
+
+def test_oracle_detects_planted_schedule_error(mats):
+    """A schedule that drops a level group must not match: the checker can fail."""
+    A = mats["st27_16"]
+    x0 = matgen.uniform_vector(A.n, 0)
+    perm, inv, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+    P = A.permuted(perm, inv)
+    lp = np.concatenate([[0], np.cumsum(lr)]).astype(np.int32)
+    gp, ur, dr = orc.mpk_groups(4, A.n, A.nnz, 2e5, 2.0, 50, lp, ln)
+    Y = orc.mpk_plain(P, x0, 4)
+    assert len(gp) > 2
+    Z = orc.mpk_wavefront(P, x0, 4, gp[:-1].copy(), ur, dr, 1)  # last group dropped
+    assert not np.array_equal(Z, Y)
