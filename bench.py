@@ -244,8 +244,9 @@ def main():
         rc.executeFunctionAsync(f32)
 
     def plain64():
-        for k in range(1, POWER + 1):
-            rc.spmv_plain(dm64, x64[(k - 1) * n:k * n], x64[k * n:(k + 1) * n])
+        # the traditional path: p separate SpMVs on the same SELL-32 layout
+        for k in range(POWER):
+            rc.spmvPowerLayout(f64, k)
 
     with ClockSampler(local) as clk:
         ms64 = timed(mpk64, args.steps)

@@ -144,6 +144,12 @@ int race_get_power(race_engine *e, int func_id, int *out);
 int race_spmv_plain(race_engine *e, int n, const int *rowPtr_dev, const int *col_dev, const double *val_dev,
                     const double *x_dev, double *b_dev);
 
+/* One plain SpMV x_{k+1} = A x_k (0 <= k < power) of a registered RACE_K_MPK
+ * function, on its internal layout and operands, without the level-blocked
+ * schedule: the traditional p-SpMV path on the same data (no counterpart in
+ * the reference, whose examples time it separately as tradPower). */
+int race_spmv_power_layout(race_engine *e, int func_id, int k);
+
 /* Host-only helpers (no GPU needed), exposed for inspection and tests:
  * the level load balancer (LB::balance, lb.cpp:188-771) on given level data,
  * out = [nScale, scale..., totalBlocks, zonePtr(totalBlocks+1)...,

@@ -12,7 +12,7 @@ namespace race {
 
 std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int power);
 void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power);
-int mpkStatus(Engine &e, MpkPlan &plan);
+void runSpmvSell(Engine &e, MpkPlan &plan, double *x, int n, int k);
 void uploadPhases(Engine &e, int dir);
 void runSweep(Engine &e, int kernel, const race_operands &ops, bool rev);
 
@@ -320,6 +320,16 @@ int race_get_power(race_engine *e, int func_id, int *out) {
     if (!e || !out || func_id < 0 || func_id >= (int)e->eng->funcs.size()) return RACE_ERR_INVALID_ARG;
     *out = e->eng->funcs[func_id].power;
     return RACE_SUCCESS;
+}
+
+int race_spmv_power_layout(race_engine *e, int func_id, int k) {
+    if (!e || func_id < 0 || func_id >= (int)e->eng->funcs.size()) return RACE_ERR_INVALID_ARG;
+    return guard(e, [&] {
+        race::FuncEntry &f = e->eng->funcs[func_id];
+        if (f.kernel != RACE_K_MPK || !f.mpk) throw Error(RACE_ERR_INVALID_ARG, "not a matrix-power function");
+        if (k < 0 || k >= f.power) throw Error(RACE_ERR_INVALID_ARG, "k out of range");
+        race::runSpmvSell(*e->eng, *f.mpk, f.ops.x, f.ops.n, k);
+    });
 }
 
 int race_spmv_plain(race_engine *e, int n, const int *rowPtr, const int *col, const double *val, const double *x,

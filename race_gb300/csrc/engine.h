@@ -20,18 +20,23 @@ struct DevPhases {
 // non-zeros fit the kernel's shared-memory stage, in RACE's wavefront order,
 // with the last tile each one depends on.
 struct MpkPlan {
-    int numTiles = 0;
+    int numChunks = 0;          // SELL-32 chunks (<= 32 rows, inside one level group)
     int power = 0;
-    int numItems = 0;           // power * numTiles
-    DevBuf<int> tileRow;        // numTiles+1 row offsets
-    DevBuf<int> depHi;          // numTiles: highest tile holding a column of the tile
-    DevBuf<int> itemTile;       // numItems: tile of each work item, wavefront order
+    int numItems = 0;           // power * numChunks
+    int valType = 0;
+    long long sellSlots = 0;    // SELL entries including padding
+    DevBuf<long long> chunkOff; // numChunks: first SELL slot of each chunk
+    DevBuf<int> chunkRow;       // numChunks+1: first row of each chunk
+    DevBuf<int> rowLen;         // n: non-zeros per row
+    DevBuf<unsigned char> sellVal;  // sellSlots values (type valType)
+    DevBuf<int> sellCol;        // sellSlots column indices
+    DevBuf<float> xf;           // (power+1)*n FP32 powers (reduced-precision storage)
+    DevBuf<int> depRange;       // numChunks*6: chunks read in the previous/own/next group
+    DevBuf<int> itemChunk;      // numItems: chunk of each work item, wavefront order
     DevBuf<unsigned char> itemPow;  // numItems: power (0-based) of each work item
-    DevBuf<int> flags;          // power * numTiles completion flags
-    DevBuf<int> watermark;      // power: completed prefix of tiles
+    DevBuf<int> done;           // power * numChunks completion flags
     DevBuf<int> ticket;         // 1: next work item
     DevBuf<int> status;         // 1: device status word
-    int maxTileNnz = 0;
 };
 
 struct FuncEntry {
@@ -85,6 +90,7 @@ class Engine {
     DevPhases dPhases[2];
 
     // power results
+    int mpkStride = 2;  // issue order of the MPK wavefront (1: RACE's, 2: GPU default)
     bool powerReady = false;
     int highestPower = 1, highestSubPower = 1;
     std::vector<int> levelPtr, groupPtr, unlockRow, dangerRow;

@@ -2,26 +2,36 @@
 //
 // RACE's schedule (src/matrixPower.cpp consolidatePartition; executor
 // src/functionManager.cpp:618-823) groups BFS levels so that p+1 powers of
-// one group fit the cache, and runs a diagonal wavefront: at step s the
-// group s-k is computed at power k for all k. Because BFS levels only couple
-// neighbouring levels, power k of a group needs power k-1 of the group
-// itself and its two neighbours, all of which come earlier in that order.
+// one group fit the cache, and runs a diagonal wavefront over (group,
+// power). BFS levels only couple neighbouring levels, so power k of a group
+// needs power k-1 of the group itself and of its two neighbours.
 //
-// GPU form: the permuted CRS is cut into tiles (contiguous rows, never
-// crossing a level group, at most kTileRows rows and kTileNnz non-zeros).
-// Work items (power, tile) are listed in the wavefront order; persistent
-// CTAs take them in order from a global ticket. Before computing, an item
-// waits until every tile up to the highest tile its columns touch is done at
-// the previous power: a per-power watermark counts the completed prefix of
-// tiles. Items only wait on earlier tickets, which are held by running CTAs,
-// so the schedule cannot deadlock; each wait is bounded anyway and reports
-// a timeout through the status word. Groups sized to the L2 keep a group's
-// rows resident while its p powers are computed, so the matrix is read from
-// HBM about once per call instead of p times.
+// Layout. At registration the permuted CRS is copied into SELL-32: rows are
+// cut into chunks of at most 32 consecutive rows that never cross a level
+// group, and each chunk stores entry j of its rows contiguously
+// (val[off + 32 j + lane]). A warp reads 32 consecutive values per load, and
+// each lane still owns one row and walks it as a sequential fma chain in CRS
+// order (MAT_SPMV_KERNEL's order, examples/src/helpers/kernels.cpp:749-777):
+// FP64 output is bit-identical to p sequential SpMVs with fused
+// multiply-adds. Padding slots are never computed (lanes stop at their row
+// length). One lane per row keeps GB300's FP64 pipe (1/64 of the FP32 rate)
+// busy with useful fmas only.
 //
-// Each row is a sequential fma chain in CRS order (the order of
-// MAT_SPMV_KERNEL, examples/src/helpers/kernels.cpp:749-777), so FP64 output
-// is bit-identical to p plain sequential SpMVs with fused multiply-adds.
+// Schedule. A work item is (power, chunk). Items are listed in wavefront
+// order and taken by persistent warps from a global ticket; each warp is an
+// independent worker (no CTA barriers). An item waits until, at the previous
+// power, the chunks holding its columns are complete: per chunk the engine
+// records one chunk range in each of the previous, own and next group
+// (narrow: a row's neighbours sit near the same position of the adjacent
+// levels), and the warp checks their completion flags in parallel. Items
+// wait only on earlier tickets, held by running warps, so the schedule
+// cannot deadlock; every wait is bounded anyway and reports a timeout
+// through the status word.
+//
+// Reduced precision (FP32/BF16 values): the powers are kept in an internal
+// FP32 copy of x and accumulated in FP32; each result is also written to the
+// caller's FP64 x through an exact float->double bit conversion, so the FP32
+// path issues no FP64 instructions in its inner loop.
 #include <algorithm>
 #include <numeric>
 
@@ -31,9 +41,7 @@
 
 namespace race {
 
-constexpr int kTileRows = 128;
-constexpr int kTileNnz = 4096;
-constexpr int kMpkThreads = 128;
+constexpr int kWarpThreads = 256;
 
 namespace {
 
@@ -42,144 +50,151 @@ __device__ __forceinline__ int ldAcquire(const int *p) {
     asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void stRelease(int *p, int v) {
-    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ void backoff() { __nanosleep(64); }
 
-// Row of the matrix times a vector. FP64 storage: fma chain in double.
-// FP32/BF16 storage: fma chain in float (values and x rounded to float).
 template <typename VT>
-struct RowDot;
+__device__ __forceinline__ float toF(VT v);
 template <>
-struct RowDot<double> {
-    static __device__ __forceinline__ double run(const double *__restrict__ val, const int *__restrict__ col, int s,
-                                                 int e, const double *__restrict__ x) {
-        double t = 0.0;
-#pragma unroll 4
-        for (int j = s; j < e; ++j) t = fma(val[j], __ldcg(x + col[j]), t);
-        return t;
-    }
-};
+__device__ __forceinline__ float toF<float>(float v) { return v; }
 template <>
-struct RowDot<float> {
-    static __device__ __forceinline__ double run(const float *__restrict__ val, const int *__restrict__ col, int s,
-                                                 int e, const double *__restrict__ x) {
-        float t = 0.0f;
-#pragma unroll 4
-        for (int j = s; j < e; ++j) t = fmaf(val[j], (float)__ldcg(x + col[j]), t);
-        return (double)t;
+__device__ __forceinline__ float toF<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// Exact binary32 -> binary64 conversion with integer operations (the IEEE
+// 754 formats: re-bias the exponent, widen the significand; subnormal
+// floats are normalised). Keeps the FP32 path off the FP64 pipe.
+__device__ __forceinline__ double floatToDoubleExact(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    unsigned long long bits;
+    if (e == 0xffu) {
+        bits = sign | (0x7ffULL << 52) | ((unsigned long long)m << 29);
+    } else if (e != 0) {
+        bits = sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+    } else if (m == 0) {
+        bits = sign;
+    } else {
+        const int p = 31 - __clz(m);  // value = m * 2^-149, leading bit at position p
+        bits = sign | ((unsigned long long)(p + 874) << 52) | (((unsigned long long)m << (52 - p)) & 0xfffffffffffffULL);
     }
+    return __longlong_as_double((long long)bits);
+}
+
+struct SellView {
+    const void *val;
+    const int *col;
+    const long long *chunkOff;  // numChunks: element offset of each chunk
+    const int *chunkRow;        // numChunks+1: first row of each chunk
+    const int *rowLen;          // n
 };
-template <>
-struct RowDot<__nv_bfloat16> {
-    static __device__ __forceinline__ double run(const __nv_bfloat16 *__restrict__ val, const int *__restrict__ col,
-                                                 int s, int e, const double *__restrict__ x) {
-        float t = 0.0f;
+
+// One row of a SELL-32 chunk, FP64 storage: lane-owned fma chain.
+__device__ __forceinline__ double sellRowD(const double *__restrict__ val, const int *__restrict__ col, long long off,
+                                           int len, const double *x) {
+    double t = 0.0;
 #pragma unroll 4
-        for (int j = s; j < e; ++j) t = fmaf(__bfloat162float(val[j]), (float)__ldcg(x + col[j]), t);
-        return (double)t;
+    for (int j = 0; j < len; ++j) t = fma(val[off + 32LL * j], x[col[off + 32LL * j]], t);
+    return t;
+}
+// FP32/BF16 storage with an FP32 vector.
+template <typename VT>
+__device__ __forceinline__ float sellRowF(const VT *__restrict__ val, const int *__restrict__ col, long long off,
+                                          int len, const float *x) {
+    float t = 0.0f;
+#pragma unroll 4
+    for (int j = 0; j < len; ++j) t = fmaf(toF<VT>(val[off + 32LL * j]), x[col[off + 32LL * j]], t);
+    return t;
+}
+
+// The lane's row of chunk c at power k -> k+1.
+template <typename VT>
+__device__ __forceinline__ void chunkRow(const SellView &m, int c, int k, int n, double *x, float *xf) {
+    const int lane = threadIdx.x & 31;
+    const int r = m.chunkRow[c] + lane;
+    if (r >= m.chunkRow[c + 1]) return;
+    const long long off = m.chunkOff[c] + lane;
+    if constexpr (sizeof(VT) == 8) {
+        x[(size_t)(k + 1) * n + r] = sellRowD((const double *)m.val, m.col, off, m.rowLen[r], x + (size_t)k * n);
+    } else {
+        const float v = sellRowF<VT>((const VT *)m.val, m.col, off, m.rowLen[r], xf + (size_t)k * n);
+        xf[(size_t)(k + 1) * n + r] = v;
+        x[(size_t)(k + 1) * n + r] = floatToDoubleExact(v);
     }
-};
+}
 
 struct MpkArgs {
-    const int *rowPtr;
-    const int *col;
-    const void *val;
-    double *x;
+    SellView m;
+    double *x;      // caller's (p+1)*n powers
+    float *xf;      // internal FP32 powers (reduced-precision storage only)
     int n;
-    const int *tileRow;
-    const int *depHi;
-    const int *itemTile;
+    const int *depRange;  // numChunks*6: [lo,hi] chunks read in the previous, own and next group
+    const int *itemChunk;
     const unsigned char *itemPow;
-    int numItems, numTiles;
-    int *flags;
-    int *watermark;
+    int numItems, numChunks;
+    int *done;            // power * numChunks completion flags
     int *ticket;
     int *status;
 };
 
+// Persistent warps: one (power, chunk) item per ticket. Taking several
+// items at once or requesting the next ticket early measured slower: an
+// item held but not started delays every item that depends on it.
 template <typename VT>
-__global__ void __launch_bounds__(kMpkThreads) kMpk(MpkArgs a) {
-    __shared__ int sItem;
-    __shared__ int sBail;
-    const VT *__restrict__ val = (const VT *)a.val;
+__global__ void __launch_bounds__(kWarpThreads) kMpk(MpkArgs a) {
+    const int lane = threadIdx.x & 31;
     for (;;) {
-        if (threadIdx.x == 0) {
-            sItem = atomicAdd(a.ticket, 1);
-            sBail = 0;
-        }
-        __syncthreads();
-        const int it = sItem;
-        if (it >= a.numItems) break;
-        const int t = a.itemTile[it];
+        int it = 0;
+        if (lane == 0) it = atomicAdd(a.ticket, 1);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= a.numItems) return;
+        const int c = a.itemChunk[it];
         const int k = a.itemPow[it];  // computes x_{k+1} from x_k
-        if (threadIdx.x == 0 && k > 0) {
-            const int need = a.depHi[t];
-            const int *wm = a.watermark + (k - 1);
+        if (k > 0) {
+            // every chunk holding a column of this chunk must be complete at
+            // power k-1: up to three chunk ranges, one per neighbouring group
+            const int *rg = a.depRange + 6 * c;
+            const int *done = a.done + (size_t)(k - 1) * a.numChunks;
             long long spins = 0;
-            while (ldAcquire(wm) <= need) {
+            for (;;) {
+                bool ok = true;
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                    for (int i = rg[2 * d] + lane; i <= rg[2 * d + 1]; i += 32)
+                        if (ldAcquire(done + i) == 0) ok = false;
+                if (__all_sync(0xffffffffu, ok)) break;
                 if (++spins > kSpinLimit || ldAcquire(a.status) != DEV_OK) {
-                    atomicCAS(a.status, DEV_OK, DEV_WAIT_TIMEOUT);
-                    sBail = 1;
-                    break;
+                    if (lane == 0) atomicCAS(a.status, DEV_OK, DEV_WAIT_TIMEOUT);
+                    return;
                 }
-                backoff();
+                __nanosleep(32);
             }
         }
-        __syncthreads();
-        if (sBail) break;
-        const int r0 = a.tileRow[t], r1 = a.tileRow[t + 1];
-        const double *__restrict__ xin = a.x + (size_t)k * a.n;
-        double *__restrict__ xout = a.x + (size_t)(k + 1) * a.n;
-        for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-            xout[r] = RowDot<VT>::run(val, a.col, a.rowPtr[r], a.rowPtr[r + 1], xin);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int *fl = a.flags + (size_t)k * a.numTiles;
-            __threadfence();
-            stRelease(fl + t, 1);
-            __threadfence();
-            // advance the completed prefix of power k past every done tile
-            int *wm = a.watermark + k;
-            int w = ldAcquire(wm);
-            while (w < a.numTiles && ldAcquire(fl + w) == 1) {
-                int old = atomicCAS(wm, w, w + 1);
-                w = (old == w) ? w + 1 : old;
-            }
-        }
+        chunkRow<VT>(a.m, c, k, a.n, a.x, a.xf);
+        // __syncwarp orders the lanes' stores before lane 0's release store
+        __syncwarp();
+        if (lane == 0)
+            asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(a.done + (size_t)k * a.numChunks + c), "r"(1)
+                         : "memory");
     }
 }
 
-// Highest column of every row, then per tile the highest tile it reads.
-__global__ void kTileDeps(const int *__restrict__ rowPtr, const int *__restrict__ col, const int *__restrict__ tileRow,
-                          int numTiles, int *__restrict__ depHi) {
-    int t = blockIdx.x;
-    if (t >= numTiles) return;
-    int r0 = tileRow[t], r1 = tileRow[t + 1];
-    int m = -1;
-    for (int j = rowPtr[r0] + threadIdx.x; j < rowPtr[r1]; j += blockDim.x) m = max(m, col[j]);
-    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    __shared__ int sm[32];
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = max(m, sm[w]);
-        m = max(m, sm[0]);
-        // binary search: tile holding row m
-        int lo = 0, hi = numTiles - 1;
-        if (m < 0) m = r0;
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (tileRow[mid] <= m) lo = mid; else hi = mid - 1;
-        }
-        depHi[t] = max(lo, t);
-    }
+// Plain y = A x on the SELL layout, no schedule: one warp per chunk.
+template <typename VT>
+__global__ void __launch_bounds__(kWarpThreads) kSpmvSell(SellView m, int numChunks, int n, int k, double *x,
+                                                          float *xf) {
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < numChunks; c += nw)
+        chunkRow<VT>(m, c, k, n, x, xf);
 }
 
-__global__ void kSpmvPlain(int n, const int *__restrict__ rowPtr, const int *__restrict__ col,
-                           const double *__restrict__ val, const double *__restrict__ x, double *__restrict__ b) {
+// x0 -> FP32 copy (rounding to nearest) for the reduced-precision path.
+__global__ void kToFloat(const double *__restrict__ x, float *__restrict__ xf, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) xf[i] = (float)x[i];
+}
+
+// CRS thread-per-row SpMV (for raw pointers without a registered layout).
+__global__ void kSpmvCrs(int n, const int *__restrict__ rowPtr, const int *__restrict__ col,
+                         const double *__restrict__ val, const double *__restrict__ x, double *__restrict__ b) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     double t = 0.0;
@@ -188,122 +203,260 @@ __global__ void kSpmvPlain(int n, const int *__restrict__ rowPtr, const int *__r
     b[r] = t;
 }
 
+// CRS -> SELL-32 copy; padding slots get value 0 and the row's own column.
+template <typename VT>
+__global__ void kToSell(const int *__restrict__ rowPtr, const int *__restrict__ col, const VT *__restrict__ val,
+                        const long long *__restrict__ chunkOff, const int *__restrict__ chunkRowP,
+                        const int *__restrict__ chunkLen, int numChunks, VT *__restrict__ sval, int *__restrict__ scol) {
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= numChunks) return;
+    const int lane = threadIdx.x & 31;
+    const int r = chunkRowP[c] + lane;
+    const bool live = r < chunkRowP[c + 1];
+    const int s = live ? rowPtr[r] : 0, len = live ? rowPtr[r + 1] - s : 0;
+    const int L = chunkLen[c];
+    for (int j = 0; j < L; ++j) {
+        long long o = chunkOff[c] + 32LL * j + lane;
+        if (j < len) {
+            sval[o] = val[s + j];
+            scol[o] = col[s + j];
+        } else {
+            sval[o] = VT(0);
+            scol[o] = live ? r : chunkRowP[c];
+        }
+    }
+}
+
+// For every chunk, the range of chunks its columns fall in, separately for
+// the previous, the own and the next level group. Columns outside those
+// three groups mark the plan invalid (*bad = 1): BFS levels only couple
+// neighbouring levels, so a RACE-permuted matrix never has them.
+__global__ void kChunkRanges(const int *__restrict__ rowPtr, const int *__restrict__ col,
+                             const int *__restrict__ chunkRowP, const int *__restrict__ chunkGroup, int numChunks,
+                             int *__restrict__ range, int *__restrict__ bad) {
+    const int t = blockIdx.x;
+    if (t >= numChunks) return;
+    __shared__ int lo[3], hi[3];
+    if (threadIdx.x < 3) {
+        lo[threadIdx.x] = INT_MAX;
+        hi[threadIdx.x] = -1;
+    }
+    __syncthreads();
+    const int g = chunkGroup[t];
+    for (int j = rowPtr[chunkRowP[t]] + threadIdx.x; j < rowPtr[chunkRowP[t + 1]]; j += blockDim.x) {
+        const int c = col[j];
+        int a = 0, b = numChunks - 1;
+        while (a < b) {
+            int mid = (a + b + 1) >> 1;
+            if (chunkRowP[mid] <= c) a = mid; else b = mid - 1;
+        }
+        const int d = chunkGroup[a] - g + 1;
+        if (d < 0 || d > 2) {
+            atomicExch(bad, 1);
+            continue;
+        }
+        atomicMin(&lo[d], a);
+        atomicMax(&hi[d], a);
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        range[6 * t + 2 * threadIdx.x] = (hi[threadIdx.x] < 0) ? 0 : lo[threadIdx.x];
+        range[6 * t + 2 * threadIdx.x + 1] = hi[threadIdx.x];  // empty range: hi = -1 < lo
+    }
+}
+
+int gDevSms = 0;
+int devSms() {
+    if (!gDevSms) {
+        int dev = 0;
+        RACE_CUDA(cudaGetDevice(&dev));
+        RACE_CUDA(cudaDeviceGetAttribute(&gDevSms, cudaDevAttrMultiProcessorCount, dev));
+    }
+    return gDevSms;
+}
+
+template <typename K>
+int residentBlocks(K kernel, int threads) {
+    int occ = 0;
+    RACE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, 0));
+    return devSms() * std::max(occ, 1);
+}
+
+size_t valBytes(int vt) { return vt == RACE_VAL_F64 ? 8 : vt == RACE_VAL_F32 ? 4 : 2; }
+
 }  // namespace
 
-// Builds the tile table and the wavefront item order of one MPK operand set
-// (the user's permuted matrix) for the engine's level groups.
+// Builds the SELL-32 copy, the chunk dependency ranges and the wavefront
+// item order of one MPK operand set (the user's permuted matrix) for the
+// engine's level groups.
 std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int power) {
     auto plan = std::make_unique<MpkPlan>();
     const int n = ops.n;
+    cudaStream_t s = e.stream;
     std::vector<int> rp(n + 1);
-    RACE_CUDA(cudaMemcpyAsync(rp.data(), ops.rowPtr, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, e.stream));
-    RACE_CUDA(cudaStreamSynchronize(e.stream));
+    RACE_CUDA(cudaMemcpyAsync(rp.data(), ops.rowPtr, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, s));
+    RACE_CUDA(cudaStreamSynchronize(s));
     const std::vector<int> &gp = e.groupPtr;
     const int G = (int)gp.size() - 1;
-    std::vector<int> tileRow{0}, tileGroup;
-    for (int g = 0; g < G; ++g) {
-        int r = gp[g];
-        while (r < gp[g + 1]) {
-            int s = r;
-            int lim = std::min(gp[g + 1], s + kTileRows);
-            int e2 = s + 1;
-            while (e2 < lim && rp[e2 + 1] - rp[s] <= kTileNnz) ++e2;
-            tileRow.push_back(e2);
-            tileGroup.push_back(g);
-            plan->maxTileNnz = std::max(plan->maxTileNnz, rp[e2] - rp[s]);
-            r = e2;
+    // chunks of <= 32 rows inside groups
+    std::vector<int> chunkRowH{0}, chunkLen, chunkGroup, rowLen(n);
+    std::vector<long long> chunkOff;
+    long long off = 0;
+    for (int r = 0; r < n; ++r) rowLen[r] = rp[r + 1] - rp[r];
+    for (int g = 0; g < G; ++g)
+        for (int r = gp[g]; r < gp[g + 1]; r += 32) {
+            int r1 = std::min(gp[g + 1], r + 32);
+            int L = 0;
+            for (int q = r; q < r1; ++q) L = std::max(L, rowLen[q]);
+            chunkOff.push_back(off);
+            chunkLen.push_back(L);
+            chunkRowH.push_back(r1);
+            chunkGroup.push_back(g);
+            off += 32LL * L;
         }
+    const int C = (int)chunkLen.size();
+    plan->numChunks = C;
+    plan->power = power;
+    plan->valType = ops.val_type;
+    plan->sellSlots = off;
+    plan->chunkOff.upload(chunkOff.data(), std::max(C, 1), s);
+    plan->chunkRow.upload(chunkRowH.data(), chunkRowH.size(), s);
+    plan->rowLen.upload(rowLen.data(), n, s);
+    DevBuf<int> dChunkLen;
+    dChunkLen.upload(chunkLen.data(), std::max(C, 1), s);
+    plan->sellVal.alloc(std::max<long long>(off, 1) * valBytes(ops.val_type));
+    plan->sellCol.alloc(std::max<long long>(off, 1));
+    if (ops.val_type != RACE_VAL_F64) plan->xf.alloc((size_t)(power + 1) * n);
+    const int blocksC = ceilDiv(std::max(C, 1), 8);
+    switch (ops.val_type) {
+    case RACE_VAL_F64:
+        kToSell<double><<<blocksC, 256, 0, s>>>(ops.rowPtr, ops.col, (const double *)ops.val, plan->chunkOff.p,
+                                                plan->chunkRow.p, dChunkLen.p, C, (double *)plan->sellVal.p,
+                                                plan->sellCol.p);
+        break;
+    case RACE_VAL_F32:
+        kToSell<float><<<blocksC, 256, 0, s>>>(ops.rowPtr, ops.col, (const float *)ops.val, plan->chunkOff.p,
+                                               plan->chunkRow.p, dChunkLen.p, C, (float *)plan->sellVal.p,
+                                               plan->sellCol.p);
+        break;
+    case RACE_VAL_BF16:
+        kToSell<__nv_bfloat16><<<blocksC, 256, 0, s>>>(ops.rowPtr, ops.col, (const __nv_bfloat16 *)ops.val,
+                                                        plan->chunkOff.p, plan->chunkRow.p, dChunkLen.p, C,
+                                                        (__nv_bfloat16 *)plan->sellVal.p, plan->sellCol.p);
+        break;
+    default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
     }
-    const int T = (int)tileGroup.size();
-    std::vector<int> groupFirst(G + 1, 0);
-    for (int t = 0, g = 0; g <= G; ++g) {
-        while (t < T && tileGroup[t] < g) ++t;
-        groupFirst[g] = t;
-    }
-    // wavefront order: step s, power k, group s-k (functionManager.cpp:638-647)
-    std::vector<int> itemTile;
+    RACE_CUDA(cudaGetLastError());
+    // Issue order. RACE's wavefront (functionManager.cpp:638-647) visits
+    // step s, power k, group s-k (stride 1): power k of group g then needs
+    // power k-1 of group g+1 from the same step, one group earlier in the
+    // order, and thousands of in-flight items would queue behind that chain.
+    // With stride 2 (step s holds power k of group s-2k) every dependency
+    // sits in an earlier step, so the items in flight are independent; each
+    // group stays in use for 2p-1 steps instead of p. Both orders compute the
+    // same rows at the same powers; results are bit-identical.
+    const int stride = e.mpkStride == 1 ? 1 : 2;
+    std::vector<int> groupFirst(G + 1, C);
+    for (int t = C - 1; t >= 0; --t) groupFirst[chunkGroup[t]] = t;
+    for (int g = G - 1; g >= 0; --g) groupFirst[g] = std::min(groupFirst[g], groupFirst[g + 1]);
+    std::vector<int> itemChunk;
     std::vector<unsigned char> itemPow;
-    itemTile.reserve((size_t)T * power);
-    for (int s = 0; s < G + power - 1; ++s)
+    itemChunk.reserve((size_t)C * power);
+    for (int st = 0; st < G + stride * (power - 1); ++st)
         for (int k = 0; k < power; ++k) {
-            int g = s - k;
+            int g = st - stride * k;
             if (g < 0 || g >= G) continue;
             for (int t = groupFirst[g]; t < groupFirst[g + 1]; ++t) {
-                itemTile.push_back(t);
+                itemChunk.push_back(t);
                 itemPow.push_back((unsigned char)k);
             }
         }
-    plan->numTiles = T;
-    plan->power = power;
-    plan->numItems = (int)itemTile.size();
-    plan->tileRow.upload(tileRow.data(), tileRow.size(), e.stream);
-    plan->itemTile.upload(itemTile.data(), itemTile.size(), e.stream);
-    plan->itemPow.upload(itemPow.data(), itemPow.size(), e.stream);
-    plan->depHi.alloc(std::max(T, 1));
-    plan->flags.alloc((size_t)std::max(T, 1) * power);
-    plan->watermark.alloc(power);
+    plan->numItems = (int)itemChunk.size();
+    plan->itemChunk.upload(itemChunk.data(), std::max<size_t>(itemChunk.size(), 1), s);
+    plan->itemPow.upload(itemPow.data(), std::max<size_t>(itemPow.size(), 1), s);
+    plan->depRange.alloc((size_t)std::max(C, 1) * 6);
+    plan->done.alloc((size_t)std::max(C, 1) * power);
     plan->ticket.alloc(1);
     plan->status.alloc(1);
-    if (T > 0) kTileDeps<<<T, 128, 0, e.stream>>>(ops.rowPtr, ops.col, plan->tileRow.p, T, plan->depHi.p);
+    DevBuf<int> dChunkGroup, dBad(1);
+    dChunkGroup.upload(chunkGroup.data(), std::max<size_t>(chunkGroup.size(), 1), s);
+    RACE_CUDA(cudaMemsetAsync(dBad.p, 0, sizeof(int), s));
+    if (C > 0)
+        kChunkRanges<<<C, 128, 0, s>>>(ops.rowPtr, ops.col, plan->chunkRow.p, dChunkGroup.p, C, plan->depRange.p,
+                                       dBad.p);
     RACE_CUDA(cudaGetLastError());
-    std::vector<int> dep(std::max(T, 1));
-    RACE_CUDA(cudaMemcpyAsync(dep.data(), plan->depHi.p, sizeof(int) * T, cudaMemcpyDeviceToHost, e.stream));
-    RACE_CUDA(cudaStreamSynchronize(e.stream));
-    // Every dependency must come earlier in the wavefront order: columns of
-    // group g may reach at most group g+1 (BFS levels couple neighbours
-    // only). A matrix not permuted with this engine's MPK permutation would
-    // break that and is rejected here instead of stalling the kernel.
-    for (int t = 0; t < T; ++t)
-        if (tileGroup[dep[t]] > tileGroup[t] + 1)
-            throw Error(RACE_ERR_INVALID_ARG,
-                        "MPK operand is not in the engine's level order (permute it with getPerm/getInvPerm)");
+    int bad = 0;
+    RACE_CUDA(cudaMemcpyAsync(&bad, dBad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RACE_CUDA(cudaStreamSynchronize(s));
+    // Every dependency must come earlier in the wavefront order: the columns
+    // of group g lie in groups g-1..g+1 (BFS levels couple neighbours only).
+    // A matrix not permuted with this engine's MPK permutation breaks that
+    // and is rejected here instead of stalling the kernel.
+    if (bad)
+        throw Error(RACE_ERR_INVALID_ARG,
+                    "MPK operand is not in the engine's level order (permute it with getPerm/getInvPerm)");
     return plan;
 }
 
+namespace {
+SellView viewOf(const MpkPlan &p) {
+    return SellView{p.sellVal.p, p.sellCol.p, p.chunkOff.p, p.chunkRow.p, p.rowLen.p};
+}
+
+template <typename VT>
+void launchMpk(const MpkArgs &a, cudaStream_t s) {
+    static int blocks = residentBlocks(kMpk<VT>, kWarpThreads);
+    kMpk<VT><<<blocks, kWarpThreads, 0, s>>>(a);
+}
+}  // namespace
+
 void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
-    if (power > plan.power) throw Error(RACE_ERR_INVALID_ARG, "power above the planned power");
+    if (power != plan.power) throw Error(RACE_ERR_INVALID_ARG, "power differs from the planned power");
     cudaStream_t s = e.stream;
-    RACE_CUDA(cudaMemsetAsync(plan.flags.p, 0, sizeof(int) * (size_t)plan.numTiles * plan.power, s));
-    RACE_CUDA(cudaMemsetAsync(plan.watermark.p, 0, sizeof(int) * plan.power, s));
+    RACE_CUDA(cudaMemsetAsync(plan.done.p, 0, sizeof(int) * (size_t)plan.numChunks * plan.power, s));
     RACE_CUDA(cudaMemsetAsync(plan.ticket.p, 0, sizeof(int), s));
     RACE_CUDA(cudaMemsetAsync(plan.status.p, 0, sizeof(int), s));
-    MpkArgs a{ops.rowPtr, ops.col, ops.val, ops.x, ops.n, plan.tileRow.p, plan.depHi.p, plan.itemTile.p,
-              plan.itemPow.p, 0, plan.numTiles, plan.flags.p, plan.watermark.p, plan.ticket.p, plan.status.p};
-    // items of powers above `power` are skipped by truncating the item list:
-    // the wavefront lists them interleaved, so run the full list only when
-    // power equals the planned power.
-    if (power != plan.power) throw Error(RACE_ERR_NOT_IMPLEMENTED, "power must equal the registered power");
-    a.numItems = plan.numItems;
-    int dev = 0, sms = 0, occ = 0;
-    RACE_CUDA(cudaGetDevice(&dev));
-    RACE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    switch (ops.val_type) {
-    case RACE_VAL_F64:
-        RACE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kMpk<double>, kMpkThreads, 0));
-        kMpk<double><<<sms * std::max(occ, 1), kMpkThreads, 0, s>>>(a);
-        break;
-    case RACE_VAL_F32:
-        RACE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kMpk<float>, kMpkThreads, 0));
-        kMpk<float><<<sms * std::max(occ, 1), kMpkThreads, 0, s>>>(a);
-        break;
-    case RACE_VAL_BF16:
-        RACE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kMpk<__nv_bfloat16>, kMpkThreads, 0));
-        kMpk<__nv_bfloat16><<<sms * std::max(occ, 1), kMpkThreads, 0, s>>>(a);
-        break;
+    if (plan.valType != RACE_VAL_F64) kToFloat<<<ceilDiv(ops.n, 256), 256, 0, s>>>(ops.x, plan.xf.p, ops.n);
+    MpkArgs a{viewOf(plan), ops.x, plan.xf.p, ops.n, plan.depRange.p, plan.itemChunk.p, plan.itemPow.p,
+              plan.numItems, plan.numChunks, plan.done.p, plan.ticket.p, plan.status.p};
+    switch (plan.valType) {
+    case RACE_VAL_F64: launchMpk<double>(a, s); break;
+    case RACE_VAL_F32: launchMpk<float>(a, s); break;
+    case RACE_VAL_BF16: launchMpk<__nv_bfloat16>(a, s); break;
     default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
     }
     RACE_CUDA(cudaGetLastError());
 }
 
-int mpkStatus(Engine &e, MpkPlan &plan) {
-    int st = 0;
-    RACE_CUDA(cudaMemcpyAsync(&st, plan.status.p, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
-    RACE_CUDA(cudaStreamSynchronize(e.stream));
-    return st;
+// One plain SpMV x_{k+1} = A x_k on the registered SELL layout (the p-SpMV
+// baseline on the same data as the blocked kernel).
+void runSpmvSell(Engine &e, MpkPlan &plan, double *x, int n, int k) {
+    cudaStream_t s = e.stream;
+    if (plan.valType != RACE_VAL_F64 && k == 0) kToFloat<<<ceilDiv(n, 256), 256, 0, s>>>(x, plan.xf.p, n);
+    SellView v = viewOf(plan);
+    switch (plan.valType) {
+    case RACE_VAL_F64: {
+        static int blocks = residentBlocks(kSpmvSell<double>, kWarpThreads);
+        kSpmvSell<double><<<blocks, kWarpThreads, 0, s>>>(v, plan.numChunks, n, k, x, plan.xf.p);
+        break;
+    }
+    case RACE_VAL_F32: {
+        static int blocks = residentBlocks(kSpmvSell<float>, kWarpThreads);
+        kSpmvSell<float><<<blocks, kWarpThreads, 0, s>>>(v, plan.numChunks, n, k, x, plan.xf.p);
+        break;
+    }
+    case RACE_VAL_BF16: {
+        static int blocks = residentBlocks(kSpmvSell<__nv_bfloat16>, kWarpThreads);
+        kSpmvSell<__nv_bfloat16><<<blocks, kWarpThreads, 0, s>>>(v, plan.numChunks, n, k, x, plan.xf.p);
+        break;
+    }
+    default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
+    }
+    RACE_CUDA(cudaGetLastError());
 }
 
 void Engine::spmvPlain(int nr, const int *rowPtr, const int *col, const double *val, const double *x, double *b) {
-    kSpmvPlain<<<ceilDiv(nr, 256), 256, 0, stream>>>(nr, rowPtr, col, val, x, b);
+    kSpmvCrs<<<ceilDiv(nr, 256), 256, 0, stream>>>(nr, rowPtr, col, val, x, b);
     RACE_CUDA(cudaGetLastError());
 }
 

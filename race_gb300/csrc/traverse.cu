@@ -232,6 +232,7 @@ Engine::Engine(int nrow, int nthreads, int dist_, const int *rowPtr, const int *
     dKeysOut.alloc(nrow);
     dValsOut.alloc(nrow);
     dStatus.alloc(4);
+    if (const char *st = getenv("RACE_GPU_MPK_STRIDE")) mpkStride = atoi(st) == 1 ? 1 : 2;
     RACE_CUDA(cudaStreamSynchronize(stream));
 }
 

@@ -239,6 +239,11 @@ class Interface:
         return best
 
     # ---- convenience
+    def spmvPowerLayout(self, funcId: int, k: int):
+        """x_{k+1} = A x_k for a registered MPK function, as a plain SpMV on
+        the same internal layout (no level blocking)."""
+        self._check(lib().race_spmv_power_layout(self._h, int(funcId), int(k)))
+
     def spmv_plain(self, mat: DeviceCsr, x: torch.Tensor, b: torch.Tensor):
         self._check(lib().race_spmv_plain(self._h, mat.n, _ptr(mat.row_ptr), _ptr(mat.col), _ptr(mat.val), _ptr(x),
                                           _ptr(b)))

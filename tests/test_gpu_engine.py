@@ -125,11 +125,19 @@ def test_mpk_full_size_c2(golden):
     x = torch.zeros(9 * A.n, dtype=torch.float64, device="cuda")
     x[: A.n] = torch.tensor(matgen.uniform_vector(A.n, 0), device="cuda")
     fid = rc.registerFunction(ri.MPK, ri.Operands(dm, x), power=8)
-    assert rc.executeFunction(fid) == 0
     y = torch.zeros_like(x)
     y[: A.n] = x[: A.n]
     for kk in range(1, 9):
         rc.spmv_plain(dm, y[(kk - 1) * A.n: kk * A.n], y[kk * A.n:(kk + 1) * A.n])
+    for rep in range(3):  # repeated calls: stale cached values would show up as mismatches
+        x[A.n:] = 0
+        assert rc.executeFunction(fid) == 0
+        torch.cuda.synchronize()
+        assert torch.equal(x, y), rep
+    # the same p SpMVs without level blocking on the registered layout
+    x[A.n:] = 0
+    for kk in range(8):
+        rc.spmvPowerLayout(fid, kk)
     torch.cuda.synchronize()
     assert torch.equal(x, y)
 
