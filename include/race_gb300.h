@@ -150,6 +150,28 @@ int race_spmv_plain(race_engine *e, int n, const int *rowPtr_dev, const int *col
  * the reference, whose examples time it separately as tradPower). */
 int race_spmv_power_layout(race_engine *e, int func_id, int k);
 
+/* Matrix power without any device allocation. No counterpart in the
+ * reference (its executor runs on the host and allocates freely).
+ * For callers that cannot allocate device memory when they run the kernel:
+ * code whose device memory is owned by its own pool, real-time loops with a
+ * fixed memory budget, library code that must not trigger a cudaMalloc (and
+ * the device synchronisation it may cause). All scratch lives in one
+ * built-in device array of 16 MiB (2^22 ints) held by every GPU that loads
+ * the library; a problem needing more than about power * ceil(n/32) +
+ * 2 * numGroups + 2 * power ints is rejected with RACE_ERR_INVALID_ARG.
+ * Inputs: the FP64 CRS matrix permuted with the engine's MPK permutation
+ * (device), the level groups from race_get_power_groups (numGroups+1 row
+ * offsets, both a device and a host copy), and x with (power+1)*n doubles,
+ * power-major, x[0:n] the input vector (device). Results equal the
+ * registered RACE_K_MPK path bit for bit. The first call on a device looks
+ * up the array's device address, so make that first call before any CUDA
+ * stream capture. Calls share the array: calls that overlap on the GPU
+ * (other streams, other host threads) race and must be serialised by the
+ * caller. Synchronises `stream` before returning. */
+int race_mpk_noalloc(int n, const int *rowPtr_dev, const int *col_dev, const double *val_dev,
+                     const int *groupPtr_dev, const int *groupPtr_host, int numGroups, int power, double *x_dev,
+                     void *stream);
+
 /* Host-only helpers (no GPU needed), exposed for inspection and tests:
  * the level load balancer (LB::balance, lb.cpp:188-771) on given level data,
  * out = [nScale, scale..., totalBlocks, zonePtr(totalBlocks+1)...,

@@ -26,8 +26,8 @@ EXPORTS = [
     "race_get_perm", "race_get_num_threads", "race_get_efficiency", "race_get_max_stage_depth", "race_get_zone_tree",
     "race_get_phases", "race_get_power_groups", "race_register_function", "race_execute_function",
     "race_execute_function_async", "race_get_status", "race_set_power",
-    "race_get_power", "race_spmv_plain", "race_spmv_power_layout", "race_lb_balance", "race_flatten_zone_tree",
-    "race_last_error",
+    "race_get_power", "race_spmv_plain", "race_spmv_power_layout", "race_mpk_noalloc", "race_lb_balance",
+    "race_flatten_zone_tree", "race_last_error",
 ]
 
 
@@ -71,6 +71,7 @@ def lib():
             "race_execute_function": [vp, i, i], "race_execute_function_async": [vp, i, i],
             "race_get_status": [vp], "race_set_power": [vp, i, i], "race_get_power": [vp, i, ip],
             "race_spmv_plain": [vp, i, vp, vp, vp, vp, vp], "race_spmv_power_layout": [vp, i, i],
+            "race_mpk_noalloc": [i, vp, vp, vp, vp, vp, i, i, vp, vp],
             "race_lb_balance": [vp, vp, i, i, C.c_double, i, i, i, i, vp, i, ip],
             "race_flatten_zone_tree": [vp, i, i, i, i, i, i, vp, vp, vp, i, ip, ip],
         }
