@@ -57,6 +57,14 @@ enum {
 /* Value storage of a registered operand set. */
 enum { RACE_VAL_F64 = 0, RACE_VAL_F32 = 1, RACE_VAL_BF16 = 2 };
 
+/* Execution of colored sweeps. WAVE: RACE's order compiled into
+ * conflict-free waves, one thread per row, results identical bit for bit to
+ * RACE's sequential walk (rows above 512 entries use a warp reduction).
+ * LEAF: one warp per RACE leaf, rows in order, warp-shuffle row reductions.
+ * AUTO (default): per function and direction, whichever is estimated
+ * cheaper. */
+enum { RACE_SWEEP_AUTO = 0, RACE_SWEEP_WAVE = 1, RACE_SWEEP_LEAF = 2 };
+
 typedef struct race_engine race_engine;
 
 /* Device operands of a built-in kernel (the `args` of registerFunction). */
@@ -66,8 +74,9 @@ typedef struct {
     const int *col;         /* dev, nnz */
     const void *val;        /* dev, nnz, type val_type */
     int val_type;           /* RACE_VAL_* */
-    double *x;              /* dev; MPK: (power+1)*n, power-major */
-    double *b;              /* dev; n (unused by MPK) */
+    void *x;                /* dev, type vec_type; MPK: (power+1)*n doubles, power-major */
+    void *b;                /* dev, type vec_type, n (unused by MPK) */
+    int vec_type;           /* RACE_VAL_F64 or RACE_VAL_F32 (sweeps); MPK vectors are always FP64 */
 } race_operands;
 
 /* Pre-processing knobs; the reference reads them from the environment
@@ -135,6 +144,14 @@ int race_execute_function(race_engine *e, int func_id, int rev);
  * synchronous. */
 int race_execute_function_async(race_engine *e, int func_id, int rev);
 int race_get_status(race_engine *e);
+/* Sweep execution mode of this engine (RACE_SWEEP_*), and the schedule
+ * sizes of a registered sweep function in one direction: waves and the
+ * largest wave, phases and the longest leaf, and the mode AUTO picks. No
+ * counterpart in the reference (its executor has one mode). */
+int race_set_sweep_mode(race_engine *e, int mode);
+int race_get_sweep_info(race_engine *e, int func_id, int rev, int *numWaves, int *maxWaveRows, int *numPhases,
+                        int *maxLeafRows, int *waveModeChosen);
+
 /* Interface::setPower / getPower (interface.cpp:574-590) */
 int race_set_power(race_engine *e, int func_id, int power);
 int race_get_power(race_engine *e, int func_id, int *out);
@@ -143,6 +160,21 @@ int race_get_power(race_engine *e, int func_id, int *out);
  * reference compares MPK against, kernels.cpp:90-105). */
 int race_spmv_plain(race_engine *e, int n, const int *rowPtr_dev, const int *col_dev, const double *val_dev,
                     const double *x_dev, double *b_dev);
+
+/* Symmetric Gauss-Seidel solve of A x = b with FP64 iterative refinement
+ * (the reference's GS driver loop, examples/src/colorSymmGS.cpp:147-267,
+ * with a mixed-precision inner solve). inner_func_id is a registered
+ * RACE_K_GS function whose operands hold the inner matrix (FP32/BF16 values
+ * with FP32 vectors, or FP64) and whose x/b buffers receive the correction d
+ * and the residual r. Each refinement computes r = b - A x in FP64 from the
+ * FP64 matrix (rowPtr/col/val, dev, same permuted matrix), runs `sweeps`
+ * forward+backward sweeps on A d = r from d = 0, and updates x += d in FP64;
+ * it stops when ||r||_2 <= tol ||b||_2 or after maxIter refinements.
+ * *iters and *relres receive the refinement count and the final relative
+ * residual. No counterpart in the reference API. */
+int race_symmgs_ir(race_engine *e, int inner_func_id, int n, const int *rowPtr_dev, const int *col_dev,
+                   const double *val_dev, const double *b_dev, double *x_dev, double tol, int maxIter, int sweeps,
+                   int *iters, double *relres);
 
 /* One plain SpMV x_{k+1} = A x_k (0 <= k < power) of a registered RACE_K_MPK
  * function, on its internal layout and operands, without the level-blocked

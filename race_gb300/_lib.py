@@ -25,9 +25,9 @@ EXPORTS = [
     "race_params_from_env", "race_create", "race_destroy", "race_set_stream", "race_color", "race_power_prepare",
     "race_get_perm", "race_get_num_threads", "race_get_efficiency", "race_get_max_stage_depth", "race_get_zone_tree",
     "race_get_phases", "race_get_power_groups", "race_register_function", "race_execute_function",
-    "race_execute_function_async", "race_get_status", "race_set_power",
-    "race_get_power", "race_spmv_plain", "race_spmv_power_layout", "race_mpk_noalloc", "race_lb_balance",
-    "race_flatten_zone_tree", "race_last_error",
+    "race_execute_function_async", "race_get_status", "race_set_sweep_mode", "race_get_sweep_info", "race_set_power",
+    "race_get_power", "race_spmv_plain", "race_spmv_power_layout", "race_mpk_noalloc", "race_symmgs_ir",
+    "race_lb_balance", "race_flatten_zone_tree", "race_last_error",
 ]
 
 
@@ -44,7 +44,7 @@ class race_params(C.Structure):
 
 class race_operands(C.Structure):
     _fields_ = [("n", C.c_int), ("rowPtr", C.c_void_p), ("col", C.c_void_p), ("val", C.c_void_p),
-                ("val_type", C.c_int), ("x", C.c_void_p), ("b", C.c_void_p)]
+                ("val_type", C.c_int), ("x", C.c_void_p), ("b", C.c_void_p), ("vec_type", C.c_int)]
 
 
 _lib = None
@@ -70,8 +70,10 @@ def lib():
             "race_register_function": [vp, i, C.POINTER(race_operands), i, ip],
             "race_execute_function": [vp, i, i], "race_execute_function_async": [vp, i, i],
             "race_get_status": [vp], "race_set_power": [vp, i, i], "race_get_power": [vp, i, ip],
+            "race_set_sweep_mode": [vp, i], "race_get_sweep_info": [vp, i, i, ip, ip, ip, ip, ip],
             "race_spmv_plain": [vp, i, vp, vp, vp, vp, vp], "race_spmv_power_layout": [vp, i, i],
             "race_mpk_noalloc": [i, vp, vp, vp, vp, vp, i, i, vp, vp],
+            "race_symmgs_ir": [vp, i, i, vp, vp, vp, vp, vp, C.c_double, i, i, ip, C.POINTER(C.c_double)],
             "race_lb_balance": [vp, vp, i, i, C.c_double, i, i, i, i, vp, i, ip],
             "race_flatten_zone_tree": [vp, i, i, i, i, i, i, vp, vp, vp, i, ip, ip],
         }

@@ -14,7 +14,11 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
 void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power);
 void runSpmvSell(Engine &e, MpkPlan &plan, double *x, int n, int k);
 void uploadPhases(Engine &e, int dir);
-void runSweep(Engine &e, int kernel, const race_operands &ops, bool rev);
+void buildSweepWaves(Engine &e, FuncEntry &f);
+void runSweep(Engine &e, FuncEntry &f, bool rev);
+bool useWaveMode(const Engine &e, const FuncEntry &f, int dir);
+void symmGsIr(Engine &e, int inner, int n, const int *rowPtr, const int *col, const double *val, const double *b,
+              double *x, double tol, int maxIter, int sweeps, int *itersOut, double *relresOut);
 
 // Interface::RACEColor() (interface.cpp:260-301): level recursion over the
 // whole matrix, then the execution phases of both sweep directions.
@@ -111,6 +115,11 @@ int Engine::registerFunction(int kernel, const race_operands &ops, int power) {
         if (!ops.x || !ops.b) throw Error(RACE_ERR_INVALID_ARG, "missing x or b");
         if ((kernel == RACE_K_SPMTV || kernel == RACE_K_KACZ || kernel == RACE_K_SYMMSPMV) && dist != DIST_TWO)
             throw Error(RACE_ERR_D2_COLOR, "scatter kernels need distance-2 coloring");
+        if (ops.vec_type == RACE_VAL_F64 && ops.val_type != RACE_VAL_F64)
+            throw Error(RACE_ERR_INVALID_ARG, "FP64 vectors need FP64 values");
+        if (ops.vec_type == RACE_VAL_F32 && ops.val_type == RACE_VAL_F64)
+            throw Error(RACE_ERR_INVALID_ARG, "FP32 vectors need FP32 or BF16 values");
+        buildSweepWaves(*this, f);
     }
     funcs.push_back(std::move(f));
     return (int)funcs.size() - 1;
@@ -123,7 +132,7 @@ void Engine::launch(int id, bool rev) {
         runMpk(*this, *f.mpk, f.ops, f.power);
         lastStatus = f.mpk->status.p;
     } else {
-        runSweep(*this, f.kernel, f.ops, rev);
+        runSweep(*this, f, rev);
         lastStatus = dStatus.p;
     }
 }
@@ -307,6 +316,28 @@ int race_get_status(race_engine *e) {
     return guard(e, [&] { e->eng->checkStatus(); });
 }
 
+int race_set_sweep_mode(race_engine *e, int mode) {
+    if (!e || mode < RACE_SWEEP_AUTO || mode > RACE_SWEEP_LEAF) return RACE_ERR_INVALID_ARG;
+    e->eng->sweepMode = mode;
+    return RACE_SUCCESS;
+}
+
+int race_get_sweep_info(race_engine *e, int func_id, int rev, int *numWaves, int *maxWaveRows, int *numPhases,
+                        int *maxLeafRows, int *waveModeChosen) {
+    if (!e || func_id < 0 || func_id >= (int)e->eng->funcs.size() || !numWaves || !maxWaveRows || !numPhases ||
+        !maxLeafRows || !waveModeChosen)
+        return RACE_ERR_INVALID_ARG;
+    const race::FuncEntry &f = e->eng->funcs[func_id];
+    if (f.kernel == RACE_K_MPK) return RACE_ERR_INVALID_ARG;
+    const int dir = rev ? 1 : 0;
+    *numWaves = f.waves[dir].numWaves;
+    *maxWaveRows = f.waves[dir].maxRows;
+    *numPhases = e->eng->dPhases[dir].numPhases;
+    *maxLeafRows = e->eng->dPhases[dir].maxLeafRows;
+    *waveModeChosen = race::useWaveMode(*e->eng, f, dir) ? 1 : 0;
+    return RACE_SUCCESS;
+}
+
 int race_set_power(race_engine *e, int func_id, int power) {
     if (!e || func_id < 0 || func_id >= (int)e->eng->funcs.size()) return RACE_ERR_INVALID_ARG;
     return guard(e, [&] {
@@ -322,13 +353,22 @@ int race_get_power(race_engine *e, int func_id, int *out) {
     return RACE_SUCCESS;
 }
 
+int race_symmgs_ir(race_engine *e, int inner_func_id, int n, const int *rowPtr, const int *col, const double *val,
+                   const double *b, double *x, double tol, int maxIter, int sweeps, int *iters, double *relres) {
+    if (!e || !rowPtr || !col || !val || !b || !x || !iters || !relres || sweeps < 1 || maxIter < 0)
+        return RACE_ERR_INVALID_ARG;
+    return guard(e, [&] {
+        race::symmGsIr(*e->eng, inner_func_id, n, rowPtr, col, val, b, x, tol, maxIter, sweeps, iters, relres);
+    });
+}
+
 int race_spmv_power_layout(race_engine *e, int func_id, int k) {
     if (!e || func_id < 0 || func_id >= (int)e->eng->funcs.size()) return RACE_ERR_INVALID_ARG;
     return guard(e, [&] {
         race::FuncEntry &f = e->eng->funcs[func_id];
         if (f.kernel != RACE_K_MPK || !f.mpk) throw Error(RACE_ERR_INVALID_ARG, "not a matrix-power function");
         if (k < 0 || k >= f.power) throw Error(RACE_ERR_INVALID_ARG, "k out of range");
-        race::runSpmvSell(*e->eng, *f.mpk, f.ops.x, f.ops.n, k);
+        race::runSpmvSell(*e->eng, *f.mpk, (double *)f.ops.x, f.ops.n, k);
     });
 }
 

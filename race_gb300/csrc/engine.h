@@ -7,12 +7,15 @@
 #include "coloring.h"
 #include "common.cuh"
 #include "lb.h"
+#include "waves.h"
 
 namespace race {
 
+enum SweepMode { SWEEP_AUTO = RACE_SWEEP_AUTO, SWEEP_WAVE = RACE_SWEEP_WAVE, SWEEP_LEAF = RACE_SWEEP_LEAF };
+
 // Device copy of a phase table for the persistent sweep kernel.
 struct DevPhases {
-    int numPhases = 0, numLeaves = 0, maxLeaves = 0;
+    int numPhases = 0, numLeaves = 0, maxLeaves = 0, maxLeafRows = 0;
     DevBuf<int> phasePtr, leafLo, leafHi;
 };
 
@@ -39,11 +42,18 @@ struct MpkPlan {
     DevBuf<int> status;         // 1: device status word
 };
 
+// Device copy of a wave plan (waves.h) of one sweep direction.
+struct DevWaves {
+    int numWaves = 0, maxRows = 0;
+    DevBuf<int> wavePtr, rows;
+};
+
 struct FuncEntry {
     int kernel = 0;
     race_operands ops{};
     int power = 1;
     std::unique_ptr<MpkPlan> mpk;
+    DevWaves waves[2];  // forward, reverse
 };
 
 class Engine {
@@ -81,6 +91,10 @@ class Engine {
     DevBuf<int> dDist, dStamp, dQ0, dQ1, dCtr, dLevelRow, dLevelNnz, dKeys, dVals, dKeysOut, dValsOut, dTmp;
     DevBuf<unsigned char> dCubTemp;
     int stamp = 0;
+
+    // sweep execution: SWEEP_AUTO, SWEEP_WAVE (bit-exact wave plans) or
+    // SWEEP_LEAF (warp per leaf)
+    int sweepMode = SWEEP_AUTO;
 
     // coloring results
     std::unique_ptr<ZoneTree> tree;

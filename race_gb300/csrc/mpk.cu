@@ -416,8 +416,8 @@ void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
     RACE_CUDA(cudaMemsetAsync(plan.done.p, 0, sizeof(int) * (size_t)plan.numChunks * plan.power, s));
     RACE_CUDA(cudaMemsetAsync(plan.ticket.p, 0, sizeof(int), s));
     RACE_CUDA(cudaMemsetAsync(plan.status.p, 0, sizeof(int), s));
-    if (plan.valType != RACE_VAL_F64) kToFloat<<<ceilDiv(ops.n, 256), 256, 0, s>>>(ops.x, plan.xf.p, ops.n);
-    MpkArgs a{viewOf(plan), ops.x, plan.xf.p, ops.n, plan.depRange.p, plan.itemChunk.p, plan.itemPow.p,
+    if (plan.valType != RACE_VAL_F64) kToFloat<<<ceilDiv(ops.n, 256), 256, 0, s>>>((const double *)ops.x, plan.xf.p, ops.n);
+    MpkArgs a{viewOf(plan), (double *)ops.x, plan.xf.p, ops.n, plan.depRange.p, plan.itemChunk.p, plan.itemPow.p,
               plan.numItems, plan.numChunks, plan.done.p, plan.ticket.p, plan.status.p};
     switch (plan.valType) {
     case RACE_VAL_F64: launchMpk<double>(a, s); break;

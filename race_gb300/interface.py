@@ -27,6 +27,7 @@ TWO_BLOCK, THREE_BLOCK = 0, 1
 ROW, NNZ = 0, 1
 FILL, SCATTER = 0, 1
 SPMV, SPMTV, SYMMSPMV, GS, KACZ, MPK = 0, 1, 2, 3, 4, 5
+SWEEP_AUTO, SWEEP_WAVE, SWEEP_LEAF = 0, 1, 2
 VAL_F64, VAL_F32, VAL_BF16 = 0, 1, 2
 _VAL_TYPE = {torch.float64: VAL_F64, torch.float32: VAL_F32, torch.bfloat16: VAL_BF16}
 
@@ -64,9 +65,10 @@ class Operands:
 
     def to_c(self) -> race_operands:
         vt = _VAL_TYPE[self.mat.val.dtype]
+        xt = VAL_F32 if self.x.dtype == torch.float32 else VAL_F64
         return race_operands(self.mat.n, self.mat.row_ptr.data_ptr(), self.mat.col.data_ptr(),
                              self.mat.val.data_ptr(), vt, self.x.data_ptr(),
-                             None if self.b is None else self.b.data_ptr())
+                             None if self.b is None else self.b.data_ptr(), xt)
 
 
 class Interface:
@@ -200,6 +202,16 @@ class Interface:
     def getStatus(self) -> int:
         return lib().race_get_status(self._h)
 
+    def setSweepMode(self, mode: int):
+        """SWEEP_AUTO, SWEEP_WAVE (bit-exact wave plans) or SWEEP_LEAF."""
+        self._check(lib().race_set_sweep_mode(self._h, int(mode)))
+
+    def getSweepInfo(self, funcId: int, rev: bool = False) -> dict:
+        v = [C.c_int() for _ in range(5)]
+        self._check(lib().race_get_sweep_info(self._h, int(funcId), int(bool(rev)), *[C.byref(a) for a in v]))
+        return dict(waves=v[0].value, max_wave_rows=v[1].value, phases=v[2].value, max_leaf_rows=v[3].value,
+                    wave_mode=bool(v[4].value))
+
     def setStream(self, stream: torch.cuda.Stream):
         self.stream = stream
         self._check(lib().race_set_stream(self._h, C.c_void_p(stream.cuda_stream)))
@@ -237,6 +249,17 @@ class Interface:
         self._tuned[funcId] = best
         self.setPower(funcId, best)
         return best
+
+    def symmGsIr(self, innerFuncId: int, mat64: DeviceCsr, b: torch.Tensor, x: torch.Tensor, tol: float = 1e-10,
+                 maxIter: int = 100, sweeps: int = 1):
+        """FP64 iterative refinement around symmetric GS sweeps of a
+        registered (reduced-precision) RACE_K_GS function; returns
+        (refinements, final relative residual)."""
+        it, rel = C.c_int(), C.c_double()
+        self._check(lib().race_symmgs_ir(self._h, int(innerFuncId), mat64.n, _ptr(mat64.row_ptr), _ptr(mat64.col),
+                                         _ptr(mat64.val), _ptr(b), _ptr(x), float(tol), int(maxIter), int(sweeps),
+                                         C.byref(it), C.byref(rel)))
+        return it.value, rel.value
 
     # ---- convenience
     def spmvPowerLayout(self, funcId: int, k: int):
