@@ -165,6 +165,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--symmgs-rows", type=int, default=1 << 20,
+                    help="rows of the power-law SymmGS system (0 skips it; the full configuration is 4194304)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
@@ -281,6 +283,8 @@ def main():
         traffic = json.loads(tpath.read_text()).get("dram_bytes_per_launch")
 
     cpu = cpu_baseline(A, P, x0, args.cpu_seconds) if rank == 0 else None
+    del dm32, x32
+    symmgs = bench_symmgs(args, ri, matgen, torch) if args.symmgs_rows > 0 else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
@@ -303,10 +307,61 @@ def main():
                           "rel_err_vs_f64": rel32, "meets_1e-10": rel32 <= 1e-10},
             "plain_f64": {"ms_per_step": ms_plain, "effective_gbs": eff_bytes / (ms_plain * 1e-3) / 1e9,
                           "hbm_frac": eff_bytes / (ms_plain * 1e-3) / 1e9 / peak},
+            "symmgs_ir": symmgs,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def bench_symmgs(args, ri, matgen, torch):
+    """Symmetric Gauss-Seidel as the smoother of an FP64 iterative refinement
+    on a symmetric power-law system (Chung-Lu, Pareto 2.1 weights, mean
+    degree 16, off-diagonals N(0,1), diagonal = sum|off| + 1), RACE
+    distance-2 coloring, b = A 1, x0 = 0, stop at relative residual 1e-10.
+    Inner sweeps with FP64, FP32 and BF16 values (FP32 vectors for the
+    latter two); residual and update always FP64. Effective bytes use the
+    FP64 model for every variant (one symmetric sweep = 2 (12 nnz + 4(n+1) +
+    24 n), one residual = 12 nnz + 4(n+1) + 16 n per refinement), so the
+    ratio of the GB/s figures is the ratio of the solve speeds."""
+    A = matgen.powerlaw_chung_lu(args.symmgs_rows, seed=0)
+    n, nnz = A.n, A.nnz
+    t0 = time.perf_counter()
+    rc = ri.Interface(n, 4096, ri.TWO, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor() == 0
+    prep = time.perf_counter() - t0
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    m64 = ri.DeviceCsr.from_csr(P)
+    ones = torch.ones(n, dtype=torch.float64, device="cuda")
+    b = torch.zeros(n, dtype=torch.float64, device="cuda")
+    rc.spmv_plain(m64, ones, b)
+    per_it = 2 * (12 * nnz + 4 * (n + 1) + 24 * n) + (12 * nnz + 4 * (n + 1) + 16 * n)
+    out = {"workload": f"power-law n={n} nnz={nnz}, RACE D2 (4096 threads requested -> {rc.getNumThreads()}, "
+                       f"efficiency {rc.getEfficiency():.4f}), b=A*1, tol 1e-10",
+           "preprocessing_s": prep}
+    for name, vdt in [("f64", torch.float64), ("f32", torch.float32), ("bf16", torch.bfloat16)]:
+        xdt = torch.float64 if name == "f64" else torch.float32
+        d = torch.zeros(n, dtype=xdt, device="cuda")
+        r = torch.zeros(n, dtype=xdt, device="cuda")
+        fid = rc.registerFunction(ri.GS, ri.Operands(ri.DeviceCsr(n, m64.row_ptr, m64.col, m64.val.to(vdt)), d, r))
+        x = torch.zeros(n, dtype=torch.float64, device="cuda")
+        rc.symmGsIr(fid, m64, b, x, tol=1e-10, maxIter=1, sweeps=1)  # warm-up
+        x.zero_()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        its, rel = rc.symmGsIr(fid, m64, b, x, tol=1e-10, maxIter=300, sweeps=1)
+        ev1.record()
+        torch.cuda.synchronize()
+        sec = ev0.elapsed_time(ev1) / 1e3
+        info = rc.getSweepInfo(fid)
+        out[name] = {"refinements": its, "rel_residual": rel, "seconds": sec,
+                     "effective_gbs": per_it * its / sec / 1e9,
+                     "max_err_vs_exact": float((x - 1).abs().max()), "waves_per_sweep": info["waves"],
+                     "wave_mode": info["wave_mode"]}
+    out["mixed_f32_speedup_vs_f64"] = out["f64"]["seconds"] / out["f32"]["seconds"]
+    out["mixed_bf16_speedup_vs_f64"] = out["f64"]["seconds"] / out["bf16"]["seconds"]
+    return out
 
 
 def cpu_baseline(A, P, x0, budget_s: float):
