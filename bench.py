@@ -3,7 +3,9 @@
 Workload (one GPU): y_k = A^k x for k = 1..8 on the 27-point stencil of a
 128^3 grid (n = 2,097,152, nnz = 55,742,968; the HPCG-128 shape the reference
 publishes MPK numbers for), FP64 values, permuted with RACE's MPK ordering
-and level groups (cacheSize 100 MB, safety 2). Synthetic data: off-diagonals
+and level groups (cacheSize 300 MB, safety 2: the fastest of 50-500 MB on
+GB300; the host-core reference runs equally fast at 100 and 300 MB).
+Synthetic data: off-diagonals
 U[-1,0) mirrored, diagonal = sum|off| + 1, x ~ U[-1,1] (seeded).
 
 Metric: effective GB/s = p * (nnz*12 + 4(n+1) + 8n + 8n) bytes per call
@@ -40,7 +42,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "MPK/SymmGS effective GB/s & % HBM peak, mixed vs FP64 at 1e-10 rel err"
 GRID = 128
 POWER = 8
-CACHE_BYTES = 100e6
+CACHE_BYTES = 300e6
 # Published RACE MPK p=8 on HPCG-128 (the same shape), best CPU result in the
 # reference's perf data: AMD Rome 49.85 GF/s = 317.9 GB/s effective
 # (examples/matrixPower_perf_test/21_Jan_2021_rome1_nps1/mtxPower.csv:2131).
@@ -158,6 +160,32 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_case(args):
+    """A short, fixed sequence of launches for ncu: --steps MPK calls, then
+    --steps rounds of the p plain SpMVs on the same SELL-32 layout."""
+    import torch
+    from race_gb300 import interface as ri
+    from race_gb300 import matgen
+    dt = torch.float32 if args.values == "f32" else torch.float64
+    A = matgen.stencil3d_27pt(args.grid)
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(POWER, CACHE_BYTES) == 0
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    dm = ri.DeviceCsr.from_csr(P, "cuda", dt)
+    x = torch.zeros((POWER + 1) * A.n, dtype=torch.float64, device="cuda")
+    x[:A.n] = torch.tensor(matgen.uniform_vector(A.n, 0), device="cuda")
+    fid = rc.registerFunction(ri.MPK, ri.Operands(dm, x), power=POWER)
+    assert fid >= 0
+    for _ in range(args.steps):
+        assert rc.executeFunction(fid) == 0
+    for _ in range(args.steps):
+        for k in range(POWER):
+            rc.spmvPowerLayout(fid, k)
+    torch.cuda.synchronize()
+    assert rc.getStatus() == 0
+    print(f"profile case done: grid {args.grid}^3, values {args.values}, {args.steps} MPK calls")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -167,12 +195,24 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the CPU baseline sample")
     ap.add_argument("--symmgs-rows", type=int, default=1 << 20,
                     help="rows of the power-law SymmGS system (0 skips it; the full configuration is 4194304)")
+    ap.add_argument("--profile", choices=["mpk"], default=None,
+                    help="profiling case: register the MPK on a --grid^3 27-point stencil, run it --steps times, "
+                         "then the same powers as --steps rounds of p plain SELL SpMVs; prints no JSON")
+    ap.add_argument("--batch-count", type=int, default=64,
+                    help="matrices of the batched block-MPK measurement (0 skips it)")
+    ap.add_argument("--batch-cache-mb", type=float, default=256.0,
+                    help="RACE cacheSize of each batched matrix (256 MB: fastest of 1-1000 MB on GB300)")
+    ap.add_argument("--grid", type=int, default=GRID)
+    ap.add_argument("--values", choices=["f64", "f32"], default="f64")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
 
+    if args.profile:
+        run_profile_case(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
@@ -285,6 +325,7 @@ def main():
     cpu = cpu_baseline(A, P, x0, args.cpu_seconds) if rank == 0 else None
     del dm32, x32
     symmgs = bench_symmgs(args, ri, matgen, torch) if args.symmgs_rows > 0 else None
+    batched = bench_batch(args, ri, matgen, torch) if args.batch_count > 0 else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
@@ -308,6 +349,7 @@ def main():
             "plain_f64": {"ms_per_step": ms_plain, "effective_gbs": eff_bytes / (ms_plain * 1e-3) / 1e9,
                           "hbm_frac": eff_bytes / (ms_plain * 1e-3) / 1e9 / peak},
             "symmgs_ir": symmgs,
+            "batched_mpk": batched,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -361,6 +403,99 @@ def bench_symmgs(args, ri, matgen, torch):
                      "wave_mode": info["wave_mode"]}
     out["mixed_f32_speedup_vs_f64"] = out["f64"]["seconds"] / out["f32"]["seconds"]
     out["mixed_bf16_speedup_vs_f64"] = out["f64"]["seconds"] / out["bf16"]["seconds"]
+    return out
+
+
+def bench_batch(args, ri, matgen, torch):
+    """Batched block MPK: ``--batch-count`` 2D anisotropic 5/9-point
+    stencils (grid sides U{100..700}, coefficient ratio log-uniform 1-100),
+    16 right-hand sides U[-1,1] each, p = 4, every matrix with its own RACE
+    level groups; all matrices in ONE persistent launch replayed from a CUDA
+    graph, FP64 (values and vectors) and FP32. Compared with the same
+    functions launched one matrix at a time, and with the plain path (p
+    multi-vector SpMV launches per matrix). Compulsory bytes: matrix once
+    (nnz (s+4) + 4 (n+1)) plus the input block and p output blocks
+    (16 (p+1) n xs); the plain path's bytes are p (nnz (s+4) + 4 (n+1) +
+    2 16 n xs)."""
+    p, nrhs = 4, 16
+    mats = matgen.aniso2d_batch(args.batch_count, seed=0)
+    t0 = time.perf_counter()
+    members = []
+    for i, A in enumerate(mats):
+        rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+        assert rc.RACEColor(p, args.batch_cache_mb * 1e6) == 0
+        P = A.permuted(rc.getPerm(), rc.getInvPerm())
+        members.append((rc, P))
+    prep = time.perf_counter() - t0
+    n_tot = sum(P.n for _, P in members)
+    nnz_tot = sum(P.nnz for _, P in members)
+    out = {"workload": f"{len(mats)} matrices (aniso 5/9-point, {n_tot} rows, {nnz_tot} nnz in total), "
+                       f"{nrhs} right-hand sides, p={p}, cacheSize {args.batch_cache_mb} MB each",
+           "preprocessing_s": prep}
+    results = {}
+    for name, vdt, xdt, vs, xs in [("f64", torch.float64, torch.float64, 8, 8),
+                                   ("f32", torch.float32, torch.float32, 4, 4)]:
+        batch = ri.Batch()
+        fns = []
+        for i, (rc, P) in enumerate(members):
+            dm = ri.DeviceCsr.from_csr(P, "cuda", vdt)
+            x = torch.zeros((p + 1) * P.n * nrhs, dtype=xdt, device="cuda")
+            x[: P.n * nrhs] = torch.tensor(matgen.uniform_block(P.n, nrhs, seed=100 + i).reshape(-1),
+                                           dtype=xdt, device="cuda")
+            fid = rc.registerMpkBlock(ri.Operands(dm, x), p, nrhs)
+            assert fid >= 0
+            batch.add(rc, fid)
+            fns.append((rc, fid, dm, x))
+        batch.prepare()
+        compulsory = nnz_tot * (vs + 4) + 4 * (n_tot + len(mats)) + nrhs * (p + 1) * n_tot * xs
+        plain_bytes = p * (nnz_tot * (vs + 4) + 4 * (n_tot + len(mats)) + 2 * nrhs * n_tot * xs)
+
+        def timeit(fn, steps):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(steps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / steps
+
+        def per_matrix():
+            for rc, fid, _, _ in fns:
+                rc.executeFunctionAsync(fid)
+
+        def plain():
+            for rc, fid, _, _ in fns:
+                for k in range(p):
+                    rc.spmvPowerLayout(fid, k)
+
+        steps = max(3, args.steps)
+        ms_graph = timeit(batch.graphLaunch, steps)
+        assert batch.getStatus() == 0
+        ms_launch = timeit(batch.execute, steps)
+        assert batch.getStatus() == 0
+        snap = [x[P.n * nrhs:].clone() for (_, _, _, x), (_, P) in zip(fns, members)]
+        ms_per = timeit(per_matrix, steps)
+        ms_plain = timeit(plain, steps)
+        same = all(torch.equal(s, x[P.n * nrhs:]) for s, (_, _, _, x), (_, P) in zip(snap, fns, members))
+        results[name] = {"ms_graph": ms_graph, "ms_one_launch": ms_launch, "ms_per_matrix_launches": ms_per,
+                         "ms_plain": ms_plain,
+                         "compulsory_gbs": compulsory / (ms_graph * 1e-3) / 1e9,
+                         "plain_equiv_gbs": plain_bytes / (ms_graph * 1e-3) / 1e9,
+                         "plain_path_gbs": plain_bytes / (ms_plain * 1e-3) / 1e9,
+                         "speedup_vs_plain": ms_plain / ms_graph, "speedup_vs_per_matrix": ms_per / ms_graph,
+                         "bit_identical_to_plain_path": bool(same), "launches_per_step": 1}
+        results[name]["_x"] = [x for (_, _, _, x) in fns]
+        del batch
+    rel = 0.0
+    for x64, x32, (_, P) in zip(results["f64"].pop("_x"), results["f32"].pop("_x"), members):
+        a, b = x64[p * P.n * nrhs:], x32[p * P.n * nrhs:].double()
+        rel = max(rel, float((a - b).abs().max() / a.abs().max()))
+    results["f32"]["rel_err_vs_f64"] = rel
+    out.update(results)
+    out["mixed_f32_speedup_vs_f64_plain"] = results["f64"]["ms_plain"] / results["f32"]["ms_graph"]
     return out
 
 

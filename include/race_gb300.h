@@ -76,7 +76,7 @@ typedef struct {
     int val_type;           /* RACE_VAL_* */
     void *x;                /* dev, type vec_type; MPK: (power+1)*n doubles, power-major */
     void *b;                /* dev, type vec_type, n (unused by MPK) */
-    int vec_type;           /* RACE_VAL_F64 or RACE_VAL_F32 (sweeps); MPK vectors are always FP64 */
+    int vec_type;           /* RACE_VAL_F64 or RACE_VAL_F32 (sweeps, block MPK); RACE_K_MPK vectors are FP64 */
 } race_operands;
 
 /* Pre-processing knobs; the reference reads them from the environment
@@ -203,6 +203,45 @@ int race_spmv_power_layout(race_engine *e, int func_id, int k);
 int race_mpk_noalloc(int n, const int *rowPtr_dev, const int *col_dev, const double *val_dev,
                      const int *groupPtr_dev, const int *groupPtr_host, int numGroups, int power, double *x_dev,
                      void *stream);
+
+/* Matrix power over a block of nrhs right-hand sides (nrhs in 1, 2, 4, 8,
+ * 16, 32): x_k = A x_{k-1} for every right-hand side, k = 1..power, on the
+ * engine's level groups. Extends the power callback of registerFunction
+ * (interface.h:151-153, one vector) to a vector block. x (device) holds
+ * (power+1) * n * nrhs elements: power-major, then row, then right-hand side
+ * (x[(k*n + r)*nrhs + j]); x[0 : n*nrhs] is the input block. Types: FP64
+ * values with FP64 x (results equal p sequential fma SpMVs per right-hand
+ * side bit for bit), or FP32/BF16 values with FP32 x (FP32 accumulation).
+ * The matrix must be permuted with the engine's MPK permutation. Executed
+ * with race_execute_function[_async]; race_spmv_power_layout runs one plain
+ * SpMV of it; race_set_power rebuilds its schedule. */
+int race_register_mpk_block(race_engine *e, const race_operands *ops, int power, int nrhs, int *func_id);
+
+/* Batches: block-MPK functions of one or more engines (matrices of any size,
+ * each with its own level groups and power) executed by ONE persistent
+ * kernel launch; members must share value type, vector type and nrhs. No
+ * counterpart in the reference (one matrix per RACE::Interface).
+ * race_batch_add records (engine, function); the batch reads the members'
+ * schedules and operand pointers at race_batch_prepare (called implicitly
+ * by the first execute), so engines and operands must outlive the batch and
+ * a member changed afterwards (race_set_power) needs a new prepare.
+ * race_batch_execute enqueues the launch on `stream` (a cudaStream_t).
+ * race_batch_graph_launch captures that launch sequence once into a CUDA
+ * graph and replays the graph on every call (inputs are read through the
+ * recorded pointers, so new data in the same buffers is picked up).
+ * race_batch_get_status synchronises `stream` and returns RACE_ERR_TIMEOUT
+ * if a device wait of the last launch gave up. race_batch_info reports
+ * members, chunks and work items (0 before prepare). */
+typedef struct race_batch race_batch;
+int race_batch_create(race_batch **out);
+int race_batch_destroy(race_batch *b);
+int race_batch_add(race_batch *b, race_engine *e, int func_id);
+int race_batch_prepare(race_batch *b, void *stream);
+int race_batch_execute(race_batch *b, void *stream);
+int race_batch_graph_launch(race_batch *b, void *stream);
+int race_batch_get_status(race_batch *b, void *stream);
+int race_batch_info(race_batch *b, int *members, int *chunks, int *items);
+const char *race_batch_last_error(race_batch *b);
 
 /* Host-only helpers (no GPU needed), exposed for inspection and tests:
  * the level load balancer (LB::balance, lb.cpp:188-771) on given level data,

@@ -54,6 +54,9 @@ def lib():
         L.orc_exec_tree.argtypes = [C.c_int, IP, IP, IP, IP, IP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                     IP, IP, DP, DP, DP]
         L.orc_mpk_plain.argtypes = [C.c_int, C.c_int, IP, IP, DP, DP]
+        FP = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+        L.orc_mpk_block.argtypes = [C.c_int, C.c_int, C.c_int, IP, IP, DP, DP]
+        L.orc_mpk_block_f32.argtypes = [C.c_int, C.c_int, C.c_int, IP, IP, FP, FP]
         L.orc_mpk_groups.restype = C.c_int
         L.orc_mpk_groups.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_double, C.c_double, C.c_int, C.c_int,
                                      IP, IP, IP, IP, IP]
@@ -128,6 +131,24 @@ def mpk_plain(csr, x0, p: int):
     x[: csr.n] = x0
     lib().orc_mpk_plain(csr.n, p, _i32(csr.row_ptr), _i32(csr.col), _f64(csr.val), x)
     return x.reshape(p + 1, csr.n)
+
+
+def mpk_block(csr, x0, p: int, val=None):
+    """Block matrix power: x0 is (n, nrhs); returns (p+1, n, nrhs). FP64
+    fma chains, or FP32 fmaf chains when x0 is float32 (then ``val`` may give
+    the float32 values, e.g. BF16 values widened exactly)."""
+    x0 = np.asarray(x0)
+    n, nrhs = x0.shape
+    if x0.dtype == np.float32:
+        v = np.ascontiguousarray(csr.val if val is None else val, dtype=np.float32)
+        x = np.zeros((p + 1) * n * nrhs, np.float32)
+        x[: n * nrhs] = x0.reshape(-1)
+        lib().orc_mpk_block_f32(n, p, nrhs, _i32(csr.row_ptr), _i32(csr.col), v, x)
+    else:
+        x = np.zeros((p + 1) * n * nrhs)
+        x[: n * nrhs] = x0.reshape(-1)
+        lib().orc_mpk_block(n, p, nrhs, _i32(csr.row_ptr), _i32(csr.col), _f64(csr.val), x)
+    return x.reshape(p + 1, n, nrhs)
 
 
 def mpk_groups(p: int, nrow: int, nnz: int, cache_bytes: float, safety: float, cutoff: int, level_ptr, level_nnz):

@@ -322,6 +322,40 @@ void orc_mpk_plain(int n, int p, const int *rowPtr, const int *col, const double
     }
 }
 
+/* The same power chain applied to a block of nrhs vectors stored row-major
+ * (x[(k*n + r)*nrhs + j]): each right-hand side is MAT_SPMV_KERNEL's
+ * sequential fma chain (kernels.cpp:749-777), in FP64 and, for the
+ * reduced-precision block path, in FP32 with fmaf. */
+void orc_mpk_block(int n, int p, int nrhs, const int *rowPtr, const int *col, const double *val, double *x) {
+    for (int k = 1; k <= p; ++k) {
+        const double *in = x + (size_t)(k - 1) * n * nrhs;
+        double *out = x + (size_t)k * n * nrhs;
+#pragma omp parallel for schedule(static)
+        for (int row = 0; row < n; ++row)
+            for (int j = 0; j < nrhs; ++j) {
+                double tmp = 0;
+                for (int idx = rowPtr[row]; idx < rowPtr[row + 1]; ++idx)
+                    tmp = fma(val[idx], in[(size_t)col[idx] * nrhs + j], tmp);
+                out[(size_t)row * nrhs + j] = tmp;
+            }
+    }
+}
+
+void orc_mpk_block_f32(int n, int p, int nrhs, const int *rowPtr, const int *col, const float *val, float *x) {
+    for (int k = 1; k <= p; ++k) {
+        const float *in = x + (size_t)(k - 1) * n * nrhs;
+        float *out = x + (size_t)k * n * nrhs;
+#pragma omp parallel for schedule(static)
+        for (int row = 0; row < n; ++row)
+            for (int j = 0; j < nrhs; ++j) {
+                float tmp = 0;
+                for (int idx = rowPtr[row]; idx < rowPtr[row + 1]; ++idx)
+                    tmp = fmaf(val[idx], in[(size_t)col[idx] * nrhs + j], tmp);
+                out[(size_t)row * nrhs + j] = tmp;
+            }
+    }
+}
+
 /* Cache-violation bookkeeping of one MPK stage (matrixPower.cpp:88-99,
  * 134-140): nnz budget of a level = safety * (p+1) * levelNnz; bytes per nnz
  * = (1 + p/nnzr) * 8 + (1 + 1/nnzr) * 4 with nnzr = NNZ/NROW. */

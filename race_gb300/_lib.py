@@ -13,6 +13,7 @@ PKG = pathlib.Path(__file__).resolve().parent
 LIB_PATH = PKG / "_build" / "librace_gb300.so"
 
 RACE_SUCCESS = 0
+RACE_ERR_INVALID_ARG = 1
 ERRORS = {
     0: "RACE_SUCCESS", 1: "RACE_ERR_INVALID_ARG", 2: "RACE_ERR_MATRIX_SYMM", 3: "RACE_ERR_D2_COLOR",
     4: "RACE_ERR_D1_COLOR", 5: "RACE_ERR_GRAPH_TRAVERSAL", 6: "RACE_ERR_INCOMPATIBILITY", 7: "RACE_ERR_HWLOC",
@@ -27,7 +28,9 @@ EXPORTS = [
     "race_get_phases", "race_get_power_groups", "race_register_function", "race_execute_function",
     "race_execute_function_async", "race_get_status", "race_set_sweep_mode", "race_get_sweep_info", "race_set_power",
     "race_get_power", "race_spmv_plain", "race_spmv_power_layout", "race_mpk_noalloc", "race_symmgs_ir",
-    "race_lb_balance", "race_flatten_zone_tree", "race_last_error",
+    "race_lb_balance", "race_flatten_zone_tree", "race_last_error", "race_register_mpk_block",
+    "race_batch_create", "race_batch_destroy", "race_batch_add", "race_batch_prepare", "race_batch_execute",
+    "race_batch_graph_launch", "race_batch_get_status", "race_batch_info", "race_batch_last_error",
 ]
 
 
@@ -76,6 +79,10 @@ def lib():
             "race_symmgs_ir": [vp, i, i, vp, vp, vp, vp, vp, C.c_double, i, i, ip, C.POINTER(C.c_double)],
             "race_lb_balance": [vp, vp, i, i, C.c_double, i, i, i, i, vp, i, ip],
             "race_flatten_zone_tree": [vp, i, i, i, i, i, i, vp, vp, vp, i, ip, ip],
+            "race_register_mpk_block": [vp, C.POINTER(race_operands), i, i, ip],
+            "race_batch_create": [C.POINTER(vp)], "race_batch_destroy": [vp], "race_batch_add": [vp, vp, i],
+            "race_batch_prepare": [vp, vp], "race_batch_execute": [vp, vp], "race_batch_graph_launch": [vp, vp],
+            "race_batch_get_status": [vp, vp], "race_batch_info": [vp, ip, ip, ip],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -83,6 +90,8 @@ def lib():
             fn.restype = C.c_int
         L.race_last_error.argtypes = [vp]
         L.race_last_error.restype = C.c_char_p
+        L.race_batch_last_error.argtypes = [vp]
+        L.race_batch_last_error.restype = C.c_char_p
         _lib = L
     return _lib
 

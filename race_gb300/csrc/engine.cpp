@@ -19,6 +19,10 @@ void runSweep(Engine &e, FuncEntry &f, bool rev);
 bool useWaveMode(const Engine &e, const FuncEntry &f, int dir);
 void symmGsIr(Engine &e, int inner, int n, const int *rowPtr, const int *col, const double *val, const double *b,
               double *x, double tol, int maxIter, int sweeps, int *itersOut, double *relresOut);
+std::unique_ptr<BlockPlan> buildBlockPlan(Engine &e, const race_operands &ops, int power, int nrhs);
+void buildBatchTables(BatchTables &t, const std::vector<const BlockPlan *> &plans, cudaStream_t s);
+void runBatch(BatchTables &t, cudaStream_t s);
+void runBlockSpmv(const BlockPlan &p, int k, cudaStream_t s);
 
 // Interface::RACEColor() (interface.cpp:260-301): level recursion over the
 // whole matrix, then the execution phases of both sweep directions.
@@ -125,10 +129,29 @@ int Engine::registerFunction(int kernel, const race_operands &ops, int power) {
     return (int)funcs.size() - 1;
 }
 
+// Matrix power over nrhs right-hand sides (no counterpart in the reference,
+// whose power callback takes one vector).
+int Engine::registerMpkBlock(const race_operands &ops, int power, int nrhs) {
+    if (ops.n != n) throw Error(RACE_ERR_INVALID_ARG, "operand rows differ from the engine's");
+    if (!ops.rowPtr || !ops.col || !ops.val || !ops.x) throw Error(RACE_ERR_INVALID_ARG, "missing operand");
+    if (dist != DIST_POWER || !powerReady) throw Error(RACE_ERR_INVALID_ARG, "MPK needs RACEColor(power, ...) first");
+    if (power < 1 || power > 255) throw Error(RACE_ERR_INVALID_ARG, "power must be in 1..255");
+    FuncEntry f;
+    f.kernel = RACE_K_MPK;
+    f.ops = ops;
+    f.power = power;
+    f.block = buildBlockPlan(*this, ops, power, nrhs);
+    funcs.push_back(std::move(f));
+    return (int)funcs.size() - 1;
+}
+
 void Engine::launch(int id, bool rev) {
     if (id < 0 || id >= (int)funcs.size()) throw Error(RACE_ERR_INVALID_ARG, "unknown function id");
     FuncEntry &f = funcs[id];
-    if (f.kernel == RACE_K_MPK) {
+    if (f.block) {
+        runBatch(f.block->tables, stream);
+        lastStatus = f.block->tables.status.p;
+    } else if (f.kernel == RACE_K_MPK) {
         runMpk(*this, *f.mpk, f.ops, f.power);
         lastStatus = f.mpk->status.p;
     } else {
@@ -342,7 +365,12 @@ int race_set_power(race_engine *e, int func_id, int power) {
     if (!e || func_id < 0 || func_id >= (int)e->eng->funcs.size()) return RACE_ERR_INVALID_ARG;
     return guard(e, [&] {
         race::FuncEntry &f = e->eng->funcs[func_id];
-        if (f.kernel == RACE_K_MPK && power != f.power) f.mpk = race::buildMpkPlan(*e->eng, f.ops, power);
+        if (f.block && power != f.power) {
+            if (power < 1 || power > 255) throw Error(RACE_ERR_INVALID_ARG, "power must be in 1..255");
+            f.block = race::buildBlockPlan(*e->eng, f.ops, power, f.block->nrhs);
+        } else if (f.kernel == RACE_K_MPK && power != f.power) {
+            f.mpk = race::buildMpkPlan(*e->eng, f.ops, power);
+        }
         f.power = power;
     });
 }
@@ -366,9 +394,13 @@ int race_spmv_power_layout(race_engine *e, int func_id, int k) {
     if (!e || func_id < 0 || func_id >= (int)e->eng->funcs.size()) return RACE_ERR_INVALID_ARG;
     return guard(e, [&] {
         race::FuncEntry &f = e->eng->funcs[func_id];
-        if (f.kernel != RACE_K_MPK || !f.mpk) throw Error(RACE_ERR_INVALID_ARG, "not a matrix-power function");
+        if (f.kernel != RACE_K_MPK || (!f.mpk && !f.block))
+            throw Error(RACE_ERR_INVALID_ARG, "not a matrix-power function");
         if (k < 0 || k >= f.power) throw Error(RACE_ERR_INVALID_ARG, "k out of range");
-        race::runSpmvSell(*e->eng, *f.mpk, (double *)f.ops.x, f.ops.n, k);
+        if (f.block)
+            race::runBlockSpmv(*f.block, k, e->eng->stream);
+        else
+            race::runSpmvSell(*e->eng, *f.mpk, (double *)f.ops.x, f.ops.n, k);
     });
 }
 
@@ -441,5 +473,143 @@ int race_flatten_zone_tree(const int *tree, int treeLen, int dist, int d2type, i
 }
 
 const char *race_last_error(race_engine *e) { return e ? e->err.c_str() : "null engine"; }
+
+int race_register_mpk_block(race_engine *e, const race_operands *ops, int power, int nrhs, int *func_id) {
+    if (!e || !ops || !func_id) return RACE_ERR_INVALID_ARG;
+    return guard(e, [&] { *func_id = e->eng->registerMpkBlock(*ops, power, nrhs); });
+}
+
+}  // extern "C"
+
+// A batch: block-MPK functions of several engines run by one persistent
+// launch; the launch sequence is captured once in a CUDA graph on request.
+struct race_batch {
+    std::vector<std::pair<race_engine *, int>> members;
+    race::BatchTables tables;
+    bool prepared = false;
+    cudaStream_t capture = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::string err;
+    void dropGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+    ~race_batch() {
+        dropGraph();
+        if (capture) cudaStreamDestroy(capture);
+    }
+    void prepare(cudaStream_t s) {
+        std::vector<const race::BlockPlan *> plans;
+        for (auto &m : members) {
+            const auto &funcs = m.first->eng->funcs;
+            if (m.second < 0 || m.second >= (int)funcs.size() || !funcs[m.second].block)
+                throw Error(RACE_ERR_INVALID_ARG, "batch member is not a block-MPK function");
+            plans.push_back(funcs[m.second].block.get());
+        }
+        dropGraph();
+        race::buildBatchTables(tables, plans, s);
+        prepared = true;
+    }
+};
+
+namespace {
+template <typename F>
+int guardBatch(race_batch *b, F &&f) {
+    try {
+        f();
+        return RACE_SUCCESS;
+    } catch (const Error &ex) {
+        b->err = ex.what();
+        return ex.code;
+    } catch (const std::exception &ex) {
+        b->err = ex.what();
+        return RACE_ERR_INTERNAL;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int race_batch_create(race_batch **out) {
+    if (!out) return RACE_ERR_INVALID_ARG;
+    *out = new race_batch;
+    return RACE_SUCCESS;
+}
+
+int race_batch_destroy(race_batch *b) {
+    delete b;
+    return RACE_SUCCESS;
+}
+
+int race_batch_add(race_batch *b, race_engine *e, int func_id) {
+    if (!b || !e) return RACE_ERR_INVALID_ARG;
+    return guardBatch(b, [&] {
+        const auto &funcs = e->eng->funcs;
+        if (func_id < 0 || func_id >= (int)funcs.size() || !funcs[func_id].block)
+            throw Error(RACE_ERR_INVALID_ARG, "not a block-MPK function (race_register_mpk_block)");
+        b->members.emplace_back(e, func_id);
+        b->prepared = false;
+        b->dropGraph();
+    });
+}
+
+int race_batch_prepare(race_batch *b, void *stream) {
+    if (!b) return RACE_ERR_INVALID_ARG;
+    return guardBatch(b, [&] { b->prepare((cudaStream_t)stream); });
+}
+
+int race_batch_execute(race_batch *b, void *stream) {
+    if (!b) return RACE_ERR_INVALID_ARG;
+    return guardBatch(b, [&] {
+        if (!b->prepared) b->prepare((cudaStream_t)stream);
+        race::runBatch(b->tables, (cudaStream_t)stream);
+    });
+}
+
+int race_batch_graph_launch(race_batch *b, void *stream) {
+    if (!b) return RACE_ERR_INVALID_ARG;
+    return guardBatch(b, [&] {
+        if (!b->prepared) b->prepare((cudaStream_t)stream);
+        if (!b->exec) {
+            if (!b->capture) RACE_CUDA(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking));
+            RACE_CUDA(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeRelaxed));
+            try {
+                race::runBatch(b->tables, b->capture);
+            } catch (...) {
+                cudaGraph_t g = nullptr;
+                cudaStreamEndCapture(b->capture, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            RACE_CUDA(cudaStreamEndCapture(b->capture, &b->graph));
+            RACE_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+        }
+        RACE_CUDA(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+    });
+}
+
+int race_batch_get_status(race_batch *b, void *stream) {
+    if (!b) return RACE_ERR_INVALID_ARG;
+    return guardBatch(b, [&] {
+        if (!b->prepared) return;
+        int st = 0;
+        RACE_CUDA(cudaMemcpyAsync(&st, b->tables.status.p, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+        RACE_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+        if (st != race::DEV_OK) throw Error(RACE_ERR_TIMEOUT, "a device wait gave up (schedule dependency)");
+    });
+}
+
+int race_batch_info(race_batch *b, int *members, int *chunks, int *items) {
+    if (!b || !members || !chunks || !items) return RACE_ERR_INVALID_ARG;
+    *members = (int)b->members.size();
+    *chunks = b->prepared ? b->tables.numChunks : 0;
+    *items = b->prepared ? b->tables.numItems : 0;
+    return RACE_SUCCESS;
+}
+
+const char *race_batch_last_error(race_batch *b) { return b ? b->err.c_str() : "null batch"; }
 
 }  // extern "C"

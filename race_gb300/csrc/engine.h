@@ -42,6 +42,42 @@ struct MpkPlan {
     DevBuf<int> status;         // 1: device status word
 };
 
+// Device tables of one persistent block-MPK launch over one or more members
+// (a member = one registered block-MPK function: matrix, x, power). Chunks
+// and items of all members are numbered globally.
+struct BlockMember {
+    const int *rowPtr;
+    const int *col;
+    const void *val;
+    void *x;  // (power+1) * n * nrhs, power-major, then row, right-hand side fastest
+    int n;
+    int power;
+};
+
+struct BatchTables {
+    int valType = 0, vecType = 0, nrhs = 1, maxPower = 0;
+    int numChunks = 0, numItems = 0, numMembers = 0;
+    DevBuf<BlockMember> members;
+    DevBuf<int> chunkMember, chunkRow, chunkEnd;  // numChunks each (local rows)
+    DevBuf<int> depRange;                          // numChunks*6, global chunk ids
+    DevBuf<int> itemChunk;                         // numItems
+    DevBuf<unsigned char> itemPow;                 // numItems
+    DevBuf<int> done;                              // maxPower * numChunks
+    DevBuf<int> ticket, status;
+};
+
+// Schedule of one block-MPK function (local chunk numbering, host copies) and
+// its own single-member tables.
+struct BlockPlan {
+    int n = 0, nrhs = 1, power = 0, valType = 0, vecType = 0, numChunks = 0;
+    race_operands ops{};
+    std::vector<int> chunkRow;   // numChunks+1
+    std::vector<int> depRange;   // numChunks*6 (local chunk ids, empty range [0,-1])
+    std::vector<int> itemChunk;  // wavefront order
+    std::vector<unsigned char> itemPow;
+    BatchTables tables;
+};
+
 // Device copy of a wave plan (waves.h) of one sweep direction.
 struct DevWaves {
     int numWaves = 0, maxRows = 0;
@@ -53,6 +89,7 @@ struct FuncEntry {
     race_operands ops{};
     int power = 1;
     std::unique_ptr<MpkPlan> mpk;
+    std::unique_ptr<BlockPlan> block;  // block MPK (race_register_mpk_block)
     DevWaves waves[2];  // forward, reverse
 };
 
@@ -70,6 +107,7 @@ class Engine {
     long long rangeNnz(int lo, int hi) const;
 
     int registerFunction(int kernel, const race_operands &ops, int power);
+    int registerMpkBlock(const race_operands &ops, int power, int nrhs);
     void execute(int id, bool rev);
     void launch(int id, bool rev);
     void checkStatus();

@@ -398,6 +398,27 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     return plan;
 }
 
+// Host entry to kChunkRanges for other schedules over the same level groups:
+// fills range (6 per chunk, local chunk ids) and returns false if some column
+// lies outside the previous/own/next group of its row.
+bool chunkDependencyRanges(const int *rowPtr, const int *col, const std::vector<int> &chunkRow,
+                           const std::vector<int> &chunkGroup, std::vector<int> &range, cudaStream_t s) {
+    const int C = (int)chunkGroup.size();
+    range.assign((size_t)C * 6, 0);
+    if (C == 0) return true;
+    DevBuf<int> dRow, dGroup, dRange((size_t)C * 6), dBad(1);
+    dRow.upload(chunkRow.data(), chunkRow.size(), s);
+    dGroup.upload(chunkGroup.data(), chunkGroup.size(), s);
+    RACE_CUDA(cudaMemsetAsync(dBad.p, 0, sizeof(int), s));
+    kChunkRanges<<<C, 128, 0, s>>>(rowPtr, col, dRow.p, dGroup.p, C, dRange.p, dBad.p);
+    RACE_CUDA(cudaGetLastError());
+    int bad = 0;
+    RACE_CUDA(cudaMemcpyAsync(range.data(), dRange.p, sizeof(int) * range.size(), cudaMemcpyDeviceToHost, s));
+    RACE_CUDA(cudaMemcpyAsync(&bad, dBad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RACE_CUDA(cudaStreamSynchronize(s));
+    return bad == 0;
+}
+
 namespace {
 SellView viewOf(const MpkPlan &p) {
     return SellView{p.sellVal.p, p.sellCol.p, p.chunkOff.p, p.chunkRow.p, p.rowLen.p};

@@ -94,16 +94,63 @@ __global__ void kIsland(const int *dist, int from, int hi, int *out) {
     if (i < hi && dist[i] == -1) atomicMin(out, i);
 }
 
+// Per-level row and nnz counts plus the (level, row) sort pairs. With few
+// levels (a BFS from a corner of a grid gives ~100) a global atomic per row
+// serialises on a handful of addresses, so each block first counts into
+// shared memory (grid-stride loop) and adds its non-zero bins once. With
+// more levels than fit, rows of a warp that share a level are combined
+// (match.any) before one lane adds for all of them.
+constexpr int kHistSmemLevels = 4096;
+constexpr int kNumSmsHint = 152;  // GB300; only sizes the grid-stride histogram grid
+
 __global__ void kLevelHist(const int *__restrict__ dist, const int *__restrict__ perm, const int *__restrict__ rowPtr,
-                           int lo, int hi, int *levelRow, int *levelNnz, int *keys, int *vals) {
-    int i = lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= hi) return;
-    int d = dist[i];
-    int pr = perm[i];
-    atomicAdd(&levelRow[d], 1);
-    atomicAdd(&levelNnz[d], rowPtr[pr + 1] - rowPtr[pr]);
-    keys[i - lo] = d;
-    vals[i - lo] = i;
+                           int lo, int hi, int numLevels, int *levelRow, int *levelNnz, int *keys, int *vals) {
+    extern __shared__ int sh[];
+    const bool smem = numLevels <= kHistSmemLevels;
+    int *shRow = sh, *shNnz = sh + numLevels;
+    if (smem) {
+        for (int l = threadIdx.x; l < 2 * numLevels; l += blockDim.x) sh[l] = 0;
+        __syncthreads();
+    }
+    const int stride = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    for (int base = lo + blockIdx.x * blockDim.x; base < hi; base += stride) {
+        int i = base + threadIdx.x;
+        bool valid = i < hi;
+        int d = -1, len = 0;
+        if (valid) {
+            d = dist[i];
+            int pr = perm[i];
+            len = rowPtr[pr + 1] - rowPtr[pr];
+            keys[i - lo] = d;
+            vals[i - lo] = i;
+        }
+        if (smem) {
+            if (valid) {
+                atomicAdd(&shRow[d], 1);
+                atomicAdd(&shNnz[d], len);
+            }
+        } else {
+            const unsigned act = __ballot_sync(0xffffffffu, valid);
+            if (valid) {
+                const unsigned peers = __match_any_sync(act, d);
+                const int sumLen = __reduce_add_sync(peers, len);
+                if (lane == __ffs(peers) - 1) {
+                    atomicAdd(&levelRow[d], __popc(peers));
+                    atomicAdd(&levelNnz[d], sumLen);
+                }
+            }
+        }
+    }
+    if (smem) {
+        __syncthreads();
+        for (int l = threadIdx.x; l < numLevels; l += blockDim.x) {
+            if (shRow[l]) {
+                atomicAdd(&levelRow[l], shRow[l]);
+                atomicAdd(&levelNnz[l], shNnz[l]);
+            }
+        }
+    }
 }
 
 // totalPerm'[i] = totalPerm[order[i-lo]]; totalInvPerm'[totalPerm'[i]] = i.
@@ -315,7 +362,12 @@ LevelData Engine::traverse(int lo, int hi, int mode, const std::string &mtxType)
     DevBuf<int> lr(std::max(totalLevel, 1)), ln(std::max(totalLevel, 1));
     RACE_CUDA(cudaMemsetAsync(lr.p, 0, sizeof(int) * lr.n, s));
     RACE_CUDA(cudaMemsetAsync(ln.p, 0, sizeof(int) * ln.n, s));
-    kLevelHist<<<blocksFor(len, 256), 256, 0, s>>>(dDist.p, dPerm.p, dRowPtr.p, lo, hi, lr.p, ln.p, dKeys.p, dVals.p);
+    {
+        const size_t smem = totalLevel <= kHistSmemLevels ? sizeof(int) * 2 * totalLevel : 0;
+        const int blocks = std::min(blocksFor(len, 256), smem ? 2 * kNumSmsHint : 1 << 30);
+        kLevelHist<<<blocks, 256, smem, s>>>(dDist.p, dPerm.p, dRowPtr.p, lo, hi, totalLevel, lr.p, ln.p, dKeys.p,
+                                             dVals.p);
+    }
     ld.levelRow.resize(totalLevel);
     ld.levelNnz.resize(totalLevel);
     RACE_CUDA(cudaMemcpyAsync(ld.levelRow.data(), lr.p, sizeof(int) * totalLevel, cudaMemcpyDeviceToHost, s));

@@ -185,11 +185,28 @@ class Interface:
     # ---- execution (interface.h:149-174)
     def registerFunction(self, kernel: int, args: Operands, power: int = 1) -> int:
         fid = C.c_int(-1)
+        if kernel == MPK and (args.x.dtype != torch.float64 or args.x.numel() < (power + 1) * args.mat.n):
+            return _lib.RACE_ERR_INVALID_ARG  # x must hold (power+1)*n doubles
         ops = args.to_c()
         rc = lib().race_register_function(self._h, int(kernel), C.byref(ops), int(power), C.byref(fid))
         if rc != _lib.RACE_SUCCESS:
             return rc  # the reference returns the error code in place of an id (interface.cpp:429)
         self._funcs[fid.value] = args  # keep operand tensors alive
+        return fid.value
+
+    def registerMpkBlock(self, args: Operands, power: int, nrhs: int) -> int:
+        """Matrix power over nrhs right-hand sides (race_register_mpk_block):
+        ``args.x`` holds (power+1)*n*nrhs values, power-major, then row, then
+        right-hand side; FP64 values with FP64 x or FP32/BF16 values with FP32
+        x. Returns a function id, or an error code like registerFunction."""
+        if args.x.numel() < (power + 1) * args.mat.n * nrhs or not args.x.is_contiguous():
+            return _lib.RACE_ERR_INVALID_ARG
+        fid = C.c_int(-1)
+        ops = args.to_c()
+        rc = lib().race_register_mpk_block(self._h, C.byref(ops), int(power), int(nrhs), C.byref(fid))
+        if rc != _lib.RACE_SUCCESS:
+            return rc
+        self._funcs[fid.value] = args
         return fid.value
 
     def executeFunction(self, funcId: int, rev: bool = False) -> int:
@@ -270,3 +287,55 @@ class Interface:
     def spmv_plain(self, mat: DeviceCsr, x: torch.Tensor, b: torch.Tensor):
         self._check(lib().race_spmv_plain(self._h, mat.n, _ptr(mat.row_ptr), _ptr(mat.col), _ptr(mat.val), _ptr(x),
                                           _ptr(b)))
+
+
+def _stream_ptr(stream: Optional[torch.cuda.Stream]):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+class Batch:
+    """Block-MPK functions of several Interfaces run by one persistent launch
+    (race_batch_*); ``graphLaunch`` replays a CUDA graph of that launch.
+    The Interfaces and operand tensors must outlive the batch; prepare() again
+    after changing a member (setPower)."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        check(lib().race_batch_create(C.byref(h)))
+        self._h = h
+        self._members = []
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().race_batch_destroy(h)
+            self._h = None
+
+    close = __del__
+
+    def _check(self, rc):
+        if rc != _lib.RACE_SUCCESS:
+            m = lib().race_batch_last_error(self._h)
+            raise _lib.RaceError(rc, m.decode() if m else "")
+
+    def add(self, iface: Interface, funcId: int):
+        self._check(lib().race_batch_add(self._h, iface._h, int(funcId)))
+        self._members.append(iface)
+
+    def prepare(self, stream: Optional[torch.cuda.Stream] = None):
+        self._check(lib().race_batch_prepare(self._h, _stream_ptr(stream)))
+
+    def execute(self, stream: Optional[torch.cuda.Stream] = None):
+        self._check(lib().race_batch_execute(self._h, _stream_ptr(stream)))
+
+    def graphLaunch(self, stream: Optional[torch.cuda.Stream] = None):
+        self._check(lib().race_batch_graph_launch(self._h, _stream_ptr(stream)))
+
+    def getStatus(self, stream: Optional[torch.cuda.Stream] = None) -> int:
+        return lib().race_batch_get_status(self._h, _stream_ptr(stream))
+
+    def info(self) -> dict:
+        v = [C.c_int() for _ in range(3)]
+        self._check(lib().race_batch_info(self._h, *[C.byref(a) for a in v]))
+        return dict(members=v[0].value, chunks=v[1].value, items=v[2].value)

@@ -230,3 +230,23 @@ def banded_scrambled(n: int, bandwidth: int, seed: int = 0, fill: float = 0.5) -
 def uniform_vector(n: int, seed: int = 0, lo: float = -1.0, hi: float = 1.0) -> np.ndarray:
     rng = np.random.Generator(np.random.PCG64(seed))
     return rng.uniform(lo, hi, n)
+
+
+def aniso2d_batch(count: int, seed: int = 0, lo: int = 100, hi: int = 700):
+    """``count`` 2D anisotropic stencils of uneven size: grid nx, ny drawn
+    from U{lo..hi}, 5- or 9-point with equal odds, coefficient ratio
+    log-uniform on [1, 100] (PCG64 seeded)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    mats = []
+    for _ in range(count):
+        nx, ny = (int(v) for v in rng.integers(lo, hi + 1, size=2))
+        pts = 5 if rng.random() < 0.5 else 9
+        ratio = float(np.exp(rng.uniform(0.0, np.log(100.0))))
+        mats.append(aniso2d(nx, ny, pts, ratio))
+    return mats
+
+
+def uniform_block(n: int, nrhs: int, seed: int = 0) -> np.ndarray:
+    """n x nrhs right-hand sides, U[-1,1] (PCG64 seeded), row-major."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return rng.uniform(-1.0, 1.0, size=(n, nrhs))

@@ -95,3 +95,18 @@ def test_oracle_detects_planted_schedule_error(mats):
     assert len(gp) > 2
     Z = orc.mpk_wavefront(P, x0, 4, gp[:-1].copy(), ur, dr, 1)  # last group dropped
     assert not np.array_equal(Z, Y)
+
+
+def test_block_mpk_oracle_is_per_column_chain(mats):
+    """The block matrix power restatement equals the single-vector fma chain
+    (MAT_SPMV_KERNEL, kernels.cpp:749-777) on every right-hand side."""
+    from race_gb300 import matgen
+    A = mats["aniso9_100x80"]
+    X0 = matgen.uniform_block(A.n, 4, seed=7)
+    blk = orc.mpk_block(A, X0, 3)
+    for j in range(4):
+        np.testing.assert_array_equal(blk[:, :, j], orc.mpk_plain(A, X0[:, j], 3))
+    X32 = X0.astype(np.float32)
+    blk32 = orc.mpk_block(A, X32, 3)
+    assert blk32.dtype == np.float32
+    np.testing.assert_allclose(blk32[3], blk[3], rtol=0, atol=1e-4 * np.abs(blk[3]).max())
