@@ -243,6 +243,30 @@ int race_batch_get_status(race_batch *b, void *stream);
 int race_batch_info(race_batch *b, int *members, int *chunks, int *items);
 const char *race_batch_last_error(race_batch *b);
 
+/* Multilayer perceptron of the parameter tuner (FP32; no counterpart in the
+ * reference, whose only tuning is the wall-clock power sweep of
+ * Interface::tuneFunction, interface.cpp:605-647). Shape: `in` inputs,
+ * `hidden_layers` ReLU layers of `hidden` units, `out` linear outputs; every
+ * layer y = x W^T + b with W row-major [out_l][in_l], parameters flattened
+ * layer by layer as W then b (race_mlp_num_params values, all zero after
+ * create). X, T and Y are device arrays, row-major [batch][in|out].
+ * race_mlp_loss_grad evaluates the mean squared error sum (y-t)^2/(batch*out)
+ * and its gradient with respect to every parameter (kept on the device;
+ * copied to grad_host when non-NULL; *loss_host likewise), synchronising
+ * `stream` when it copies. race_mlp_adam_step applies one Adam update with
+ * the last gradient. */
+typedef struct race_mlp race_mlp;
+int race_mlp_create(race_mlp **out, int in, int hidden, int hidden_layers, int out_dim);
+int race_mlp_destroy(race_mlp *m);
+int race_mlp_num_params(race_mlp *m, long long *count);
+int race_mlp_set_params(race_mlp *m, const float *params_host, long long count);
+int race_mlp_get_params(race_mlp *m, float *params_host, long long count);
+int race_mlp_forward(race_mlp *m, const float *X_dev, int batch, float *Y_dev, void *stream);
+int race_mlp_loss_grad(race_mlp *m, const float *X_dev, const float *T_dev, int batch, float *loss_host,
+                       float *grad_host, void *stream);
+int race_mlp_adam_step(race_mlp *m, float lr, float beta1, float beta2, float eps, void *stream);
+const char *race_mlp_last_error(race_mlp *m);
+
 /* Host-only helpers (no GPU needed), exposed for inspection and tests:
  * the level load balancer (LB::balance, lb.cpp:188-771) on given level data,
  * out = [nScale, scale..., totalBlocks, zonePtr(totalBlocks+1)...,

@@ -31,6 +31,8 @@ EXPORTS = [
     "race_lb_balance", "race_flatten_zone_tree", "race_last_error", "race_register_mpk_block",
     "race_batch_create", "race_batch_destroy", "race_batch_add", "race_batch_prepare", "race_batch_execute",
     "race_batch_graph_launch", "race_batch_get_status", "race_batch_info", "race_batch_last_error",
+    "race_mlp_create", "race_mlp_destroy", "race_mlp_num_params", "race_mlp_set_params", "race_mlp_get_params",
+    "race_mlp_forward", "race_mlp_loss_grad", "race_mlp_adam_step", "race_mlp_last_error",
 ]
 
 
@@ -83,6 +85,11 @@ def lib():
             "race_batch_create": [C.POINTER(vp)], "race_batch_destroy": [vp], "race_batch_add": [vp, vp, i],
             "race_batch_prepare": [vp, vp], "race_batch_execute": [vp, vp], "race_batch_graph_launch": [vp, vp],
             "race_batch_get_status": [vp, vp], "race_batch_info": [vp, ip, ip, ip],
+            "race_mlp_create": [C.POINTER(vp), i, i, i, i], "race_mlp_destroy": [vp],
+            "race_mlp_num_params": [vp, C.POINTER(C.c_longlong)], "race_mlp_set_params": [vp, vp, C.c_longlong],
+            "race_mlp_get_params": [vp, vp, C.c_longlong], "race_mlp_forward": [vp, vp, i, vp, vp],
+            "race_mlp_loss_grad": [vp, vp, vp, i, vp, vp, vp],
+            "race_mlp_adam_step": [vp, C.c_float, C.c_float, C.c_float, C.c_float, vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -92,6 +99,8 @@ def lib():
         L.race_last_error.restype = C.c_char_p
         L.race_batch_last_error.argtypes = [vp]
         L.race_batch_last_error.restype = C.c_char_p
+        L.race_mlp_last_error.argtypes = [vp]
+        L.race_mlp_last_error.restype = C.c_char_p
         _lib = L
     return _lib
 

@@ -69,9 +69,12 @@ struct DevBuf {
         p = nullptr;
         n = 0;
     }
+    // Copies count elements from h; h may be null (an empty host vector's
+    // data()) when the caller only needs a placeholder of at least one
+    // element, which is then allocated but left unset.
     void upload(const T *h, size_t count, cudaStream_t s = 0) {
         ensure(count);
-        if (count) RACE_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+        if (count && h) RACE_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
     }
 };
 

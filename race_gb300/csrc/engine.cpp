@@ -52,7 +52,16 @@ void Engine::powerPrepare(int hp, double cacheSize, double safety, const std::st
     highestPower = hp;
     highestSubPower = subPow;
     const int P = hp * subPow;
-    LevelData ld = traverse(0, n, DIST_POWER, mtxType);
+    // The BFS levels depend on neither the power nor the cache budget: a
+    // repeated call (a parameter search) regroups the cached levels instead
+    // of traversing the already permuted matrix again, so the permutation
+    // stays the one of the first call.
+    if (!powerLevelsCached || powerLevelsType != mtxType) {
+        powerLevels = traverse(0, n, DIST_POWER, mtxType);
+        powerLevelsType = mtxType;
+        powerLevelsCached = true;
+    }
+    const LevelData &ld = powerLevels;
     const int L = ld.totalLevel;
     levelPtr.assign(L + 1, 0);
     for (int l = 0; l < L; ++l) levelPtr[l + 1] = levelPtr[l] + ld.levelRow[l];

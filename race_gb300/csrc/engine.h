@@ -30,7 +30,14 @@ struct MpkPlan {
     long long sellSlots = 0;    // SELL entries including padding
     DevBuf<long long> chunkOff; // numChunks: first SELL slot of each chunk
     DevBuf<int> chunkRow;       // numChunks+1: first row of each chunk
-    DevBuf<int> rowLen;         // n: non-zeros per row
+    DevBuf<int> rowLen;         // n: non-zeros per row (-1: hub row, stored apart)
+    // hub rows (more than kHubRowLen entries): contiguous CRS copies, summed
+    // by a whole warp; the chunks' SELL width ignores them
+    int numHubs = 0;
+    DevBuf<int> hubChunkStart;  // numChunks+1: hubs of chunk c are [start[c], start[c+1])
+    DevBuf<int> hubRow, hubPtr; // numHubs, numHubs+1
+    DevBuf<unsigned char> hubVal;  // hub entries (type valType)
+    DevBuf<int> hubCol;
     DevBuf<unsigned char> sellVal;  // sellSlots values (type valType)
     DevBuf<int> sellCol;        // sellSlots column indices
     DevBuf<float> xf;           // (power+1)*n FP32 powers (reduced-precision storage)
@@ -146,6 +153,9 @@ class Engine {
     bool powerReady = false;
     int highestPower = 1, highestSubPower = 1;
     std::vector<int> levelPtr, groupPtr, unlockRow, dangerRow;
+    bool powerLevelsCached = false;
+    std::string powerLevelsType;
+    LevelData powerLevels;
 
     std::vector<FuncEntry> funcs;
     DevBuf<int> dStatus;

@@ -15,7 +15,11 @@
 // FP64 output is bit-identical to p sequential SpMVs with fused
 // multiply-adds. Padding slots are never computed (lanes stop at their row
 // length). One lane per row keeps GB300's FP64 pipe (1/64 of the FP32 rate)
-// busy with useful fmas only.
+// busy with useful fmas only. Rows of more than kHubRowLen entries (hubs of
+// power-law graphs) would stall their lane and pad their whole chunk: they
+// are kept out of the SELL width, copied contiguously and summed by the
+// whole warp (32 ordered partial chains and a fixed butterfly), which
+// matches the sequential sum to rounding rather than bit for bit.
 //
 // Schedule. A work item is (power, chunk). Items are listed in wavefront
 // order and taken by persistent warps from a global ticket; each warp is an
@@ -42,6 +46,8 @@
 namespace race {
 
 constexpr int kWarpThreads = 256;
+// Rows longer than this are summed by a whole warp from a contiguous copy.
+constexpr int kHubRowLen = 256;
 
 namespace {
 
@@ -84,7 +90,11 @@ struct SellView {
     const int *col;
     const long long *chunkOff;  // numChunks: element offset of each chunk
     const int *chunkRow;        // numChunks+1: first row of each chunk
-    const int *rowLen;          // n
+    const int *rowLen;          // n (-1: hub row)
+    const int *hubChunkStart;   // numChunks+1
+    const int *hubRow, *hubPtr;
+    const void *hubVal;
+    const int *hubCol;
 };
 
 // One row of a SELL-32 chunk, FP64 storage: lane-owned fma chain.
@@ -105,19 +115,59 @@ __device__ __forceinline__ float sellRowF(const VT *__restrict__ val, const int 
     return t;
 }
 
-// The lane's row of chunk c at power k -> k+1.
+// A hub row summed by the whole warp: lane l takes entries l, l+32, ... in
+// order (one fma chain per lane, coalesced reads of the contiguous copy),
+// then a fixed butterfly combines the 32 partial sums. Deterministic, but
+// not the sequential order of the short rows: results agree with the
+// single-chain sum to rounding (relative 1e-15 scale), not bit for bit.
+template <typename VT, typename AT>
+__device__ __forceinline__ AT hubSum(const SellView &m, int h, const AT *x) {
+    const int lane = threadIdx.x & 31;
+    const VT *__restrict__ val = (const VT *)m.hubVal;
+    AT t = AT(0);
+    for (int e = m.hubPtr[h] + lane; e < m.hubPtr[h + 1]; e += 32) {
+        if constexpr (sizeof(VT) == 8)
+            t = fma(val[e], x[m.hubCol[e]], t);
+        else
+            t = fmaf(toF<VT>(val[e]), x[m.hubCol[e]], t);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+}
+
+// Chunk c at power k -> k+1: the lane's row (unless it is a hub row), then
+// the chunk's hub rows one at a time with the whole warp. Called by all 32
+// lanes of a warp.
 template <typename VT>
 __device__ __forceinline__ void chunkRow(const SellView &m, int c, int k, int n, double *x, float *xf) {
     const int lane = threadIdx.x & 31;
     const int r = m.chunkRow[c] + lane;
-    if (r >= m.chunkRow[c + 1]) return;
-    const long long off = m.chunkOff[c] + lane;
-    if constexpr (sizeof(VT) == 8) {
-        x[(size_t)(k + 1) * n + r] = sellRowD((const double *)m.val, m.col, off, m.rowLen[r], x + (size_t)k * n);
-    } else {
-        const float v = sellRowF<VT>((const VT *)m.val, m.col, off, m.rowLen[r], xf + (size_t)k * n);
-        xf[(size_t)(k + 1) * n + r] = v;
-        x[(size_t)(k + 1) * n + r] = floatToDoubleExact(v);
+    if (r < m.chunkRow[c + 1]) {
+        const int len = m.rowLen[r];
+        const long long off = m.chunkOff[c] + lane;
+        if (len >= 0) {
+            if constexpr (sizeof(VT) == 8) {
+                x[(size_t)(k + 1) * n + r] = sellRowD((const double *)m.val, m.col, off, len, x + (size_t)k * n);
+            } else {
+                const float v = sellRowF<VT>((const VT *)m.val, m.col, off, len, xf + (size_t)k * n);
+                xf[(size_t)(k + 1) * n + r] = v;
+                x[(size_t)(k + 1) * n + r] = floatToDoubleExact(v);
+            }
+        }
+    }
+    for (int h = m.hubChunkStart[c]; h < m.hubChunkStart[c + 1]; ++h) {
+        const int hr = m.hubRow[h];
+        if constexpr (sizeof(VT) == 8) {
+            const double v = hubSum<VT, double>(m, h, x + (size_t)k * n);
+            if (lane == 0) x[(size_t)(k + 1) * n + hr] = v;
+        } else {
+            const float v = hubSum<VT, float>(m, h, xf + (size_t)k * n);
+            if (lane == 0) {
+                xf[(size_t)(k + 1) * n + hr] = v;
+                x[(size_t)(k + 1) * n + hr] = floatToDoubleExact(v);
+            }
+        }
     }
 }
 
@@ -203,7 +253,23 @@ __global__ void kSpmvCrs(int n, const int *__restrict__ rowPtr, const int *__res
     b[r] = t;
 }
 
+// Contiguous copies of the hub rows, one warp per hub.
+template <typename VT>
+__global__ void kGatherHubs(const int *__restrict__ rowPtr, const int *__restrict__ col, const VT *__restrict__ val,
+                            const int *__restrict__ hubRow, const int *__restrict__ hubPtr, int numHubs,
+                            VT *__restrict__ hval, int *__restrict__ hcol) {
+    const int h = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (h >= numHubs) return;
+    const int s = rowPtr[hubRow[h]], len = hubPtr[h + 1] - hubPtr[h];
+    for (int j = threadIdx.x & 31; j < len; j += 32) {
+        hval[hubPtr[h] + j] = val[s + j];
+        hcol[hubPtr[h] + j] = col[s + j];
+    }
+}
+
 // CRS -> SELL-32 copy; padding slots get value 0 and the row's own column.
+// Hub rows are longer than the chunk width L: their first L entries are
+// copied and never read.
 template <typename VT>
 __global__ void kToSell(const int *__restrict__ rowPtr, const int *__restrict__ col, const VT *__restrict__ val,
                         const long long *__restrict__ chunkOff, const int *__restrict__ chunkRowP,
@@ -300,9 +366,18 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     const int G = (int)gp.size() - 1;
     // chunks of <= 32 rows inside groups
     std::vector<int> chunkRowH{0}, chunkLen, chunkGroup, rowLen(n);
+    std::vector<int> hubRowH, hubPtrH{0}, hubStartH{0};
     std::vector<long long> chunkOff;
     long long off = 0;
-    for (int r = 0; r < n; ++r) rowLen[r] = rp[r + 1] - rp[r];
+    for (int r = 0; r < n; ++r) {
+        rowLen[r] = rp[r + 1] - rp[r];
+        if (rowLen[r] > kHubRowLen) {
+            hubRowH.push_back(r);
+            hubPtrH.push_back(hubPtrH.back() + rowLen[r]);
+            rowLen[r] = -1;
+        }
+    }
+    size_t hubIdx = 0;
     for (int g = 0; g < G; ++g)
         for (int r = gp[g]; r < gp[g + 1]; r += 32) {
             int r1 = std::min(gp[g + 1], r + 32);
@@ -313,8 +388,17 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
             chunkRowH.push_back(r1);
             chunkGroup.push_back(g);
             off += 32LL * L;
+            while (hubIdx < hubRowH.size() && hubRowH[hubIdx] < r1) ++hubIdx;
+            hubStartH.push_back((int)hubIdx);
         }
     const int C = (int)chunkLen.size();
+    const int H = (int)hubRowH.size();
+    plan->numHubs = H;
+    plan->hubChunkStart.upload(hubStartH.data(), hubStartH.size(), s);
+    plan->hubRow.upload(H ? hubRowH.data() : nullptr, std::max(H, 1), s);
+    plan->hubPtr.upload(hubPtrH.data(), hubPtrH.size(), s);
+    plan->hubVal.alloc(std::max<long long>(hubPtrH.back(), 1) * valBytes(ops.val_type));
+    plan->hubCol.alloc(std::max<long long>(hubPtrH.back(), 1));
     plan->numChunks = C;
     plan->power = power;
     plan->valType = ops.val_type;
@@ -328,21 +412,32 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     plan->sellCol.alloc(std::max<long long>(off, 1));
     if (ops.val_type != RACE_VAL_F64) plan->xf.alloc((size_t)(power + 1) * n);
     const int blocksC = ceilDiv(std::max(C, 1), 8);
+    const int blocksH = ceilDiv(std::max(H, 1), 8);
     switch (ops.val_type) {
     case RACE_VAL_F64:
         kToSell<double><<<blocksC, 256, 0, s>>>(ops.rowPtr, ops.col, (const double *)ops.val, plan->chunkOff.p,
                                                 plan->chunkRow.p, dChunkLen.p, C, (double *)plan->sellVal.p,
                                                 plan->sellCol.p);
+        if (H)
+            kGatherHubs<double><<<blocksH, 256, 0, s>>>(ops.rowPtr, ops.col, (const double *)ops.val, plan->hubRow.p,
+                                                        plan->hubPtr.p, H, (double *)plan->hubVal.p, plan->hubCol.p);
         break;
     case RACE_VAL_F32:
         kToSell<float><<<blocksC, 256, 0, s>>>(ops.rowPtr, ops.col, (const float *)ops.val, plan->chunkOff.p,
                                                plan->chunkRow.p, dChunkLen.p, C, (float *)plan->sellVal.p,
                                                plan->sellCol.p);
+        if (H)
+            kGatherHubs<float><<<blocksH, 256, 0, s>>>(ops.rowPtr, ops.col, (const float *)ops.val, plan->hubRow.p,
+                                                       plan->hubPtr.p, H, (float *)plan->hubVal.p, plan->hubCol.p);
         break;
     case RACE_VAL_BF16:
         kToSell<__nv_bfloat16><<<blocksC, 256, 0, s>>>(ops.rowPtr, ops.col, (const __nv_bfloat16 *)ops.val,
                                                         plan->chunkOff.p, plan->chunkRow.p, dChunkLen.p, C,
                                                         (__nv_bfloat16 *)plan->sellVal.p, plan->sellCol.p);
+        if (H)
+            kGatherHubs<__nv_bfloat16><<<blocksH, 256, 0, s>>>(ops.rowPtr, ops.col, (const __nv_bfloat16 *)ops.val,
+                                                               plan->hubRow.p, plan->hubPtr.p, H,
+                                                               (__nv_bfloat16 *)plan->hubVal.p, plan->hubCol.p);
         break;
     default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
     }
@@ -421,7 +516,8 @@ bool chunkDependencyRanges(const int *rowPtr, const int *col, const std::vector<
 
 namespace {
 SellView viewOf(const MpkPlan &p) {
-    return SellView{p.sellVal.p, p.sellCol.p, p.chunkOff.p, p.chunkRow.p, p.rowLen.p};
+    return SellView{p.sellVal.p, p.sellCol.p, p.chunkOff.p, p.chunkRow.p, p.rowLen.p,
+                    p.hubChunkStart.p, p.hubRow.p, p.hubPtr.p, p.hubVal.p, p.hubCol.p};
 }
 
 template <typename VT>

@@ -194,9 +194,15 @@ def test_symmgs_iterative_refinement(mats, inner):
     assert np.max(np.abs(xh - 1.0)) < 1e-8  # the exact solution is all ones
 
 
+HUB_ROW_LEN = 256  # rows longer than this are summed by a warp (mpk.cu kHubRowLen)
+
+
 @pytest.mark.parametrize("m,p,c", POWER_CASES)
 def test_mpk_fp64_bit_exact(golden, mats, m, p, c):
-    """Level-blocked MPK in FP64 equals p sequential fma SpMVs bit for bit."""
+    """Level-blocked MPK in FP64 equals p sequential fma SpMVs bit for bit;
+    with rows above HUB_ROW_LEN entries (warp-summed) every power stays
+    within 1e-12 relative, and the other rows of the first power are still
+    exact."""
     A = mats[m]
     rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
     assert rc.RACEColor(p, c) == 0
@@ -209,10 +215,18 @@ def test_mpk_fp64_bit_exact(golden, mats, m, p, c):
     x[: A.n] = torch.tensor(x0, device="cuda")
     fid = rc.registerFunction(ri.MPK, ri.Operands(dm, x), power=p)
     assert fid >= 0
+    lens = np.diff(P.row_ptr)
+    hubs = lens > HUB_ROW_LEN
     for _ in range(2):  # repeated calls reuse the plan
         assert rc.executeFunction(fid) == 0
         torch.cuda.synchronize()
-        np.testing.assert_array_equal(x.cpu().numpy().reshape(p + 1, A.n), Y)
+        got = x.cpu().numpy().reshape(p + 1, A.n)
+        if not hubs.any():
+            np.testing.assert_array_equal(got, Y)
+        else:
+            np.testing.assert_array_equal(got[1][~hubs], Y[1][~hubs])
+            for kk in range(1, p + 1):
+                assert _rel_err(got[kk], Y[kk]) <= 1e-12
 
 
 def test_mpk_full_size_c2(golden):

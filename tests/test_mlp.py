@@ -1,0 +1,67 @@
+"""The tuner's MLP kernels (forward, MSE gradient, Adam) against the CPU
+oracle, and the trained cost model's gain over the method without it on the
+committed search timings. Needs a GB300."""
+import pathlib
+
+import numpy as np
+import pytest
+
+from oracle import mlp_ref
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from race_gb300 import tuner  # noqa: E402
+
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden" / "tuner_search.npz"
+
+
+def _data(batch, n_in, n_out, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return rng.normal(size=(batch, n_in)).astype(np.float32), rng.normal(size=(batch, n_out)).astype(np.float32)
+
+
+@pytest.mark.parametrize("dims,batch", [((32, 128, 3, 1), 200), ((7, 40, 2, 3), 33), ((5, 17, 1, 2), 1)])
+def test_mlp_forward_and_gradient_match_cpu_oracle(dims, batch):
+    net = tuner.Mlp(*dims, seed=3)
+    theta = net.get_params()
+    X, T = _data(batch, dims[0], dims[3], 5)
+    Xt, Tt = torch.tensor(X, device="cuda"), torch.tensor(T, device="cuda")
+    y = net.forward(Xt).cpu().numpy()
+    acts = mlp_ref.forward(theta.astype(np.float64), X.astype(np.float64), dims)
+    np.testing.assert_allclose(y, acts[-1], rtol=0, atol=1e-5 * max(1.0, np.abs(acts[-1]).max()))
+    loss, g = net.loss_grad(Xt, Tt)
+    loss_ref, g_ref = mlp_ref.loss_grad(theta.astype(np.float64), X.astype(np.float64), T.astype(np.float64), dims)
+    assert abs(loss - loss_ref) <= 1e-5 * max(1.0, loss_ref)
+    # FP32 kernels against a float64 oracle: per-parameter error relative to
+    # the largest gradient entry
+    assert np.max(np.abs(g - g_ref)) <= 1e-4 * np.max(np.abs(g_ref))
+
+
+def test_mlp_adam_training_fits_a_function():
+    rng = np.random.Generator(np.random.PCG64(1))
+    X = rng.uniform(-1, 1, size=(2048, 4)).astype(np.float32)
+    T = (np.sin(3 * X[:, :1]) + X[:, 1:2] ** 2 - 0.5 * X[:, 2:3] * X[:, 3:4]).astype(np.float32)
+    net = tuner.Mlp(4, 64, 2, 1, seed=2)
+    hist = net.train(torch.tensor(X, device="cuda"), torch.tensor(T, device="cuda"), epochs=60, batch=128, lr=3e-3)
+    assert hist[-1] < 0.05 * hist[0]
+
+
+@pytest.mark.skipif(not GOLDEN.exists(), reason="no committed search timings")
+def test_cost_model_beats_best_fixed_config_on_held_out_matrices():
+    ds = tuner.Dataset.load(GOLDEN)
+    n = len(ds.times)
+    held = np.arange(n) % 5 == 4           # every fifth matrix is held out
+    train, test = ds.subset(~held), ds.subset(held)
+    model = tuner.CostModel(seed=0)
+    hist = model.fit(train, epochs=300, seed=0)
+    assert hist[-1] < hist[0]
+    fixed = tuner.best_fixed_config(train)
+    res = tuner.evaluate(model, test, fixed)
+    print(res)
+    # the network's choice against the best single config (the method
+    # without it) and against the searched optimum (10 %)
+    assert res["mlp_mean_regret"] < res["fixed_mean_regret"]
+    assert res["mlp_mean_regret"] <= 0.10
+    assert res["mlp_within_10pct"] > res["fixed_within_10pct"]
+    assert res["mlp_top2_mean_regret"] <= res["mlp_mean_regret"] + 1e-12

@@ -110,3 +110,25 @@ def test_block_mpk_oracle_is_per_column_chain(mats):
     blk32 = orc.mpk_block(A, X32, 3)
     assert blk32.dtype == np.float32
     np.testing.assert_allclose(blk32[3], blk[3], rtol=0, atol=1e-4 * np.abs(blk[3]).max())
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    """The tuner network's CPU gradient (oracle/mlp_ref.py) against central
+    differences in float64: pins the oracle the GPU kernels are checked
+    against."""
+    from oracle import mlp_ref
+    dims = (5, 7, 2, 2)
+    rng = np.random.Generator(np.random.PCG64(4))
+    theta = rng.normal(0, 0.5, mlp_ref.num_params(*dims))
+    X = rng.normal(size=(6, 5))
+    T = rng.normal(size=(6, 2))
+    loss, g = mlp_ref.loss_grad(theta, X, T, dims)
+    h = 1e-6
+    fd = np.zeros_like(theta)
+    for i in range(theta.size):
+        tp, tm = theta.copy(), theta.copy()
+        tp[i] += h
+        tm[i] -= h
+        fd[i] = (mlp_ref.loss_grad(tp, X, T, dims)[0] - mlp_ref.loss_grad(tm, X, T, dims)[0]) / (2 * h)
+    assert np.max(np.abs(fd - g)) <= 1e-6 * max(1.0, np.max(np.abs(g)))
+    assert loss > 0
