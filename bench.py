@@ -161,11 +161,56 @@ def run_reference(args, rank, world):
 
 
 def run_profile_case(args):
-    """A short, fixed sequence of launches for ncu: --steps MPK calls, then
-    --steps rounds of the p plain SpMVs on the same SELL-32 layout."""
+    """Short, fixed sequences of launches for ncu.
+    mpk: --steps MPK calls, then --steps rounds of the p plain SpMVs on the
+    same SELL-32 layout (27-point stencil, --grid^3).
+    batch: the batched block MPK of --batch-count matrices, --steps graph
+    replays, then --steps rounds of the plain per-matrix launches.
+    symmgs: --steps forward+backward GS sweeps (FP32 values) on the
+    --symmgs-rows power-law system of the SymmGS measurement."""
     import torch
     from race_gb300 import interface as ri
     from race_gb300 import matgen
+    if args.profile == "batch":
+        p, nrhs = 4, 16
+        dt = torch.float32 if args.values == "f32" else torch.float64
+        batch, fns = ri.Batch(), []
+        for i, A in enumerate(matgen.aniso2d_batch(args.batch_count, seed=0)):
+            rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+            assert rc.RACEColor(p, args.batch_cache_mb * 1e6) == 0
+            P = A.permuted(rc.getPerm(), rc.getInvPerm())
+            dm = ri.DeviceCsr.from_csr(P, "cuda", dt)
+            x = torch.zeros((p + 1) * P.n * nrhs, dtype=dt, device="cuda")
+            x[: P.n * nrhs] = torch.tensor(matgen.uniform_block(P.n, nrhs, seed=100 + i).reshape(-1), dtype=dt,
+                                           device="cuda")
+            fid = rc.registerMpkBlock(ri.Operands(dm, x), p, nrhs)
+            assert rc.executeFunction(fid) == 0
+            batch.add(rc, fid)
+            fns.append((rc, fid, dm, x))
+        for _ in range(args.steps):
+            batch.graphLaunch()
+        assert batch.getStatus() == 0
+        for _ in range(args.steps):
+            for rc, fid, _, _ in fns:
+                for k in range(p):
+                    rc.spmvPowerLayout(fid, k)
+        torch.cuda.synchronize()
+        print(f"profile case done: batch of {args.batch_count}, values {args.values}")
+        return
+    if args.profile == "symmgs":
+        A = matgen.powerlaw_chung_lu(args.symmgs_rows, seed=0)
+        rc = ri.Interface(A.n, 4096, ri.TWO, A.row_ptr, A.col, symm_hint=True)
+        assert rc.RACEColor() == 0
+        P = A.permuted(rc.getPerm(), rc.getInvPerm())
+        m32 = ri.DeviceCsr.from_csr(P, "cuda", torch.float32)
+        d = torch.zeros(A.n, dtype=torch.float32, device="cuda")
+        r = torch.ones(A.n, dtype=torch.float32, device="cuda")
+        fid = rc.registerFunction(ri.GS, ri.Operands(m32, d, r))
+        for _ in range(args.steps):
+            assert rc.executeFunction(fid) == 0
+            assert rc.executeFunction(fid, True) == 0
+        print(f"profile case done: symmetric GS on power-law n={A.n}")
+        return
     dt = torch.float32 if args.values == "f32" else torch.float64
     A = matgen.stencil3d_27pt(args.grid)
     rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
@@ -195,9 +240,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the CPU baseline sample")
     ap.add_argument("--symmgs-rows", type=int, default=1 << 20,
                     help="rows of the power-law SymmGS system (0 skips it; the full configuration is 4194304)")
-    ap.add_argument("--profile", choices=["mpk"], default=None,
-                    help="profiling case: register the MPK on a --grid^3 27-point stencil, run it --steps times, "
-                         "then the same powers as --steps rounds of p plain SELL SpMVs; prints no JSON")
+    ap.add_argument("--profile", choices=["mpk", "batch", "symmgs"], default=None,
+                    help="profiling case (mpk, batch or symmgs; see run_profile_case); prints no JSON")
     ap.add_argument("--batch-count", type=int, default=64,
                     help="matrices of the batched block-MPK measurement (0 skips it)")
     ap.add_argument("--batch-cache-mb", type=float, default=256.0,
@@ -326,6 +370,7 @@ def main():
     del dm32, x32
     symmgs = bench_symmgs(args, ri, matgen, torch) if args.symmgs_rows > 0 else None
     batched = bench_batch(args, ri, matgen, torch) if args.batch_count > 0 else None
+    tuned = bench_tuner(torch)
     if rank == 0:
         line = {
             "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
@@ -350,6 +395,7 @@ def main():
                           "hbm_frac": eff_bytes / (ms_plain * 1e-3) / 1e9 / peak},
             "symmgs_ir": symmgs,
             "batched_mpk": batched,
+            "mlp_tuner": tuned,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -497,6 +543,30 @@ def bench_batch(args, ri, matgen, torch):
     out.update(results)
     out["mixed_f32_speedup_vs_f64_plain"] = results["f64"]["ms_plain"] / results["f32"]["ms_graph"]
     return out
+
+
+def bench_tuner(torch):
+    """The MLP cost model (32 features -> 3 x 128 ReLU -> log time), trained
+    by the engine's CUDA kernels on the committed search timings (300
+    matrices, 13 configs of power per block x cache budget for A^8 x) and
+    evaluated on the held-out fifth against the searched optimum and against
+    the best single config."""
+    from race_gb300 import tuner
+    path = ROOT / "tests" / "golden" / "tuner_search.npz"
+    if not path.exists():
+        return None
+    ds = tuner.Dataset.load(path)
+    held = np.arange(len(ds.times)) % 5 == 4
+    train, test = ds.subset(~held), ds.subset(held)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    model = tuner.CostModel(seed=0)
+    hist = model.fit(train, seed=0)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    res = tuner.evaluate(model, test, tuner.best_fixed_config(train))
+    res.update({"train_matrices": len(train.times), "train_seconds": train_s, "final_train_loss": hist[-1]})
+    return res
 
 
 def cpu_baseline(A, P, x0, budget_s: float):
