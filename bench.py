@@ -242,6 +242,7 @@ def main():
                     help="rows of the power-law SymmGS system (0 skips it; the full configuration is 4194304)")
     ap.add_argument("--profile", choices=["mpk", "batch", "symmgs"], default=None,
                     help="profiling case (mpk, batch or symmgs; see run_profile_case); prints no JSON")
+    ap.add_argument("--no-tuner", action="store_true", help="skip the MLP tuner training/evaluation")
     ap.add_argument("--batch-count", type=int, default=64,
                     help="matrices of the batched block-MPK measurement (0 skips it)")
     ap.add_argument("--batch-cache-mb", type=float, default=256.0,
@@ -370,7 +371,7 @@ def main():
     del dm32, x32
     symmgs = bench_symmgs(args, ri, matgen, torch) if args.symmgs_rows > 0 else None
     batched = bench_batch(args, ri, matgen, torch) if args.batch_count > 0 else None
-    tuned = bench_tuner(torch)
+    tuned = bench_tuner(torch) if not args.no_tuner else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,

@@ -138,8 +138,9 @@ __device__ __forceinline__ AT hubSum(const SellView &m, int h, const AT *x) {
 
 // Chunk c at power k -> k+1: the lane's row (unless it is a hub row), then
 // the chunk's hub rows one at a time with the whole warp. Called by all 32
-// lanes of a warp.
-template <typename VT>
+// lanes of a warp. HUBS = false compiles the plain SELL row only (plans
+// without hub rows keep the register count, hence the occupancy, of that).
+template <typename VT, bool HUBS>
 __device__ __forceinline__ void chunkRow(const SellView &m, int c, int k, int n, double *x, float *xf) {
     const int lane = threadIdx.x & 31;
     const int r = m.chunkRow[c] + lane;
@@ -156,6 +157,7 @@ __device__ __forceinline__ void chunkRow(const SellView &m, int c, int k, int n,
             }
         }
     }
+    if constexpr (HUBS)
     for (int h = m.hubChunkStart[c]; h < m.hubChunkStart[c + 1]; ++h) {
         const int hr = m.hubRow[h];
         if constexpr (sizeof(VT) == 8) {
@@ -188,7 +190,7 @@ struct MpkArgs {
 // Persistent warps: one (power, chunk) item per ticket. Taking several
 // items at once or requesting the next ticket early measured slower: an
 // item held but not started delays every item that depends on it.
-template <typename VT>
+template <typename VT, bool HUBS>
 __global__ void __launch_bounds__(kWarpThreads) kMpk(MpkArgs a) {
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(kWarpThreads) kMpk(MpkArgs a) {
                 __nanosleep(32);
             }
         }
-        chunkRow<VT>(a.m, c, k, a.n, a.x, a.xf);
+        chunkRow<VT, HUBS>(a.m, c, k, a.n, a.x, a.xf);
         // __syncwarp orders the lanes' stores before lane 0's release store
         __syncwarp();
         if (lane == 0)
@@ -228,12 +230,12 @@ __global__ void __launch_bounds__(kWarpThreads) kMpk(MpkArgs a) {
 }
 
 // Plain y = A x on the SELL layout, no schedule: one warp per chunk.
-template <typename VT>
+template <typename VT, bool HUBS>
 __global__ void __launch_bounds__(kWarpThreads) kSpmvSell(SellView m, int numChunks, int n, int k, double *x,
                                                           float *xf) {
     const int nw = gridDim.x * (blockDim.x >> 5);
     for (int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < numChunks; c += nw)
-        chunkRow<VT>(m, c, k, n, x, xf);
+        chunkRow<VT, HUBS>(m, c, k, n, x, xf);
 }
 
 // x0 -> FP32 copy (rounding to nearest) for the reduced-precision path.
@@ -521,9 +523,26 @@ SellView viewOf(const MpkPlan &p) {
 }
 
 template <typename VT>
-void launchMpk(const MpkArgs &a, cudaStream_t s) {
-    static int blocks = residentBlocks(kMpk<VT>, kWarpThreads);
-    kMpk<VT><<<blocks, kWarpThreads, 0, s>>>(a);
+void launchMpk(const MpkArgs &a, bool hubs, cudaStream_t s) {
+    if (hubs) {
+        static int blocks = residentBlocks(kMpk<VT, true>, kWarpThreads);
+        kMpk<VT, true><<<blocks, kWarpThreads, 0, s>>>(a);
+    } else {
+        static int blocks = residentBlocks(kMpk<VT, false>, kWarpThreads);
+        kMpk<VT, false><<<blocks, kWarpThreads, 0, s>>>(a);
+    }
+}
+
+template <typename VT>
+void launchSpmvSell(const SellView &v, int numChunks, int n, int k, double *x, float *xf, bool hubs,
+                    cudaStream_t s) {
+    if (hubs) {
+        static int blocks = residentBlocks(kSpmvSell<VT, true>, kWarpThreads);
+        kSpmvSell<VT, true><<<blocks, kWarpThreads, 0, s>>>(v, numChunks, n, k, x, xf);
+    } else {
+        static int blocks = residentBlocks(kSpmvSell<VT, false>, kWarpThreads);
+        kSpmvSell<VT, false><<<blocks, kWarpThreads, 0, s>>>(v, numChunks, n, k, x, xf);
+    }
 }
 }  // namespace
 
@@ -537,9 +556,9 @@ void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
     MpkArgs a{viewOf(plan), (double *)ops.x, plan.xf.p, ops.n, plan.depRange.p, plan.itemChunk.p, plan.itemPow.p,
               plan.numItems, plan.numChunks, plan.done.p, plan.ticket.p, plan.status.p};
     switch (plan.valType) {
-    case RACE_VAL_F64: launchMpk<double>(a, s); break;
-    case RACE_VAL_F32: launchMpk<float>(a, s); break;
-    case RACE_VAL_BF16: launchMpk<__nv_bfloat16>(a, s); break;
+    case RACE_VAL_F64: launchMpk<double>(a, plan.numHubs > 0, s); break;
+    case RACE_VAL_F32: launchMpk<float>(a, plan.numHubs > 0, s); break;
+    case RACE_VAL_BF16: launchMpk<__nv_bfloat16>(a, plan.numHubs > 0, s); break;
     default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
     }
     RACE_CUDA(cudaGetLastError());
@@ -552,21 +571,11 @@ void runSpmvSell(Engine &e, MpkPlan &plan, double *x, int n, int k) {
     if (plan.valType != RACE_VAL_F64 && k == 0) kToFloat<<<ceilDiv(n, 256), 256, 0, s>>>(x, plan.xf.p, n);
     SellView v = viewOf(plan);
     switch (plan.valType) {
-    case RACE_VAL_F64: {
-        static int blocks = residentBlocks(kSpmvSell<double>, kWarpThreads);
-        kSpmvSell<double><<<blocks, kWarpThreads, 0, s>>>(v, plan.numChunks, n, k, x, plan.xf.p);
+    case RACE_VAL_F64: launchSpmvSell<double>(v, plan.numChunks, n, k, x, plan.xf.p, plan.numHubs > 0, s); break;
+    case RACE_VAL_F32: launchSpmvSell<float>(v, plan.numChunks, n, k, x, plan.xf.p, plan.numHubs > 0, s); break;
+    case RACE_VAL_BF16:
+        launchSpmvSell<__nv_bfloat16>(v, plan.numChunks, n, k, x, plan.xf.p, plan.numHubs > 0, s);
         break;
-    }
-    case RACE_VAL_F32: {
-        static int blocks = residentBlocks(kSpmvSell<float>, kWarpThreads);
-        kSpmvSell<float><<<blocks, kWarpThreads, 0, s>>>(v, plan.numChunks, n, k, x, plan.xf.p);
-        break;
-    }
-    case RACE_VAL_BF16: {
-        static int blocks = residentBlocks(kSpmvSell<__nv_bfloat16>, kWarpThreads);
-        kSpmvSell<__nv_bfloat16><<<blocks, kWarpThreads, 0, s>>>(v, plan.numChunks, n, k, x, plan.xf.p);
-        break;
-    }
     default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
     }
     RACE_CUDA(cudaGetLastError());
