@@ -107,7 +107,10 @@ int race_set_stream(race_engine *e, void *cuda_stream);
 /* Interface::RACEColor() (interface.h:128, interface.cpp:260-301) */
 int race_color(race_engine *e);
 /* Interface::RACEColor(highestPower, cacheSize, safetyFactor, mtxType,
- * highestSubPower) (interface.h:127, interface.cpp:205-257); cacheSize in bytes. */
+ * highestSubPower) (interface.h:127, interface.cpp:205-257); cacheSize in bytes.
+ * A repeated call on the same engine (another power or cache budget, e.g. a
+ * parameter search) regroups the BFS levels of the first call: the
+ * permutation stays that of the first call. */
 int race_power_prepare(race_engine *e, int highestPower, double cacheSize, double safetyFactor, const char *mtxType,
                        int highestSubPower);
 

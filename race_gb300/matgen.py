@@ -250,3 +250,47 @@ def uniform_block(n: int, nrhs: int, seed: int = 0) -> np.ndarray:
     """n x nrhs right-hand sides, U[-1,1] (PCG64 seeded), row-major."""
     rng = np.random.Generator(np.random.PCG64(seed))
     return rng.uniform(-1.0, 1.0, size=(n, nrhs))
+
+
+def islands(seed: int = 0) -> Csr:
+    """Disconnected pieces with isolated rows: a 6^3 7-point Laplacian (216
+    rows), a 12 x 9 anisotropic 5-point stencil (108 rows) and 6 rows holding
+    only their diagonal, rows scrambled by a seeded permutation (330 rows)."""
+    parts = [laplace3d_7pt(6), aniso2d(12, 9, 5, 4.0)]
+    rows, cols, vals, diag, off = [], [], [], [], 0
+    for P in parts:
+        r = np.repeat(np.arange(P.n), np.diff(P.row_ptr))
+        keep = r != P.col
+        rows.append(r[keep] + off)
+        cols.append(P.col[keep].astype(np.int64) + off)
+        vals.append(P.val[keep])
+        d = np.zeros(P.n)
+        dm = ~keep
+        d[r[dm]] = P.val[dm]
+        diag.append(d)
+        off += P.n
+    diag.append(np.full(6, 2.0))
+    n = off + 6
+    rows, cols, vals, diag = np.concatenate(rows), np.concatenate(cols), np.concatenate(vals), np.concatenate(diag)
+    perm = np.random.Generator(np.random.PCG64(seed)).permutation(n)  # new index of old row i
+    return _assemble(n, perm[rows], perm[cols].astype(np.int32), vals, diag[np.argsort(perm)], "islands_330")
+
+
+def chain_with_empty_rows(n: int = 300, empty=(0, 150, 299)) -> Csr:
+    """1D Laplacian chain whose rows in `empty` hold no entry at all (not
+    even a diagonal): edge cases for traversal and the matrix power."""
+    r = np.arange(n - 1)
+    rows = np.concatenate([r, r + 1])
+    cols = np.concatenate([r + 1, r])
+    e = np.asarray(empty)
+    keep = ~(np.isin(rows, e) | np.isin(cols, e))
+    rows, cols = rows[keep], cols[keep].astype(np.int32)
+    vals = np.full(rows.size, -1.0)
+    B = _assemble(n, rows, cols, vals, np.full(n, 2.0), f"chain{n}_empty")
+    # drop the diagonal of the empty rows
+    rl = np.diff(B.row_ptr)
+    r_of = np.repeat(np.arange(n), rl)
+    keep = ~np.isin(r_of, e)
+    rp = np.zeros(n + 1, np.int32)
+    np.cumsum(np.bincount(r_of[keep], minlength=n), out=rp[1:])
+    return Csr(n, rp, B.col[keep].astype(np.int32), B.val[keep].copy(), B.name)

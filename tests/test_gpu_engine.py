@@ -50,7 +50,8 @@ def _upload(P, dtype=torch.float64):
 
 
 SWEEP_CASES = [("lap7_16", 2, 16), ("lap7_32", 2, 1024), ("lap7_32", 1, 256), ("aniso9_100x80", 1, 16),
-               ("plaw_3k", 1, 32), ("band_5k", 2, 32), ("st27_16", 2, 128), ("aniso5_120x90", 2, 48)]
+               ("plaw_3k", 1, 32), ("band_5k", 2, 32), ("st27_16", 2, 128), ("aniso5_120x90", 2, 48),
+               ("islands_330", 2, 16), ("islands_330", 1, 8), ("tiny_1", 1, 4)]
 
 
 @pytest.mark.parametrize("m,d,t", SWEEP_CASES)
@@ -323,3 +324,36 @@ def test_unsymmetric_pattern_is_symmetrised(mats):
     S2 = matgen._assemble(S.n, rr[off], cc[off].astype(np.int32), np.ones(off.sum()), np.ones(S.n), "s2")
     perm, _, _, _, _ = orc.traverse(S2, 3, 0, S2.n)
     np.testing.assert_array_equal(rc.getPerm(), perm)
+
+
+def test_empty_rows_spmv_and_mpk():
+    """Rows without any entry (not even a diagonal) are undefined input for
+    the reference (its graph build reads each row's first entry,
+    src/graph_SoA.cpp:121-130), so there is no golden; the engine must still
+    color and permute such a matrix and give empty rows a zero result in
+    SpMV and every power of the MPK."""
+    A = matgen.chain_with_empty_rows(300, (0, 150, 299))
+    for d, t in ((1, 8), (2, 16)):
+        rc = ri.Interface(A.n, t, d, A.row_ptr, A.col, symm_hint=True)
+        assert rc.RACEColor() == 0
+        perm, inv = rc.getPerm(), rc.getInvPerm()
+        assert np.array_equal(np.sort(perm), np.arange(A.n))
+        P = A.permuted(perm, inv)
+        x0 = matgen.uniform_vector(A.n, 0)
+        x = torch.tensor(x0, device="cuda")
+        b = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+        fid = rc.registerFunction(ri.SPMV, ri.Operands(_upload(P), x, b))
+        assert rc.executeFunction(fid) == 0
+        ref = np.zeros(A.n)
+        orc.run_kernel(orc.K_SPMV, 0, A.n, P, x0.copy(), ref)
+        np.testing.assert_array_equal(b.cpu().numpy(), ref)
+    p = 4
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, 1e4) == 0
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    x0 = matgen.uniform_vector(A.n, 0)
+    x = torch.zeros((p + 1) * A.n, dtype=torch.float64, device="cuda")
+    x[: A.n] = torch.tensor(x0, device="cuda")
+    fid = rc.registerFunction(ri.MPK, ri.Operands(_upload(P), x), power=p)
+    assert rc.executeFunction(fid) == 0
+    np.testing.assert_array_equal(x.cpu().numpy().reshape(p + 1, A.n), orc.mpk_plain(P, x0, p))
