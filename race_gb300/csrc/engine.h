@@ -89,6 +89,14 @@ struct BlockPlan {
 struct DevWaves {
     int numWaves = 0, maxRows = 0;
     DevBuf<int> wavePtr, rows;
+    // Rows above the huge-row length run in waves of their own, summed by
+    // all warps of the grid: per wave a flag, per plan position the first of
+    // its row's segments (positions+1), per segment its position and entry
+    // range, and the segments' partial sums (3 per segment).
+    int numSegs = 0;
+    DevBuf<unsigned char> waveHuge;
+    DevBuf<int> segFirst, segPos, segBeg, segEnd;
+    DevBuf<double> segScratch;
 };
 
 struct FuncEntry {

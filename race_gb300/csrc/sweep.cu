@@ -9,10 +9,13 @@
 // * Wave mode (default). The execution order is compiled into conflict-free
 //   waves (waves.cpp). One cooperative launch walks the waves with a bounded
 //   grid barrier between them; inside a wave every row is independent and
-//   one thread runs it with the kernel body's own operation order
-//   (examples/src/helpers/kernels.cpp), so FP64 results are identical bit for
-//   bit to RACE's sequential walk, and rows that RACE keeps in one long leaf
-//   still run in parallel when they do not conflict.
+//   runs with the kernel body's own operation order
+//   (examples/src/helpers/kernels.cpp) — one thread per row up to 32
+//   entries, one warp folding gathered entries in order up to 512 — so FP64
+//   results are identical bit for bit to RACE's sequential walk, and rows
+//   that RACE keeps in one long leaf still run in parallel when they do not
+//   conflict. Rows above 512 entries get waves of their own, shared by all
+//   warps of the grid (reassociated, within 1e-12).
 // * Leaf mode (RACE_GPU_SWEEP_MODE=leaf). The flattened phases run with a
 //   grid barrier between phases; one warp owns one leaf and walks its rows in
 //   order, lanes splitting a row's non-zeros with warp-shuffle reductions.
@@ -20,6 +23,8 @@
 //
 // Neither mode needs atomics on the transpose scatter: the coloring (leaf
 // mode) or the wave plan (wave mode) gives every written entry one writer.
+#include <cstdlib>
+
 #include <cuda_bf16.h>
 
 #include "engine.h"
@@ -29,6 +34,7 @@ namespace {
 
 constexpr int kSweepThreads = 256;
 constexpr int kWarps = kSweepThreads / 32;
+constexpr int kWaveBlocksPerSm = 1;
 
 __device__ __forceinline__ unsigned ldAcquireU(const unsigned *p) {
     unsigned v;
@@ -97,6 +103,11 @@ struct SweepArgs {
     int num;          // waves or phases
     unsigned *bar;
     int *status;
+    // wave mode, rows above kHugeRow (see DevWaves)
+    const unsigned char *waveHuge;
+    const int *segFirst, *segPos, *segBeg, *segEnd;
+    double *segScratch;
+    int numSegs;
 };
 
 // One row with the kernel body's own operation order (thread per row).
@@ -158,14 +169,122 @@ __device__ __forceinline__ void rowSerial(const SweepArgs &a, int r) {
     }
 }
 
-// Rows longer than this are run by a whole warp with a shuffle reduction
-// instead of one thread (hub rows of power-law graphs would otherwise turn
-// one thread's sequential fma chain into the wave's critical path); their
-// sums are reassociated, all other rows keep the sequential order.
-constexpr int kLongRow = 512;
+// Wave mode keeps the sequential order (bit-exact) for rows of up to
+// kHugeRow entries: up to kMidRow one thread, above that one warp
+// (rowWarpExact). Longer rows are reassociated (hugeWave).
+// Rows longer than this (and up to kHugeRow) are run by a whole warp that
+// keeps the sequential order (rowWarpExact): one thread walking a few hundred
+// entries would pay a dependent gather per few entries and make its row the
+// wave's critical path.
+constexpr int kMidRow = 32;
 
 template <typename VT, typename XT>
 __device__ __forceinline__ void rowWarp(const SweepArgs &a, int row, int lane);
+
+// Rows above this many entries (one reaches a quarter of a million in a
+// power-law graph) get waves of their own in which all warps of the grid
+// share them: segments of kHugeSeg entries are summed by one warp each, a
+// grid barrier, then one warp per row combines its segments in order and
+// applies the kernel's row update (Kaczmarz: a second barrier, then the
+// scatter with the row's scale). Sums are reassociated, deterministically.
+constexpr int kHugeRow = 512;
+constexpr int kHugeSeg = 256;
+
+template <typename VT, typename XT>
+__device__ bool hugeWave(const SweepArgs &a, int r0, int r1, int gw, int nw, int lane);
+
+// Entries [jb, e) of a row, folded in order by every lane of a warp: each
+// round gathers up to kFoldBlocks x 32 entries at once (all loads in
+// flight), then applies f(value, x[col]) to them in the row's order through
+// broadcasts, so every lane runs the same sequential chain.
+constexpr int kFoldBlocks = 8;
+
+template <typename VT, typename XT, typename F>
+__device__ __forceinline__ void foldRow(const SweepArgs &a, int jb, int e, int lane, F &&f) {
+    constexpr unsigned kFull = 0xffffffffu;
+    const VT *val = (const VT *)a.val;
+    const XT *x = (const XT *)a.x;
+    for (int jr = jb; jr < e; jr += 32 * kFoldBlocks) {
+        XT v[kFoldBlocks], xv[kFoldBlocks];
+#pragma unroll
+        for (int k = 0; k < kFoldBlocks; ++k) {
+            const int j = jr + 32 * k + lane;
+            const bool ok = j < e;
+            v[k] = ok ? ld<VT, XT>(val, j) : XT(0);
+            xv[k] = ok ? x[a.col[j]] : XT(0);
+        }
+#pragma unroll
+        for (int k = 0; k < kFoldBlocks; ++k) {
+            const int m = min(32, e - (jr + 32 * k));
+            for (int q = 0; q < m; ++q) f(__shfl_sync(kFull, v[k], q), __shfl_sync(kFull, xv[k], q));
+        }
+    }
+}
+
+// A row with the kernel body's own operation order, run by a warp (rows of
+// kMidRow+1..kHugeRow entries): sums through foldRow, identical bit for bit
+// to rowSerial; scatters (one distinct column per entry) run lane-parallel
+// with the same per-entry arithmetic.
+template <typename VT, typename XT>
+__device__ __forceinline__ void rowWarpExact(const SweepArgs &a, int r, int lane) {
+    const VT *val = (const VT *)a.val;
+    XT *x = (XT *)a.x;
+    XT *b = (XT *)a.b;
+    const int s = a.rowPtr[r], e = a.rowPtr[r + 1];
+    switch (a.kernel) {
+    case RACE_K_SPMV: {
+        XT t = XT(0);
+        foldRow<VT, XT>(a, s, e, lane, [&](XT v, XT xv) { t = mac(v, xv, t); });
+        if (lane == 0) b[r] = t;
+        break;
+    }
+    case RACE_K_SPMTV: {
+        const XT xr = x[r];
+        for (int j = s + lane; j < e; j += 32) {
+            const int c = a.col[j];
+            b[c] = mac(ld<VT, XT>(val, j), xr, b[c]);
+        }
+        break;
+    }
+    case RACE_K_SYMMSPMV: {
+        // the diagonal update and the final b[r] += t touch only b[r]; the
+        // scatter only columns above r, so lane 0 does both at the end
+        const XT xr = x[r];
+        XT t = XT(0);
+        foldRow<VT, XT>(a, s + 1, e, lane, [&](XT v, XT xv) { t = mac(v, xv, t); });
+        for (int j = s + 1 + lane; j < e; j += 32) {
+            const int c = a.col[j];
+            b[c] = mac(ld<VT, XT>(val, j), xr, b[c]);
+        }
+        if (lane == 0) {
+            b[r] = mac(ld<VT, XT>(val, s), xr, b[r]);
+            b[r] += t;
+        }
+        break;
+    }
+    case RACE_K_GS: {
+        XT t = b[r];
+        foldRow<VT, XT>(a, s + 1, e, lane, [&](XT v, XT xv) { t = mac(-v, xv, t); });
+        if (lane == 0) x[r] = t / ld<VT, XT>(val, s);
+        break;
+    }
+    case RACE_K_KACZ: {
+        XT nrm = XT(0), sc = -b[r];
+        foldRow<VT, XT>(a, s, e, lane, [&](XT v, XT xv) {
+            sc = mac(v, xv, sc);
+            nrm = mac(v, v, nrm);
+        });
+        sc /= nrm;
+        __syncwarp();  // every lane's reads of x precede the scatter
+        for (int j = s + lane; j < e; j += 32) {
+            const int c = a.col[j];
+            x[c] = mac(-sc, ld<VT, XT>(val, j), x[c]);
+        }
+        break;
+    }
+    default: break;
+    }
+}
 
 template <typename VT, typename XT>
 __global__ void __launch_bounds__(kSweepThreads) kWaveSweep(SweepArgs a) {
@@ -175,16 +294,25 @@ __global__ void __launch_bounds__(kSweepThreads) kWaveSweep(SweepArgs a) {
     const int gw = tid >> 5, nw = nt >> 5;
     for (int w = 0; w < a.num; ++w) {
         const int r0 = a.ptr[w], r1 = a.ptr[w + 1];
+        if (a.waveHuge && a.waveHuge[w]) {
+            if (!hugeWave<VT, XT>(a, r0, r1, gw, nw, lane)) return;
+            if (w + 1 < a.num && !gridBarrier(a.bar, a.status)) return;
+            continue;
+        }
         for (int i = r0 + tid; i < r1; i += nt) {
             const int r = a.rows[i];
-            if (a.rowPtr[r + 1] - a.rowPtr[r] <= kLongRow) rowSerial<VT, XT>(a, r);
+            if (a.rowPtr[r + 1] - a.rowPtr[r] <= kMidRow) rowSerial<VT, XT>(a, r);
         }
-        // long rows of this wave: one warp each, distributed over all warps
-        // of the grid (rows of a wave are independent, so the two passes may
+        // longer rows of this wave: one warp each, distributed over all warps
+        // of the grid (rows of a wave are independent, so the passes may
         // interleave)
         for (int i = r0 + gw; i < r1; i += nw) {
             const int r = a.rows[i];
-            if (a.rowPtr[r + 1] - a.rowPtr[r] > kLongRow) rowWarp<VT, XT>(a, r, lane);
+            const int len = a.rowPtr[r + 1] - a.rowPtr[r];
+            if (len > kHugeRow)
+                rowWarp<VT, XT>(a, r, lane);  // not reached: the plan gives such rows huge waves
+            else if (len > kMidRow)
+                rowWarpExact<VT, XT>(a, r, lane);
         }
         if (w + 1 < a.num && !gridBarrier(a.bar, a.status)) return;
     }
@@ -197,6 +325,103 @@ __device__ __forceinline__ XT warpSum(XT v) {
 #pragma unroll
     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
+}
+
+template <typename VT, typename XT>
+__device__ bool hugeWave(const SweepArgs &a, int r0, int r1, int gw, int nw, int lane) {
+    const VT *val = (const VT *)a.val;
+    XT *x = (XT *)a.x;
+    XT *b = (XT *)a.b;
+    double *dot = a.segScratch, *nrm = a.segScratch + a.numSegs, *scl = a.segScratch + 2 * a.numSegs;
+    const int g0 = a.segFirst[r0], g1 = a.segFirst[r1];
+    // 1. segment sums, and the scatters that need no row result
+    for (int g = g0 + gw; g < g1; g += nw) {
+        const int r = a.rows[a.segPos[g]];
+        const int s = a.rowPtr[r], jb = a.segBeg[g], je = a.segEnd[g];
+        XT t = XT(0), q = XT(0);
+        switch (a.kernel) {
+        case RACE_K_SPMV:
+        case RACE_K_GS:
+        case RACE_K_KACZ: {
+            // a segment holds at most 8 entries per lane: gather all, then sum
+            constexpr int kPer = kHugeSeg / 32;
+            XT v[kPer], xv[kPer];
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                const int j = jb + lane + 32 * k;
+                const bool ok = j < je && !(a.kernel == RACE_K_GS && j == s);
+                v[k] = ok ? ld<VT, XT>(val, j) : XT(0);
+                xv[k] = ok ? x[a.col[j]] : XT(0);
+            }
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                t = mac(v[k], xv[k], t);
+                q = mac(v[k], v[k], q);
+            }
+            break;
+        }
+        case RACE_K_SYMMSPMV: {
+            const XT xr = x[r];
+            for (int j = jb + lane; j < je; j += 32)
+                if (j != s) {
+                    const int c = a.col[j];
+                    const XT v = ld<VT, XT>(val, j);
+                    t = mac(v, x[c], t);
+                    b[c] = mac(v, xr, b[c]);
+                }
+            break;
+        }
+        case RACE_K_SPMTV: {
+            const XT xr = x[r];
+            for (int j = jb + lane; j < je; j += 32) {
+                const int c = a.col[j];
+                b[c] = mac(ld<VT, XT>(val, j), xr, b[c]);
+            }
+            break;
+        }
+        default: break;
+        }
+        t = warpSum(t);
+        q = warpSum(q);
+        if (lane == 0) {
+            dot[g] = (double)t;
+            nrm[g] = (double)q;
+        }
+    }
+    if (a.kernel == RACE_K_SPMTV) return true;
+    if (!gridBarrier(a.bar, a.status)) return false;
+    // 2. one warp per row: its segments in order, then the row update
+    for (int i = r0 + gw; i < r1; i += nw) {
+        const int r = a.rows[i];
+        XT S = XT(0), Q = XT(0);
+        for (int g = a.segFirst[i] + lane; g < a.segFirst[i + 1]; g += 32) {
+            S += (XT)dot[g];
+            Q += (XT)nrm[g];
+        }
+        S = warpSum(S);
+        Q = warpSum(Q);
+        if (lane == 0) {
+            const int s = a.rowPtr[r];
+            switch (a.kernel) {
+            case RACE_K_SPMV: b[r] = S; break;
+            case RACE_K_GS: x[r] = (b[r] - S) / ld<VT, XT>(val, s); break;
+            case RACE_K_SYMMSPMV: b[r] = mac(ld<VT, XT>(val, s), x[r], b[r]) + S; break;
+            case RACE_K_KACZ: scl[a.segFirst[i]] = (double)((S - b[r]) / Q); break;
+            default: break;
+            }
+        }
+    }
+    if (a.kernel != RACE_K_KACZ) return true;
+    if (!gridBarrier(a.bar, a.status)) return false;
+    // 3. Kaczmarz scatter with the row's scale
+    for (int g = g0 + gw; g < g1; g += nw) {
+        const XT sc = (XT)scl[a.segFirst[a.segPos[g]]];
+        for (int j = a.segBeg[g] + lane; j < a.segEnd[g]; j += 32) {
+            const int c = a.col[j];
+            x[c] = mac(-sc, ld<VT, XT>(val, j), x[c]);
+        }
+    }
+    return true;
 }
 
 template <typename VT, typename XT>
@@ -281,19 +506,33 @@ __global__ void __launch_bounds__(kSweepThreads) kLeafSweep(SweepArgs a) {
 }
 
 template <typename K>
-int coopBlocks(K kernel, int want) {
+int coopBlocks(K kernel, int want, int capPerSm = 0) {
     int dev = 0, sms = 0, occ = 0;
     RACE_CUDA(cudaGetDevice(&dev));
     RACE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     RACE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kSweepThreads, 0));
-    return std::max(1, std::min(sms * std::max(occ, 1), want));
+    occ = std::max(occ, 1);
+    if (capPerSm > 0) occ = std::min(occ, capPerSm);
+    return std::max(1, std::min(sms * occ, want));
+}
+
+// Blocks per SM of the wave-mode grid. Every wave ends with a grid barrier
+// whose cost grows with the number of blocks, while a wave rarely holds more
+// rows than a few blocks per SM cover (256 threads each, grid-stride loops
+// take the rest). RACE_GPU_SWEEP_BLOCKS_PER_SM overrides it (0: occupancy).
+int waveBlocksPerSm() {
+    static const int v = [] {
+        const char *s = getenv("RACE_GPU_SWEEP_BLOCKS_PER_SM");
+        return s ? atoi(s) : kWaveBlocksPerSm;
+    }();
+    return v;
 }
 
 template <typename VT, typename XT>
 void launch(bool waveMode, SweepArgs &a, int maxWork, cudaStream_t s) {
     void *args[] = {&a};
     if (waveMode) {
-        int blocks = coopBlocks(kWaveSweep<VT, XT>, ceilDiv(maxWork, kSweepThreads));
+        int blocks = coopBlocks(kWaveSweep<VT, XT>, ceilDiv(maxWork, kSweepThreads), waveBlocksPerSm());
         RACE_CUDA(cudaLaunchCooperativeKernel((void *)kWaveSweep<VT, XT>, blocks, kSweepThreads, args, 0, s));
     } else {
         int blocks = coopBlocks(kLeafSweep<VT, XT>, ceilDiv(maxWork, kWarps));
@@ -342,12 +581,56 @@ void buildSweepWaves(Engine &e, FuncEntry &f) {
     RACE_CUDA(cudaStreamSynchronize(e.stream));
     for (int dir = 0; dir < 2; ++dir) {
         WavePlan wp = buildWavePlan(f.kernel, n, rp.data(), cl.data(), e.phases[dir]);
+        // Rows above kHugeRow leave their wave for a wave of their own just
+        // before it (rows of a wave are independent, so any split keeps the
+        // order valid); their segments are listed per plan position.
+        std::vector<int> ptr{0}, rows, segFirst{0}, segPos, segBeg, segEnd;
+        std::vector<unsigned char> huge;
+        std::vector<int> normal;
+        for (int w = 0; w < wp.numWaves(); ++w) {
+            normal.clear();
+            const size_t hugeStart = rows.size();
+            for (int i = wp.wavePtr[w]; i < wp.wavePtr[w + 1]; ++i) {
+                const int r = wp.rows[i];
+                if (rp[r + 1] - rp[r] <= kHugeRow) {
+                    normal.push_back(r);
+                    continue;
+                }
+                const int pos = (int)rows.size();
+                rows.push_back(r);
+                for (int j = rp[r]; j < rp[r + 1]; j += kHugeSeg) {
+                    segPos.push_back(pos);
+                    segBeg.push_back(j);
+                    segEnd.push_back(std::min(rp[r + 1], j + kHugeSeg));
+                }
+                segFirst.push_back((int)segPos.size());
+            }
+            if (rows.size() > hugeStart) {
+                ptr.push_back((int)rows.size());
+                huge.push_back(1);
+            }
+            if (!normal.empty()) {
+                for (int r : normal) {
+                    rows.push_back(r);
+                    segFirst.push_back((int)segPos.size());
+                }
+                ptr.push_back((int)rows.size());
+                huge.push_back(0);
+            }
+        }
         DevWaves &w = f.waves[dir];
-        w.numWaves = wp.numWaves();
+        w.numWaves = (int)huge.size();
         w.maxRows = 0;
-        for (int i = 0; i < w.numWaves; ++i) w.maxRows = std::max(w.maxRows, wp.wavePtr[i + 1] - wp.wavePtr[i]);
-        w.wavePtr.upload(wp.wavePtr.data(), wp.wavePtr.size(), e.stream);
-        w.rows.upload(wp.rows.data(), std::max<size_t>(wp.rows.size(), 1), e.stream);
+        for (int i = 0; i < w.numWaves; ++i) w.maxRows = std::max(w.maxRows, ptr[i + 1] - ptr[i]);
+        w.numSegs = (int)segPos.size();
+        w.wavePtr.upload(ptr.data(), ptr.size(), e.stream);
+        w.rows.upload(rows.empty() ? nullptr : rows.data(), std::max<size_t>(rows.size(), 1), e.stream);
+        w.waveHuge.upload(huge.empty() ? nullptr : huge.data(), std::max<size_t>(huge.size(), 1), e.stream);
+        w.segFirst.upload(segFirst.data(), segFirst.size(), e.stream);
+        w.segPos.upload(segPos.empty() ? nullptr : segPos.data(), std::max<size_t>(segPos.size(), 1), e.stream);
+        w.segBeg.upload(segBeg.empty() ? nullptr : segBeg.data(), std::max<size_t>(segBeg.size(), 1), e.stream);
+        w.segEnd.upload(segEnd.empty() ? nullptr : segEnd.data(), std::max<size_t>(segEnd.size(), 1), e.stream);
+        w.segScratch.alloc(std::max<size_t>(3 * segPos.size(), 1));
     }
     RACE_CUDA(cudaStreamSynchronize(e.stream));
 }
@@ -365,6 +648,13 @@ void runSweep(Engine &e, FuncEntry &f, bool rev) {
         a.ptr = w.wavePtr.p;
         a.rows = w.rows.p;
         a.num = w.numWaves;
+        a.waveHuge = w.numSegs > 0 ? w.waveHuge.p : nullptr;
+        a.segFirst = w.segFirst.p;
+        a.segPos = w.segPos.p;
+        a.segBeg = w.segBeg.p;
+        a.segEnd = w.segEnd.p;
+        a.segScratch = w.segScratch.p;
+        a.numSegs = w.numSegs;
         maxWork = w.maxRows;
     } else {
         DevPhases &d = e.dPhases[dir];

@@ -122,26 +122,63 @@ def test_leaf_mode_sweeps(golden, mats, m, d, t):
 
 
 def test_long_rows_use_warp_path(mats):
-    """A power-law graph has hub rows above 512 entries: the wave executor
-    runs them with a warp reduction; the sweep stays within 1e-12 of the
-    oracle."""
+    """A power-law graph has hub rows above 512 entries (warp reduction) and
+    above 2048 (segments summed by all warps of the grid in waves of their
+    own): every kernel's sweep stays within 1e-12 of the oracle's sequential
+    walk of the engine's phases, and repeated runs are identical."""
     A = matgen.powerlaw_chung_lu(20000, seed=2)
-    assert np.diff(A.row_ptr).max() > 512
+    assert np.diff(A.row_ptr).max() > 2048
     rc = ri.Interface(A.n, 64, ri.TWO, A.row_ptr, A.col, symm_hint=True)
     assert rc.RACEColor() == 0
     rc.setSweepMode(ri.SWEEP_WAVE)
     P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    U = P.upper()
     pp, lo, hi = rc.getPhases(False)
     x0 = matgen.uniform_vector(A.n, 0)
     b0 = matgen.uniform_vector(A.n, 1)
-    xr = x0.copy()
-    for ph in range(len(pp) - 1):
-        for leaf in range(pp[ph], pp[ph + 1]):
-            orc.run_kernel(orc.K_GS, int(lo[leaf]), int(hi[leaf]), P, xr, b0.copy())
-    x = torch.tensor(x0, device="cuda")
-    fid = rc.registerFunction(ri.GS, ri.Operands(_upload(P), x, torch.tensor(b0, device="cuda")))
-    assert rc.executeFunction(fid) == 0
-    assert _rel_err(x.cpu().numpy(), xr) <= 1e-12
+    okern = {ri.GS: orc.K_GS, ri.KACZ: orc.K_KACZ, ri.SPMV: orc.K_SPMV, ri.SYMMSPMV: orc.K_SYMMSPMV,
+             ri.SPMTV: orc.K_SPMTV}
+    for kern, mat in [(ri.GS, P), (ri.KACZ, P), (ri.SPMV, P), (ri.SYMMSPMV, U), (ri.SPMTV, P)]:
+        zero_b = kern in (ri.SPMV, ri.SYMMSPMV, ri.SPMTV)
+        xr, br = x0.copy(), (np.zeros(A.n) if zero_b else b0.copy())
+        for ph in range(len(pp) - 1):
+            for leaf in range(pp[ph], pp[ph + 1]):
+                orc.run_kernel(okern[kern], int(lo[leaf]), int(hi[leaf]), mat, xr, br)
+        outs = []
+        for _ in range(2):
+            x = torch.tensor(x0, device="cuda")
+            b = torch.zeros(A.n, dtype=torch.float64, device="cuda") if zero_b else torch.tensor(b0, device="cuda")
+            fid = rc.registerFunction(kern, ri.Operands(_upload(mat), x, b))
+            assert fid >= 0 and rc.executeFunction(fid) == 0
+            outs.append((b if zero_b else x).cpu().numpy())
+        assert _rel_err(outs[0], br if zero_b else xr) <= 1e-12, kern
+        assert np.array_equal(outs[0], outs[1]), kern
+
+
+def test_symmgs_refinement_power_law():
+    """Refinement on a power-law system (hub rows: the FP64 residual runs
+    them as warp-summed segments): FP32 inner sweeps reach 1e-10, and two
+    solves give identical results (fixed reduction orders)."""
+    sp = pytest.importorskip("scipy.sparse")
+    A = matgen.powerlaw_chung_lu(20000, seed=2)
+    rc = ri.Interface(A.n, 64, ri.TWO, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor() == 0
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    S = sp.csr_matrix((P.val, P.col, P.row_ptr), shape=(A.n, A.n))
+    m64 = _upload(P)
+    bh = S @ np.ones(A.n)
+    b = torch.tensor(bh, device="cuda")
+    d = torch.zeros(A.n, dtype=torch.float32, device="cuda")
+    r = torch.zeros(A.n, dtype=torch.float32, device="cuda")
+    fid = rc.registerFunction(ri.GS, ri.Operands(_upload(P, torch.float32), d, r))
+    xs = []
+    for _ in range(2):
+        x = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+        its, rel = rc.symmGsIr(fid, m64, b, x, tol=1e-10, maxIter=300, sweeps=1)
+        assert rel <= 1e-10, (its, rel)
+        xs.append(x.cpu().numpy())
+    assert np.linalg.norm(bh - S @ xs[0]) <= 1.01e-10 * np.linalg.norm(bh)
+    assert np.array_equal(xs[0], xs[1])
 
 
 @pytest.mark.parametrize("vdtype,tol", [(torch.float32, 1e-5), (torch.bfloat16, 3e-2)])
@@ -357,3 +394,36 @@ def test_empty_rows_spmv_and_mpk():
     fid = rc.registerFunction(ri.MPK, ri.Operands(_upload(P), x), power=p)
     assert rc.executeFunction(fid) == 0
     np.testing.assert_array_equal(x.cpu().numpy().reshape(p + 1, A.n), orc.mpk_plain(P, x0, p))
+
+
+def test_medium_rows_warp_path_is_bit_exact():
+    """Rows of 33..512 entries run as one warp that keeps the sequential
+    order (gathers 32 entries at a time, folds them in order): every kernel's
+    forward sweep stays identical bit for bit to the sequential walk of the
+    engine's phases."""
+    A = matgen.banded_scrambled(4000, 48, seed=5, fill=1.0)
+    lens = np.diff(A.row_ptr)
+    assert lens.max() <= 512 and (lens > 32).mean() > 0.9
+    rc = ri.Interface(A.n, 64, ri.TWO, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor() == 0
+    rc.setSweepMode(ri.SWEEP_WAVE)
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    U = P.upper()
+    pp, lo, hi = rc.getPhases(False)
+    x0 = matgen.uniform_vector(A.n, 0)
+    b0 = matgen.uniform_vector(A.n, 1)
+    for kern, mat in [(ri.GS, P), (ri.KACZ, P), (ri.SPMV, P), (ri.SYMMSPMV, U), (ri.SPMTV, P)]:
+        zero_b = kern in (ri.SPMV, ri.SYMMSPMV, ri.SPMTV)
+        xr, br = x0.copy(), (np.zeros(A.n) if zero_b else b0.copy())
+        okern = {ri.GS: orc.K_GS, ri.KACZ: orc.K_KACZ, ri.SPMV: orc.K_SPMV, ri.SYMMSPMV: orc.K_SYMMSPMV,
+                 ri.SPMTV: orc.K_SPMTV}[kern]
+        for ph in range(len(pp) - 1):
+            for leaf in range(pp[ph], pp[ph + 1]):
+                orc.run_kernel(okern, int(lo[leaf]), int(hi[leaf]), mat, xr, br)
+        x = torch.tensor(x0, device="cuda")
+        b = torch.zeros(A.n, dtype=torch.float64, device="cuda") if zero_b else torch.tensor(b0, device="cuda")
+        fid = rc.registerFunction(kern, ri.Operands(_upload(mat), x, b))
+        assert fid >= 0 and rc.getSweepInfo(fid)["wave_mode"]
+        assert rc.executeFunction(fid) == 0
+        out = (b if zero_b else x).cpu().numpy()
+        assert np.array_equal(out, br if zero_b else xr), (kern, _rel_err(out, br if zero_b else xr))
