@@ -603,26 +603,30 @@ def bench_batch(args, ri, matgen, torch):
 
 def bench_tuner(torch):
     """The MLP cost model (32 features -> 3 x 128 ReLU -> log time), trained
-    by the engine's CUDA kernels on the committed search timings (300
-    matrices, 13 configs of power per block x cache budget for A^8 x) and
-    evaluated on the held-out fifth against the searched optimum and against
-    the best single config."""
+    by the engine's CUDA kernels on committed search timings and evaluated on
+    the held-out fifth against the searched optimum and against the best
+    single config. Tasks: A^8 x over power per block x cache budget (300
+    matrices, 13 configs) and a symmetric GS sweep over requested threads x
+    efficiency threshold (9 configs)."""
     from race_gb300 import tuner
-    path = ROOT / "tests" / "golden" / "tuner_search.npz"
-    if not path.exists():
-        return None
-    ds = tuner.Dataset.load(path)
-    held = np.arange(len(ds.times)) % 5 == 4
-    train, test = ds.subset(~held), ds.subset(held)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    model = tuner.CostModel(seed=0)
-    hist = model.fit(train, seed=0)
-    torch.cuda.synchronize()
-    train_s = time.perf_counter() - t0
-    res = tuner.evaluate(model, test, tuner.best_fixed_config(train))
-    res.update({"train_matrices": len(train.times), "train_seconds": train_s, "final_train_loss": hist[-1]})
-    return res
+    out = {}
+    for name, fname in [("mpk", "tuner_search.npz"), ("symmgs", "tuner_search_symmgs.npz")]:
+        path = ROOT / "tests" / "golden" / fname
+        if not path.exists():
+            continue
+        ds = tuner.Dataset.load(path)
+        held = np.arange(len(ds.times)) % 5 == 4
+        train, test = ds.subset(~held), ds.subset(held)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        model = tuner.CostModel(seed=0, task=tuner.TASKS[ds.task])
+        hist = model.fit(train, seed=0)
+        torch.cuda.synchronize()
+        res = tuner.evaluate(model, test, tuner.best_fixed_config(train))
+        res.update({"train_matrices": len(train.times), "train_seconds": time.perf_counter() - t0,
+                    "final_train_loss": hist[-1]})
+        out[name] = res
+    return out or None
 
 
 def cpu_baseline(A, P, x0, budget_s: float):

@@ -22,6 +22,13 @@ of power p) and learns from the search:
 * ``Tuner.choose``: the MLP's choice, or the search (the fallback when no
   model is loaded, and the judge of the model's regret:
   regret = t(chosen) / t(best searched) - 1).
+
+A second task, ``SWEEP_TASK``, tunes RACE's coloring for a symmetric
+Gauss-Seidel sweep (forward + backward, FP64, distance-2 coloring): requested
+threads in {64, 256, 1024} times the efficiency threshold RACE_EFFICIENCY in
+{20, 40, 80} (src/level_recursion.cpp:48-70). RACE's other recursion knob,
+RACE_MAX_RECURSION_STAGES, steers the recursive MPK partition, which this
+engine does not build (stage 0 only), so it has nothing to tune here.
 """
 from __future__ import annotations
 
@@ -101,8 +108,23 @@ def config_features(mf: np.ndarray, p: int, cache_mb: float) -> np.ndarray:
     return np.asarray(f, np.float32)
 
 
-def feature_rows(mf: np.ndarray) -> np.ndarray:
-    return np.stack([np.concatenate([mf, config_features(mf, p, c)]) for p, c in CONFIGS])
+def sweep_config_features(mf: np.ndarray, threads: int, eff: float) -> np.ndarray:
+    """Features of a coloring config: requested threads and efficiency
+    threshold, alone and against the matrix size and BFS level count."""
+    lt = math.log2(threads)
+    log_n = mf[0] * 20
+    log_levels = mf[15] * 20
+    e = eff / 100.0
+    f = [lt / 12, e, e * e, lt * e / 12, (log_n - lt) / 20, (log_levels - lt) / 20, lt * lt / 144, 1.0]
+    return np.asarray(f, np.float32)
+
+
+SWEEP_CONFIGS = [(t, e) for t in (64, 256, 1024) for e in (20.0, 40.0, 80.0)]
+
+
+def feature_rows(mf: np.ndarray, task=None) -> np.ndarray:
+    task = task or MPK_TASK
+    return np.stack([np.concatenate([mf, task.config_features(mf, *c)]) for c in task.configs])
 
 
 # ---------------------------------------------------------------- search
@@ -150,6 +172,47 @@ def search(A, reps: int = 5, warmup: int = 2, stream=None) -> np.ndarray:
         times[ci] = float(np.median(ts))
         del x
     rc.close()
+    return times
+
+
+def search_sweep(A, reps: int = 5, warmup: int = 2) -> np.ndarray:
+    """Seconds of one symmetric GS sweep (forward + backward, FP64) per
+    coloring config (np.inf where RACEColor fails)."""
+    import torch
+
+    from . import interface as ri
+    times = np.full(len(SWEEP_CONFIGS), np.inf)
+    x0 = torch.tensor(matgen.uniform_vector(A.n, 0), device="cuda")
+    b0 = torch.tensor(matgen.uniform_vector(A.n, 1), device="cuda")
+    for ci, (threads, eff) in enumerate(SWEEP_CONFIGS):
+        rc = ri.Interface(A.n, threads, ri.TWO, A.row_ptr, A.col, symm_hint=True, params={"efficiency": [eff]})
+        if rc.RACEColor() != 0:
+            rc.close()
+            continue
+        P = A.permuted(rc.getPerm(), rc.getInvPerm())
+        x, b = x0.clone(), b0.clone()
+        fid = rc.registerFunction(ri.GS, ri.Operands(ri.DeviceCsr.from_csr(P, "cuda", torch.float64), x, b))
+        if rc.executeFunction(fid) != 0:  # also catches an error code returned in place of an id
+            rc.close()
+            continue
+
+        def run():
+            rc.executeFunctionAsync(fid)
+            rc.executeFunctionAsync(fid, True)
+
+        for _ in range(warmup):
+            run()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            run()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        if rc.getStatus() == 0:
+            times[ci] = float(np.median(ts))
+        rc.close()
     return times
 
 
@@ -266,25 +329,41 @@ class Mlp:
 
 
 # ---------------------------------------------------------------- the tuner
+@dataclasses.dataclass(frozen=True)
+class Task:
+    name: str
+    configs: list
+    config_features: object
+    search: object
+
+
+MPK_TASK = Task("mpk", CONFIGS, config_features, search)
+SWEEP_TASK = Task("symmgs", SWEEP_CONFIGS, sweep_config_features, search_sweep)
+TASKS = {t.name: t for t in (MPK_TASK, SWEEP_TASK)}
+
+
 @dataclasses.dataclass
 class Dataset:
     features: np.ndarray   # (matrices, 24)
     times: np.ndarray      # (matrices, len(CONFIGS)) seconds, inf = infeasible
     families: np.ndarray
     sizes: np.ndarray      # (matrices, 2): n, nnz
+    task: str = "mpk"      # configs of the times' columns: TASKS[task].configs
 
     def save(self, path):
         np.savez_compressed(path, features=self.features, times=self.times, families=self.families,
-                            sizes=self.sizes, configs=np.asarray(CONFIGS))
+                            sizes=self.sizes, configs=np.asarray(TASKS[self.task].configs),
+                            task=np.array(self.task))
 
     @staticmethod
     def load(path) -> "Dataset":
         d = np.load(path)
-        assert [tuple(c) for c in d["configs"]] == CONFIGS, "config space changed"
-        return Dataset(d["features"], d["times"], d["families"], d["sizes"])
+        task = str(d["task"]) if "task" in d.files else "mpk"
+        assert [tuple(c) for c in d["configs"]] == [tuple(c) for c in TASKS[task].configs], "config space changed"
+        return Dataset(d["features"], d["times"], d["families"], d["sizes"], task)
 
     def subset(self, idx) -> "Dataset":
-        return Dataset(self.features[idx], self.times[idx], self.families[idx], self.sizes[idx])
+        return Dataset(self.features[idx], self.times[idx], self.families[idx], self.sizes[idx], self.task)
 
 
 def regret(times_row: np.ndarray, choice: int) -> float:
@@ -294,15 +373,16 @@ def regret(times_row: np.ndarray, choice: int) -> float:
 class CostModel:
     """MLP regression of log time on (matrix, config) features."""
 
-    def __init__(self, seed: int = 0):
+    def __init__(self, seed: int = 0, task: Task = None):
         self.net = Mlp(seed=seed)
+        self.task = task or MPK_TASK
         self.mu = 0.0
         self.sd = 1.0
 
     def _rows(self, ds: Dataset):
         X, T = [], []
         for mf, tr in zip(ds.features, ds.times):
-            rows = feature_rows(mf)
+            rows = feature_rows(mf, self.task)
             ok = np.isfinite(tr)
             X.append(rows[ok])
             T.append(np.log(tr[ok]))
@@ -319,7 +399,7 @@ class CostModel:
     def predict(self, mf: np.ndarray) -> np.ndarray:
         """Predicted seconds of every config."""
         import torch
-        y = self.net.forward(torch.tensor(feature_rows(mf), device="cuda")).cpu().numpy()[:, 0]
+        y = self.net.forward(torch.tensor(feature_rows(mf, self.task), device="cuda")).cpu().numpy()[:, 0]
         return np.exp(y * self.sd + self.mu)
 
     def choose(self, mf: np.ndarray, feasible: Optional[np.ndarray] = None) -> int:
@@ -333,7 +413,7 @@ def best_fixed_config(ds: Dataset) -> int:
     """The single config with the lowest mean regret over a dataset (the
     method without the model)."""
     best, arg = np.inf, 0
-    for ci in range(len(CONFIGS)):
+    for ci in range(len(TASKS[ds.task].configs)):
         r = [regret(t, ci) if np.isfinite(t[ci]) else 10.0 for t in ds.times]
         if np.mean(r) < best:
             best, arg = float(np.mean(r)), ci
@@ -355,48 +435,51 @@ def evaluate(model: CostModel, ds: Dataset, fixed: int) -> dict:
     return {"matrices": len(rm), "mlp_mean_regret": float(rm.mean()), "mlp_median_regret": float(np.median(rm)),
             "mlp_p90_regret": float(np.percentile(rm, 90)), "mlp_within_10pct": float((rm <= 0.10).mean()),
             "mlp_top2_mean_regret": float(rs.mean()), "mlp_top2_within_10pct": float((rs <= 0.10).mean()),
-            "fixed_config": list(CONFIGS[fixed]), "fixed_mean_regret": float(rf.mean()),
+            "fixed_config": list(TASKS[ds.task].configs[fixed]), "fixed_mean_regret": float(rf.mean()),
             "fixed_within_10pct": float((rf <= 0.10).mean())}
 
 
 class Tuner:
-    """Parameter choice for A^8 x: the trained cost model when one is given,
-    else (and on request) the exhaustive search."""
+    """Parameter choice for one task (A^8 x by default): the trained cost
+    model when one is given, else (and on request) the exhaustive search."""
 
-    def __init__(self, model: Optional[CostModel] = None):
+    def __init__(self, model: Optional[CostModel] = None, task: Task = None):
         self.model = model
+        self.task = model.task if model is not None else (task or MPK_TASK)
 
     def choose(self, A, mode: str = "auto"):
-        """Returns ((p, cacheMB), info). mode: 'mlp', 'search' or 'auto'
-        (the model when loaded, else the search)."""
+        """Returns (config, info); config is (p, cacheMB) for the MPK task and
+        (threads, efficiency) for the sweep task. mode: 'mlp', 'search' or
+        'auto' (the model when loaded, else the search)."""
         if mode == "search" or (mode == "auto" and self.model is None):
             t0 = time.perf_counter()
-            tr = search(A)
-            return CONFIGS[int(np.argmin(tr))], {"how": "search", "seconds": time.perf_counter() - t0}
+            tr = self.task.search(A)
+            return self.task.configs[int(np.argmin(tr))], {"how": "search", "seconds": time.perf_counter() - t0}
         t0 = time.perf_counter()
         c = self.model.choose(matrix_features(A))
-        return CONFIGS[c], {"how": "mlp", "seconds": time.perf_counter() - t0}
+        return self.task.configs[c], {"how": "mlp", "seconds": time.perf_counter() - t0}
 
 
 def build_dataset(count: int, seed: int = 0, nmin: int = 20_000, nmax: int = 400_000, log=None,
-                  out=None, save_every: int = 10) -> Dataset:
-    """Search `count` matrices of the seeded set; with `out`, the partial
-    dataset is saved every `save_every` matrices."""
+                  out=None, save_every: int = 10, task: str = "mpk") -> Dataset:
+    """Search `count` matrices of the seeded set for one task; with `out`,
+    the partial dataset is saved every `save_every` matrices."""
     feats, times, fams, sizes = [], [], [], []
+    tk = TASKS[task]
 
     def ds():
-        return Dataset(np.stack(feats), np.stack(times), np.asarray(fams), np.asarray(sizes, np.int64))
+        return Dataset(np.stack(feats), np.stack(times), np.asarray(fams), np.asarray(sizes, np.int64), task)
 
     for i in range(count):
         fam, A = dataset_matrix(i, seed, nmin, nmax)
         t0 = time.perf_counter()
-        tr = search(A)
+        tr = tk.search(A)
         feats.append(matrix_features(A))
         times.append(tr)
         fams.append(fam)
         sizes.append((A.n, A.nnz))
         if log:
-            log(f"{i} {fam} n={A.n} nnz={A.nnz} best={CONFIGS[int(np.argmin(tr))]} "
+            log(f"{i} {fam} n={A.n} nnz={A.nnz} best={tk.configs[int(np.argmin(tr))]} "
                 f"{time.perf_counter() - t0:.1f}s")
         if out is not None and (i + 1) % save_every == 0:
             ds().save(out)
@@ -409,14 +492,25 @@ def build_dataset(count: int, seed: int = 0, nmin: int = 20_000, nmax: int = 400
 def main(argv=None):
     import argparse
     ap = argparse.ArgumentParser(description="parameter search for the MPK tuner (needs a GPU)")
-    ap.add_argument("command", choices=["search"])
+    ap.add_argument("command", choices=["search", "merge"],
+                    help="search: time every config of --count matrices; merge: concatenate saved datasets "
+                         "(the inputs) of one task into --out")
+    ap.add_argument("inputs", nargs="*")
     ap.add_argument("--count", type=int, default=300)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--nmin", type=int, default=20_000)
     ap.add_argument("--nmax", type=int, default=400_000)
+    ap.add_argument("--task", choices=sorted(TASKS), default="mpk")
     ap.add_argument("--out", required=True)
-    a = ap.parse_args(argv)
-    build_dataset(a.count, a.seed, a.nmin, a.nmax, log=lambda s: print(s, flush=True), out=a.out)
+    a = ap.parse_intermixed_args(argv)
+    if a.command == "merge":
+        parts = [Dataset.load(p) for p in a.inputs]
+        assert parts and len({d.task for d in parts}) == 1, "merge needs datasets of one task"
+        Dataset(np.concatenate([d.features for d in parts]), np.concatenate([d.times for d in parts]),
+                np.concatenate([d.families for d in parts]), np.concatenate([d.sizes for d in parts]),
+                parts[0].task).save(a.out)
+        return
+    build_dataset(a.count, a.seed, a.nmin, a.nmax, log=lambda s: print(s, flush=True), out=a.out, task=a.task)
 
 
 if __name__ == "__main__":

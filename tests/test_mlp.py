@@ -65,3 +65,22 @@ def test_cost_model_beats_best_fixed_config_on_held_out_matrices():
     assert res["mlp_mean_regret"] <= 0.10
     assert res["mlp_within_10pct"] > res["fixed_within_10pct"]
     assert res["mlp_top2_mean_regret"] <= res["mlp_mean_regret"] + 1e-12
+
+
+GOLDEN_SWEEP = pathlib.Path(__file__).resolve().parent / "golden" / "tuner_search_symmgs.npz"
+
+
+@pytest.mark.skipif(not GOLDEN_SWEEP.exists(), reason="no committed search timings")
+def test_cost_model_coloring_knobs_held_out():
+    """The same network on the coloring task (requested threads x efficiency
+    threshold for a symmetric GS sweep): better than the best single config
+    on held-out matrices."""
+    ds = tuner.Dataset.load(GOLDEN_SWEEP)
+    assert ds.task == "symmgs"
+    held = np.arange(len(ds.times)) % 5 == 4
+    train, test = ds.subset(~held), ds.subset(held)
+    model = tuner.CostModel(seed=0, task=tuner.SWEEP_TASK)
+    model.fit(train, epochs=300, seed=0)
+    res = tuner.evaluate(model, test, tuner.best_fixed_config(train))
+    print(res)
+    assert res["mlp_mean_regret"] <= res["fixed_mean_regret"]
