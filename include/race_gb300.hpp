@@ -90,6 +90,19 @@ class Interface {
         return rc == RACE_SUCCESS ? id : rc;
     }
     int executeFunction(int funcId, bool rev = false) { return race_execute_function(e_, funcId, rev ? 1 : 0); }
+    // No counterpart in the reference: enqueue without waiting, and the
+    // status word of the last launch (waits for the stream).
+    int executeFunctionAsync(int funcId, bool rev = false) {
+        return race_execute_function_async(e_, funcId, rev ? 1 : 0);
+    }
+    int getStatus() { return race_get_status(e_); }
+    // Matrix power over nrhs right-hand sides (race_register_mpk_block);
+    // returns the function id, or the error code like registerFunction.
+    int registerMpkBlock(const race_operands &args, int power, int nrhs) {
+        int id = -1;
+        int rc = race_register_mpk_block(e_, &args, power, nrhs, &id);
+        return rc == RACE_SUCCESS ? id : rc;
+    }
     void setPower(int funcId, int pow) { race_set_power(e_, funcId, pow); }
     int getPower(int funcId) {
         int v = 0;
@@ -102,6 +115,29 @@ class Interface {
   private:
     race_engine *e_ = nullptr;
     int nrow_;
+};
+
+// Block-MPK functions of several Interfaces in one persistent launch
+// (race_batch_*; no counterpart in the reference). The Interfaces and their
+// operands must outlive the batch.
+class Batch {
+  public:
+    Batch() {
+        if (race_batch_create(&b_) != RACE_SUCCESS) throw std::runtime_error("race_batch_create failed");
+    }
+    ~Batch() { race_batch_destroy(b_); }
+    Batch(const Batch &) = delete;
+    Batch &operator=(const Batch &) = delete;
+    int add(Interface &ce, int funcId) { return race_batch_add(b_, ce.handle(), funcId); }
+    int prepare(void *cudaStream = nullptr) { return race_batch_prepare(b_, cudaStream); }
+    int execute(void *cudaStream = nullptr) { return race_batch_execute(b_, cudaStream); }
+    // first call captures the launch into a CUDA graph, later calls replay it
+    int graphLaunch(void *cudaStream = nullptr) { return race_batch_graph_launch(b_, cudaStream); }
+    int getStatus(void *cudaStream = nullptr) { return race_batch_get_status(b_, cudaStream); }
+    const char *lastError() { return race_batch_last_error(b_); }
+
+  private:
+    race_batch *b_ = nullptr;
 };
 
 }  // namespace gb300

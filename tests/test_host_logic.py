@@ -113,3 +113,34 @@ def test_phases_reproduce_reference_order(golden, mats, m, d, t):
         _run_phases(pp, lo, hi, kern, mat, x2, b2)
         np.testing.assert_array_equal(x1, x2)
         np.testing.assert_array_equal(b1, b2)
+
+
+def test_cpp_header_compiles(tmp_path):
+    """The header-only C++ Interface (include/race_gb300.hpp) compiles against
+    the C ABI and exposes the reference's method names."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    src = tmp_path / "use.cpp"
+    src.write_text("""
+#include "race_gb300.hpp"
+int use(int n, int *rp, int *col, race_operands ops) {
+    RACE::gb300::Interface ce(n, 8, RACE::gb300::POWER, rp, col, true);
+    int rc = ce.RACEColor(4, 1e6);
+    int *perm = nullptr, len = 0;
+    ce.getPerm(&perm, &len);
+    delete[] perm;
+    int f = ce.registerFunction(RACE::gb300::MPK, ops, 4);
+    int g = ce.registerMpkBlock(ops, 4, 16);
+    RACE::gb300::Batch b;
+    b.add(ce, g);
+    b.graphLaunch();
+    return rc + f + ce.executeFunctionAsync(f) + ce.getStatus() + b.getStatus() + ce.getNumThreads();
+}
+""")
+    root = pathlib.Path(__file__).resolve().parents[1]
+    r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-I", str(root / "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
