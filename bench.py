@@ -424,6 +424,7 @@ def main():
     symmgs = bench_symmgs(args, ri, matgen, torch) if args.symmgs_rows > 0 else None
     batched = bench_batch(args, ri, matgen, torch) if args.batch_count > 0 else None
     tuned = bench_tuner(torch) if not args.no_tuner else None
+    c1 = bench_c1(ri, matgen, torch) if rank == 0 else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
@@ -452,6 +453,7 @@ def main():
             "symmgs_ir": symmgs,
             "batched_mpk": batched,
             "mlp_tuner": tuned,
+            "symmspmv_c1": c1,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -599,6 +601,60 @@ def bench_batch(args, ri, matgen, torch):
     out.update(results)
     out["mixed_f32_speedup_vs_f64_plain"] = results["f64"]["ms_plain"] / results["f32"]["ms_graph"]
     return out
+
+
+def bench_c1(ri, matgen, torch, reps: int = 100):
+    """SymmSpMV with RACE distance-2 coloring on the 32^3 7-point Laplacian
+    (n = 32,768, upper triangle 128,000 entries incl. the diagonal), x
+    U[-1,1] seed 0, 100 calls per setting. Bytes per call: 12 nnz_u + 4(n+1)
+    + 8n (x) + 16n (b read and written) = 2,453,508 B; the working set
+    (2.5 MB) lives in L2, so "% of HBM" does not apply and the time is the
+    latency of RACE's phases. Requested threads (RACE_THREADS, 256/1024/4096)
+    and sweep mode (wave/leaf) are searched as a user tunes them; the best is
+    reported with all settings. The CPU figure is the sequential restatement
+    of the kernel body over all rows (one core)."""
+    from oracle import oracle as orc
+    A = matgen.laplace3d_7pt(32)
+    x0 = matgen.uniform_vector(A.n, 0)
+    nbytes = None
+    settings = []
+    for threads in (256, 1024, 4096):
+        rc = ri.Interface(A.n, threads, ri.TWO, A.row_ptr, A.col, symm_hint=True)
+        assert rc.RACEColor() == 0
+        P = A.permuted(rc.getPerm(), rc.getInvPerm())
+        U = P.upper()
+        nbytes = 12 * U.nnz + 4 * (A.n + 1) + 24 * A.n
+        x = torch.tensor(x0, device="cuda")
+        b = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+        fid = rc.registerFunction(ri.SYMMSPMV, ri.Operands(ri.DeviceCsr.from_csr(U), x, b))
+        assert fid >= 0
+        info = rc.getSweepInfo(fid)
+        for mode, mname in ((ri.SWEEP_WAVE, "wave"), (ri.SWEEP_LEAF, "leaf")):
+            rc.setSweepMode(mode)
+            for _ in range(5):
+                rc.executeFunctionAsync(fid)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                rc.executeFunctionAsync(fid)
+            e1.record()
+            torch.cuda.synchronize()
+            assert rc.getStatus() == 0
+            settings.append({"threads": threads, "threads_used": rc.getNumThreads(), "mode": mname,
+                             "waves": info["waves"], "phases": info["phases"],
+                             "ms": e0.elapsed_time(e1) / reps})
+        rc.close()
+    best = min(settings, key=lambda d: d["ms"])
+    U = A.upper()
+    xr, br = x0.copy(), np.zeros(A.n)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        orc.run_kernel(orc.K_SYMMSPMV, 0, A.n, U, xr, br)
+    cpu_ms = (time.perf_counter() - t0) / reps * 1e3
+    return {"workload": f"SymmSpMV, 7-point Laplacian 32^3, RACE D2, {reps} calls per setting",
+            "bytes_per_call": nbytes, "best": best, "gpu_gbs_best": nbytes / (best["ms"] * 1e-3) / 1e9,
+            "settings": settings, "cpu_port_ms_per_call": cpu_ms, "cpu_port_cores": 1}
 
 
 def bench_tuner(torch):
