@@ -41,34 +41,30 @@ __device__ __forceinline__ unsigned ldAcquireU(const unsigned *p) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void stReleaseU(unsigned *p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
-// Sense-reversing grid barrier. bar[0] arrivals, bar[1] generation. Returns
-// false (and sets *status) if the wait exceeded the spin limit.
+// Grid barrier on a monotonic arrival counter (bar[0], zeroed at launch).
+// Every block arrives once per barrier and no block can arrive at the next
+// barrier before all have arrived at this one, so the arrivals of barrier k
+// are k*G+1 .. (k+1)*G (G = gridDim.x): a block's own arrival number gives
+// the count to wait for, with no reset or generation word (one atomic and
+// the polling, instead of three dependent round trips). Returns false (and
+// sets *status) if the wait exceeded the spin limit.
 __device__ bool gridBarrier(unsigned *bar, int *status) {
     __shared__ int sOk;
     __syncthreads();
     if (threadIdx.x == 0) {
         sOk = 1;
-        unsigned gen = ldAcquireU(bar + 1);
         __threadfence();
-        unsigned arrived = atomicAdd(bar, 1u) + 1;
-        if (arrived == gridDim.x) {
-            bar[0] = 0;
-            __threadfence();
-            stReleaseU(bar + 1, gen + 1);
-        } else {
-            long long spins = 0;
-            while (ldAcquireU(bar + 1) == gen) {
-                if (++spins > kSpinLimit) {
-                    atomicCAS(status, DEV_OK, DEV_WAIT_TIMEOUT);
-                    sOk = 0;
-                    break;
-                }
-                __nanosleep(32);
+        const unsigned arrived = atomicAdd(bar, 1u) + 1;
+        const unsigned target = ((arrived - 1) / gridDim.x + 1) * gridDim.x;
+        long long spins = 0;
+        while (ldAcquireU(bar) < target) {
+            if (++spins > kSpinLimit) {
+                atomicCAS(status, DEV_OK, DEV_WAIT_TIMEOUT);
+                sOk = 0;
+                break;
             }
+            __nanosleep(32);
         }
     }
     __syncthreads();
