@@ -19,9 +19,9 @@ struct DevPhases {
     DevBuf<int> phasePtr, leafLo, leafHi;
 };
 
-// Tiles of a matrix-power operand set: contiguous row ranges whose
-// non-zeros fit the kernel's shared-memory stage, in RACE's wavefront order,
-// with the last tile each one depends on.
+// Schedule and layout of one registered matrix-power function: the
+// permuted matrix in SELL-32 chunks inside RACE's level groups, the chunks'
+// dependency ranges, and the (power, chunk) work items in wavefront order.
 struct MpkPlan {
     int numChunks = 0;          // SELL-32 chunks (<= 32 rows, inside one level group)
     int power = 0;
