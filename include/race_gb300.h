@@ -134,8 +134,8 @@ int race_get_phases(race_engine *e, int rev, int *phasePtr, int *leafLo, int *le
 int race_get_power_groups(race_engine *e, int *buf, int cap, int *len);
 
 /* Interface::registerFunction (interface.h:149-157, interface.cpp:391-485)
- * with a built-in device kernel in place of a host callback; `power` is used
- * by RACE_K_MPK. */
+ * with a built-in device kernel in place of a host callback; `power`
+ * (1..255) is used by RACE_K_MPK. */
 int race_register_function(race_engine *e, int kernel, const race_operands *ops, int power, int *func_id);
 /* Interface::executeFunction (interface.h:167, interface.cpp:541-572):
  * enqueues the kernel on the engine's stream, waits for it and returns

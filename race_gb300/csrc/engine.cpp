@@ -117,7 +117,7 @@ int Engine::registerFunction(int kernel, const race_operands &ops, int power) {
     if (kernel == RACE_K_MPK) {
         // interface.cpp:438-458
         if (dist != DIST_POWER || !powerReady) throw Error(RACE_ERR_INVALID_ARG, "MPK needs RACEColor(power, ...) first");
-        if (power < 1) throw Error(RACE_ERR_INVALID_ARG, "power must be >= 1");
+        if (power < 1 || power > 255) throw Error(RACE_ERR_INVALID_ARG, "power must be in 1..255");
         if (!ops.x) throw Error(RACE_ERR_INVALID_ARG, "missing x");
         f.mpk = buildMpkPlan(*this, ops, power);
     } else {
@@ -378,6 +378,7 @@ int race_set_power(race_engine *e, int func_id, int power) {
             if (power < 1 || power > 255) throw Error(RACE_ERR_INVALID_ARG, "power must be in 1..255");
             f.block = race::buildBlockPlan(*e->eng, f.ops, power, f.block->nrhs);
         } else if (f.kernel == RACE_K_MPK && power != f.power) {
+            if (power < 1 || power > 255) throw Error(RACE_ERR_INVALID_ARG, "power must be in 1..255");
             f.mpk = race::buildMpkPlan(*e->eng, f.ops, power);
         }
         f.power = power;

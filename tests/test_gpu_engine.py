@@ -334,6 +334,15 @@ def test_error_codes(mats):
     rp = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
     assert rp.RACEColor() == 1  # coloring needs dist ONE/TWO (interface.cpp:264-267)
     assert rp.RACEColor(4, 1e6, 2.0, "N", 0) == 1  # sub power < 1
+    assert rp.RACEColor(4, 1e6) == 0
+    dmp = _upload(A.permuted(rp.getPerm(), rp.getInvPerm()))
+    xp = torch.zeros(257 * A.n, dtype=torch.float64, device="cuda")
+    assert rp.registerFunction(ri.MPK, ri.Operands(dmp, xp), power=256) == 1  # powers are stored in 8 bits
+    fp = rp.registerFunction(ri.MPK, ri.Operands(dmp, xp), power=4)
+    assert rp.getPower(fp) == 4  # a real function id, not an error code
+    with pytest.raises(Exception):
+        rp.setPower(fp, 300)
+    assert rp.getPower(fp) == 4
     d1 = ri.Interface(A.n, 8, ri.ONE, A.row_ptr, A.col, symm_hint=True)
     assert d1.RACEColor() == 0
     b = torch.zeros(A.n, dtype=torch.float64, device="cuda")
