@@ -282,6 +282,15 @@ int race_lb_balance(const int *levelRow, const int *levelNnz, int totalLevel, in
 int race_flatten_zone_tree(const int *tree, int treeLen, int dist, int d2type, int rev, int serialLo, int serialHi,
                            int *phasePtr, int *leafLo, int *leafHi, int cap, int *numPhases, int *numLeaves);
 
+/* Host-only: the wave plan of built-in kernel `kernel` on a CRS pattern
+ * (host arrays) for a phase table (as from race_get_phases): rows grouped
+ * into conflict-free waves that keep RACE's order between every pair of
+ * conflicting accesses. wavePtr (numWaves+1) and rows (numRows) are written
+ * when cap is large enough for both (call once with cap 0 for the sizes).
+ * No counterpart in the reference; exposed for inspection and tests. */
+int race_wave_plan(int kernel, int n, const int *rowPtr, const int *col, const int *phasePtr, const int *leafLo,
+                   const int *leafHi, int numPhases, int *wavePtr, int *rows, int cap, int *numWaves, int *numRows);
+
 /* Last error message of this engine (NUL-terminated, owned by the engine). */
 const char *race_last_error(race_engine *e);
 

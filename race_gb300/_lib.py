@@ -32,7 +32,7 @@ EXPORTS = [
     "race_batch_create", "race_batch_destroy", "race_batch_add", "race_batch_prepare", "race_batch_execute",
     "race_batch_graph_launch", "race_batch_get_status", "race_batch_info", "race_batch_last_error",
     "race_mlp_create", "race_mlp_destroy", "race_mlp_num_params", "race_mlp_set_params", "race_mlp_get_params",
-    "race_mlp_forward", "race_mlp_loss_grad", "race_mlp_adam_step", "race_mlp_last_error",
+    "race_mlp_forward", "race_mlp_loss_grad", "race_mlp_adam_step", "race_mlp_last_error", "race_wave_plan",
 ]
 
 
@@ -90,6 +90,7 @@ def lib():
             "race_mlp_get_params": [vp, vp, C.c_longlong], "race_mlp_forward": [vp, vp, i, vp, vp],
             "race_mlp_loss_grad": [vp, vp, vp, i, vp, vp, vp],
             "race_mlp_adam_step": [vp, C.c_float, C.c_float, C.c_float, C.c_float, vp],
+            "race_wave_plan": [i, i, vp, vp, vp, vp, vp, i, vp, vp, i, ip, ip],
         }
         for name, args in sig.items():
             fn = getattr(L, name)

@@ -482,6 +482,25 @@ int race_flatten_zone_tree(const int *tree, int treeLen, int dist, int d2type, i
     });
 }
 
+int race_wave_plan(int kernel, int n, const int *rowPtr, const int *col, const int *phasePtr, const int *leafLo,
+                   const int *leafHi, int numPhases, int *wavePtr, int *rows, int cap, int *numWaves, int *numRows) {
+    if (!rowPtr || !col || !phasePtr || !leafLo || !leafHi || n < 0 || numPhases < 0 || !numWaves || !numRows)
+        return RACE_ERR_INVALID_ARG;
+    return guard(nullptr, [&] {
+        race::PhaseTable pt;
+        pt.phasePtr.assign(phasePtr, phasePtr + numPhases + 1);
+        pt.leafLo.assign(leafLo, leafLo + pt.phasePtr.back());
+        pt.leafHi.assign(leafHi, leafHi + pt.phasePtr.back());
+        race::WavePlan wp = race::buildWavePlan(kernel, n, rowPtr, col, pt);
+        *numWaves = wp.numWaves();
+        *numRows = (int)wp.rows.size();
+        if (wavePtr && rows && cap >= (int)wp.rows.size() && cap >= wp.numWaves() + 1) {
+            memcpy(wavePtr, wp.wavePtr.data(), sizeof(int) * wp.wavePtr.size());
+            memcpy(rows, wp.rows.data(), sizeof(int) * wp.rows.size());
+        }
+    });
+}
+
 const char *race_last_error(race_engine *e) { return e ? e->err.c_str() : "null engine"; }
 
 int race_register_mpk_block(race_engine *e, const race_operands *ops, int power, int nrhs, int *func_id) {

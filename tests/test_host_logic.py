@@ -144,3 +144,53 @@ int use(int n, int *rp, int *col, race_operands ops) {
     r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-I", str(root / "include"), str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def _wave_plan(kernel, mat, pp, lo, hi):
+    L = _lib.lib()
+    rp, cl = np.ascontiguousarray(mat.row_ptr, np.int32), np.ascontiguousarray(mat.col, np.int32)
+    pp, lo, hi = (np.ascontiguousarray(a, np.int32) for a in (pp, lo, hi))
+    nw, nr = C.c_int(), C.c_int()
+    args = [kernel, mat.n, rp.ctypes.data, cl.ctypes.data, pp.ctypes.data, lo.ctypes.data, hi.ctypes.data,
+            len(pp) - 1]
+    _lib.check(L.race_wave_plan(*args, None, None, 0, C.byref(nw), C.byref(nr)))
+    cap = max(nr.value, nw.value + 1)
+    wp, rows = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
+    _lib.check(L.race_wave_plan(*args, wp.ctypes.data, rows.ctypes.data, cap, C.byref(nw), C.byref(nr)))
+    return wp[: nw.value + 1], rows[: nr.value]
+
+
+@pytest.mark.parametrize("m,d,t", sorted(EXEC_CASES) + [("lap7_32", 2, 1024), ("lap7_32", 1, 256)])
+def test_wave_plans_reproduce_the_sequential_walk(golden, mats, m, d, t):
+    """The wave compiler behind the GPU's bit-exact sweeps: every row of a
+    wave is run on its own, in REVERSED order inside each wave, and the
+    result still equals the sequential walk of the reference's phases bit
+    for bit, for every kernel (and both directions of the sweeps): rows of one wave do not
+    conflict and the order of conflicting accesses is RACE's."""
+    A = mats[m]
+    k = key_color(m, d, t)
+    perm = golden[k + "__perm"]
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(A.n, dtype=np.int32)
+    P = A.permuted(perm, inv)
+    U = P.upper()
+    x0 = matgen.uniform_vector(A.n, 0)
+    b0 = matgen.uniform_vector(A.n, 1)
+    kernels = [(orc.K_GS, P), (orc.K_SPMV, P)]
+    if d == 2:
+        kernels += [(orc.K_SYMMSPMV, U), (orc.K_KACZ, P), (orc.K_SPMTV, P)]
+    for kern, mat in kernels:
+        # only the sweeps run backward (the oracle's product kernels take forward ranges)
+        for rev in ((False, True) if kern in (orc.K_GS, orc.K_KACZ) else (False,)):
+            zero_b = kern in (orc.K_SPMV, orc.K_SYMMSPMV, orc.K_SPMTV)
+            x1, b1 = x0.copy(), (np.zeros(A.n) if zero_b else b0.copy())
+            x2, b2 = x1.copy(), b1.copy()
+            pp, lo, hi = _flatten(golden[k + "__tree"], d, rev, A.n)
+            _run_phases(pp, lo, hi, kern, mat, x1, b1)
+            wp, rows = _wave_plan(kern, mat, pp, lo, hi)
+            assert np.array_equal(np.sort(rows), np.arange(A.n))
+            for w in range(len(wp) - 1):
+                for r in rows[wp[w]:wp[w + 1]][::-1]:
+                    orc.run_kernel(kern, int(r), int(r) + 1, mat, x2, b2)
+            np.testing.assert_array_equal(x1, x2, err_msg=f"{kern} rev={rev}")
+            np.testing.assert_array_equal(b1, b2, err_msg=f"{kern} rev={rev}")
