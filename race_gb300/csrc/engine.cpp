@@ -486,6 +486,15 @@ int race_wave_plan(int kernel, int n, const int *rowPtr, const int *col, const i
                    const int *leafHi, int numPhases, int *wavePtr, int *rows, int cap, int *numWaves, int *numRows) {
     if (!rowPtr || !col || !phasePtr || !leafLo || !leafHi || n < 0 || numPhases < 0 || !numWaves || !numRows)
         return RACE_ERR_INVALID_ARG;
+    if (kernel < RACE_K_SPMV || kernel > RACE_K_KACZ || phasePtr[0] != 0) return RACE_ERR_INVALID_ARG;
+    for (int p = 0; p < numPhases; ++p)
+        if (phasePtr[p + 1] < phasePtr[p]) return RACE_ERR_INVALID_ARG;
+    for (int l = 0; l < phasePtr[numPhases]; ++l) {
+        // forward leaf [lo, hi) or backward leaf (hi, lo], inside 0..n-1
+        const int lo = leafLo[l], hi = leafHi[l];
+        const bool ok = lo <= hi ? (lo >= 0 && hi <= n) : (hi >= -1 && lo < n);
+        if (!ok) return RACE_ERR_INVALID_ARG;
+    }
     return guard(nullptr, [&] {
         race::PhaseTable pt;
         pt.phasePtr.assign(phasePtr, phasePtr + numPhases + 1);

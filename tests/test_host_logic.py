@@ -194,3 +194,24 @@ def test_wave_plans_reproduce_the_sequential_walk(golden, mats, m, d, t):
                     orc.run_kernel(kern, int(r), int(r) + 1, mat, x2, b2)
             np.testing.assert_array_equal(x1, x2, err_msg=f"{kern} rev={rev}")
             np.testing.assert_array_equal(b1, b2, err_msg=f"{kern} rev={rev}")
+
+
+def test_wave_plan_rejects_bad_phase_tables():
+    L = _lib.lib()
+    rp = np.array([0, 1, 2], np.int32)
+    cl = np.array([0, 1], np.int32)
+    nw, nr = C.c_int(), C.c_int()
+
+    def call(kernel, pp, lo, hi):
+        pp, lo, hi = (np.ascontiguousarray(a, np.int32) for a in (pp, lo, hi))
+        return L.race_wave_plan(kernel, 2, rp.ctypes.data, cl.ctypes.data, pp.ctypes.data, lo.ctypes.data,
+                                hi.ctypes.data, len(pp) - 1, None, None, 0, C.byref(nw), C.byref(nr))
+
+    assert call(orc.K_GS, [0, 1], [0], [2]) == _lib.RACE_SUCCESS and (nw.value, nr.value) == (1, 2)  # diagonal: one wave
+    assert call(orc.K_GS, [0, 1], [1], [-1]) == _lib.RACE_SUCCESS and nr.value == 2  # backward leaf
+    bad = _lib.RACE_ERR_INVALID_ARG
+    assert call(orc.K_GS, [0, 1], [0], [3]) == bad      # past the last row
+    assert call(orc.K_GS, [0, 1], [2], [0]) == bad      # backward leaf from row n
+    assert call(orc.K_GS, [1, 1], [0], [2]) == bad      # phase table not from 0
+    assert call(orc.K_GS, [0, 1, 0], [0], [2]) == bad   # phases not monotonic
+    assert call(5, [0, 1], [0], [2]) == bad             # MPK has no wave plan
