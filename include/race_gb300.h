@@ -291,6 +291,42 @@ int race_flatten_zone_tree(const int *tree, int treeLen, int dist, int d2type, i
 int race_wave_plan(int kernel, int n, const int *rowPtr, const int *col, const int *phasePtr, const int *leafLo,
                    const int *leafHi, int numPhases, int *wavePtr, int *rows, int cap, int *numWaves, int *numRows);
 
+/* RACE::Interface::getHighestPower (interface.cpp:1055-1058): the highest
+ * power given to race_power_prepare (1 before it). */
+int race_get_highest_power(race_engine *e, int *power);
+
+/* SELL-C-sigma preparation for SIMD kernels, RACE::Interface::simdify and
+ * simdifyD1 (include/interface.h:179-185; include/simdify.h,
+ * src/sell_c_sigmize.cpp). Host arrays in the reference's layout: entry j of
+ * row r at chunkStart[r/C] + r%C + j*C, rl[r] row r's length, clp[c] chunk
+ * c's padded length; C a multiple of simdWidth; the matrix in the engine's
+ * permuted order. col and val (val_type RACE_VAL_F64/F32/BF16; val may be
+ * NULL) are rewritten in place.
+ *
+ * race_simdify (distance-2 scatter kernels): pads each row of each leaf
+ * [start, end) of the forward schedule with columns start + (row-start) %
+ * simdWidth, then reorders the rows so that the simdWidth rows of a SIMD
+ * group hold pairwise different columns in every slot (diagonal kept in slot
+ * 0 with diagFirst). The engine must be colored and nrows its row count.
+ * RACE_ERR_INCOMPATIBILITY when a row cannot be placed (the reference's
+ * `false`; the arrays are then partly rearranged, as there). collisions
+ * (nullable): rows that needed a move. */
+int race_simdify(race_engine *e, int simdWidth, int C, int nrows, int *col, const int *chunkStart, const int *rl,
+                 const int *clp, void *val, int val_type, int diagFirst, int *collisions);
+
+/* Host-only: race_simdify on an explicit forward schedule (leaves as from
+ * race_get_phases or race_flatten_zone_tree). No engine needed. */
+int race_simdify_schedule(int simdWidth, int C, int nrows, int *col, const int *chunkStart, const int *rl,
+                          const int *clp, void *val, int val_type, int diagFirst, const int *leafLo,
+                          const int *leafHi, int numLeaves, int *collisions);
+
+/* Host-only, simdifyD1 (distance-1 kernels such as Gauss-Seidel): moves each
+ * row's entries on the earlier rows of its SIMD group to the row's last
+ * slots, nearest row last (dist2Compatible = 0) or first (1). rl is unused,
+ * as in the reference. */
+int race_simdify_d1(int simdWidth, int C, int nrows, int *col, const int *chunkStart, const int *rl, const int *clp,
+                    void *val, int val_type, int dist2Compatible);
+
 /* Last error message of this engine (NUL-terminated, owned by the engine). */
 const char *race_last_error(race_engine *e);
 

@@ -109,6 +109,33 @@ class Interface {
         race_get_power(e_, funcId, &v);
         return v;
     }
+    int getHighestPower() {
+        int v = 0;
+        race_get_highest_power(e_, &v);
+        return v;
+    }
+    // SELL-C-sigma preparation (interface.h:179-185): true on success, false
+    // when a row cannot be placed, as in the reference.
+    bool simdify(int simdWidth, int C, int nrows, int *col, int *chunkStart, int *rl, int *clp, double *val,
+                 bool diagFirst = false) {
+        return race_simdify(e_, simdWidth, C, nrows, col, chunkStart, rl, clp, val, RACE_VAL_F64, diagFirst ? 1 : 0,
+                            nullptr) == RACE_SUCCESS;
+    }
+    bool simdify(int simdWidth, int C, int nrows, int *col, int *chunkStart, int *rl, int *clp, float *val,
+                 bool diagFirst = false) {
+        return race_simdify(e_, simdWidth, C, nrows, col, chunkStart, rl, clp, val, RACE_VAL_F32, diagFirst ? 1 : 0,
+                            nullptr) == RACE_SUCCESS;
+    }
+    bool simdifyD1(int simdWidth, int C, int nrows, int *col, int *chunkStart, int *rl, int *clp, double *val,
+                   bool dist2Compatible = false) {
+        return race_simdify_d1(simdWidth, C, nrows, col, chunkStart, rl, clp, val, RACE_VAL_F64,
+                               dist2Compatible ? 1 : 0) == RACE_SUCCESS;
+    }
+    bool simdifyD1(int simdWidth, int C, int nrows, int *col, int *chunkStart, int *rl, int *clp, float *val,
+                   bool dist2Compatible = false) {
+        return race_simdify_d1(simdWidth, C, nrows, col, chunkStart, rl, clp, val, RACE_VAL_F32,
+                               dist2Compatible ? 1 : 0) == RACE_SUCCESS;
+    }
     void setStream(void *cudaStream) { race_set_stream(e_, cudaStream); }
     race_engine *handle() { return e_; }
 

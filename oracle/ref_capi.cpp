@@ -34,6 +34,7 @@
 #include "functionManager.h"
 #include "matrixPowerRecursive.h"
 #include "traverse.h"
+#include "interface.h"
 
 namespace {
 
@@ -457,6 +458,69 @@ int refc_power_coverage(void *vh, int power, int *cover) {
     FuncManager fm(f6, &args, power, 1, h->mp, false);
     fm.Run();
     return 0;
+}
+
+/* ---------------- simdify (interface.cpp:824-842) ---------------- */
+
+/* A RACE::Interface colored by RACEColor() (interface.cpp:260-301; its
+ * pinning step binds nothing with the hwloc stand-in), for simdify, whose
+ * padding pass runs a callback through the interface's own executor
+ * (sell_c_sigmize.cpp:48-62). The CRS arrays are copied and outlive the
+ * interface, which borrows them. */
+struct IfaceHandle {
+    RACE::Interface *ce = nullptr;
+    int n = 0;
+    std::vector<int> rowPtr, col;
+};
+
+void *refc_iface(int n, const int *rowPtr, const int *col, int dist, int nthreads, int symm_hint, int d2type,
+                 int lbtarget) {
+    Quiet q;
+    IfaceHandle *h = new IfaceHandle;
+    h->n = n;
+    h->rowPtr.assign(rowPtr, rowPtr + n + 1);
+    h->col.assign(col, col + rowPtr[n]);
+    h->ce = new RACE::Interface(n, nthreads, (RACE::dist)dist, h->rowPtr.data(), h->col.data(), symm_hint != 0, 1,
+                                RACE::SCATTER, NULL, NULL, (RACE::d2Method)d2type, (RACE::LBTarget)lbtarget);
+    if (h->ce->RACEColor() != RACE_SUCCESS) {
+        delete h->ce;
+        delete h;
+        return nullptr;
+    }
+    return h;
+}
+
+void refc_iface_free(void *vh) {
+    IfaceHandle *h = (IfaceHandle *)vh;
+    delete h->ce;
+    delete h;
+}
+
+void refc_iface_perm(void *vh, int *perm, int *invPerm) {
+    IfaceHandle *h = (IfaceHandle *)vh;
+    int *p = nullptr, *ip = nullptr, len = 0;
+    h->ce->getPerm(&p, &len);
+    h->ce->getInvPerm(&ip, &len);
+    memcpy(perm, p, sizeof(int) * h->n);
+    memcpy(invPerm, ip, sizeof(int) * h->n);
+    delete[] p;
+    delete[] ip;
+}
+
+/* Interface::simdify (double values); returns its bool. */
+int refc_simdify(void *vh, int simdWidth, int C, int nrows, int *col, int *chunkStart, int *rl, int *clp,
+                 double *val, int diagFirst) {
+    IfaceHandle *h = (IfaceHandle *)vh;
+    Quiet q;
+    return h->ce->simdify(simdWidth, C, nrows, col, chunkStart, rl, clp, val, diagFirst != 0) ? 1 : 0;
+}
+
+/* Interface::simdifyD1 (double values); returns its bool. */
+int refc_simdify_d1(void *vh, int simdWidth, int C, int nrows, int *col, int *chunkStart, int *rl, int *clp,
+                    double *val, int dist2Compatible) {
+    IfaceHandle *h = (IfaceHandle *)vh;
+    Quiet q;
+    return h->ce->simdifyD1(simdWidth, C, nrows, col, chunkStart, rl, clp, val, dist2Compatible != 0) ? 1 : 0;
 }
 
 } // extern "C"

@@ -51,6 +51,12 @@ def lib():
         L.refc_power_tree.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         L.refc_power_exec.argtypes = [C.c_void_p, C.c_int, C.c_int, IP, IP, DP, DP]
         L.refc_power_coverage.argtypes = [C.c_void_p, C.c_int, IP]
+        L.refc_iface.restype = C.c_void_p
+        L.refc_iface.argtypes = [C.c_int, IP, IP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.refc_iface_free.argtypes = [C.c_void_p]
+        L.refc_iface_perm.argtypes = [C.c_void_p, IP, IP]
+        L.refc_simdify.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, IP, IP, IP, IP, DP, C.c_int]
+        L.refc_simdify_d1.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, IP, IP, IP, IP, DP, C.c_int]
         _lib = L
     return _lib
 
@@ -90,6 +96,39 @@ def parse_power_tree(buf):
             nv = int(buf[k]); d[nm] = [int(v) for v in buf[k + 1:k + 1 + nv]]; k += 1 + nv
         leaves.append(d)
     return leaves
+
+
+class RefInterface:
+    """A colored RACE::Interface, for simdify/simdifyD1 (interface.cpp:824-842)."""
+
+    def __init__(self, csr, dist: int, nthreads: int, symm_hint: bool = True, d2type: int = 0, lbtarget: int = 1):
+        self.n = csr.n
+        self.h = lib().refc_iface(csr.n, _i32(csr.row_ptr), _i32(csr.col), dist, nthreads, int(symm_hint), d2type,
+                                  lbtarget)
+        if not self.h:
+            raise RuntimeError("RACEColor failed")
+
+    def close(self):
+        if self.h:
+            lib().refc_iface_free(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def perm(self):
+        p = np.zeros(self.n, np.int32); ip = np.zeros(self.n, np.int32)
+        lib().refc_iface_perm(self.h, p, ip)
+        return p, ip
+
+    def simdify(self, simd_width, C, sell, diag_first):
+        """Runs Interface::simdify on sell = (col, val, chunkStart, rl, clp) in place; returns its bool."""
+        col, val, cs, rl, clp = sell
+        return bool(lib().refc_simdify(self.h, simd_width, C, self.n, col, cs, rl, clp, val, int(diag_first)))
+
+    def simdify_d1(self, simd_width, C, sell, dist2_compatible):
+        col, val, cs, rl, clp = sell
+        return bool(lib().refc_simdify_d1(self.h, simd_width, C, self.n, col, cs, rl, clp, val,
+                                          int(dist2_compatible)))
 
 
 class RefColor:

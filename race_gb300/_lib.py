@@ -14,6 +14,7 @@ LIB_PATH = PKG / "_build" / "librace_gb300.so"
 
 RACE_SUCCESS = 0
 RACE_ERR_INVALID_ARG = 1
+RACE_ERR_INCOMPATIBILITY = 6
 ERRORS = {
     0: "RACE_SUCCESS", 1: "RACE_ERR_INVALID_ARG", 2: "RACE_ERR_MATRIX_SYMM", 3: "RACE_ERR_D2_COLOR",
     4: "RACE_ERR_D1_COLOR", 5: "RACE_ERR_GRAPH_TRAVERSAL", 6: "RACE_ERR_INCOMPATIBILITY", 7: "RACE_ERR_HWLOC",
@@ -33,6 +34,7 @@ EXPORTS = [
     "race_batch_graph_launch", "race_batch_get_status", "race_batch_info", "race_batch_last_error",
     "race_mlp_create", "race_mlp_destroy", "race_mlp_num_params", "race_mlp_set_params", "race_mlp_get_params",
     "race_mlp_forward", "race_mlp_loss_grad", "race_mlp_adam_step", "race_mlp_last_error", "race_wave_plan",
+    "race_simdify", "race_simdify_schedule", "race_simdify_d1", "race_get_highest_power",
 ]
 
 
@@ -91,6 +93,10 @@ def lib():
             "race_mlp_loss_grad": [vp, vp, vp, i, vp, vp, vp],
             "race_mlp_adam_step": [vp, C.c_float, C.c_float, C.c_float, C.c_float, vp],
             "race_wave_plan": [i, i, vp, vp, vp, vp, vp, i, vp, vp, i, ip, ip],
+            "race_simdify": [vp, i, i, i, vp, vp, vp, vp, vp, i, i, ip],
+            "race_get_highest_power": [vp, ip],
+            "race_simdify_schedule": [i, i, i, vp, vp, vp, vp, vp, i, i, vp, vp, i, ip],
+            "race_simdify_d1": [i, i, i, vp, vp, vp, vp, vp, i, i],
         }
         for name, args in sig.items():
             fn = getattr(L, name)

@@ -7,6 +7,7 @@
 #include <numeric>
 
 #include "engine.h"
+#include "simdify.h"
 
 namespace race {
 
@@ -507,6 +508,76 @@ int race_wave_plan(int kernel, int n, const int *rowPtr, const int *col, const i
             memcpy(wavePtr, wp.wavePtr.data(), sizeof(int) * wp.wavePtr.size());
             memcpy(rows, wp.rows.data(), sizeof(int) * wp.rows.size());
         }
+    });
+}
+
+namespace {
+race::SellArrays sellArrays(int simdWidth, int C, int nrows, int *col, const int *chunkStart, const int *rl,
+                            const int *clp, void *val, int valType) {
+    if (valType < RACE_VAL_F64 || valType > RACE_VAL_BF16) throw Error(RACE_ERR_INVALID_ARG, "simdify: bad val_type");
+    race::SellArrays m;
+    m.simdWidth = simdWidth;
+    m.C = C;
+    m.nrows = nrows;
+    m.col = col;
+    m.chunkStart = chunkStart;
+    m.rl = rl;
+    m.clp = clp;
+    m.val = static_cast<unsigned char *>(val);
+    m.valBytes = valType == RACE_VAL_F64 ? 8 : valType == RACE_VAL_F32 ? 4 : 2;
+    return m;
+}
+
+void throwSimdify(int st, const std::string &msg) {
+    if (st == race::SIMDIFY_BAD_ARG) throw Error(RACE_ERR_INVALID_ARG, msg);
+    if (st == race::SIMDIFY_UNPLACEABLE) throw Error(RACE_ERR_INCOMPATIBILITY, msg);
+}
+}  // namespace
+
+int race_get_highest_power(race_engine *e, int *power) {
+    if (!e || !power) return RACE_ERR_INVALID_ARG;
+    *power = e->eng->highestPower;
+    return RACE_SUCCESS;
+}
+
+int race_simdify(race_engine *e, int simdWidth, int C, int nrows, int *col, const int *chunkStart, const int *rl,
+                 const int *clp, void *val, int val_type, int diagFirst, int *collisions) {
+    if (!e) return RACE_ERR_INVALID_ARG;
+    return guard(e, [&] {
+        race::Engine &E = *e->eng;
+        if (!E.colored) throw Error(RACE_ERR_INVALID_ARG, "simdify needs a colored engine (race_color)");
+        if (nrows != E.n) throw Error(RACE_ERR_INVALID_ARG, "simdify: nrows must be the engine's row count");
+        race::SellArrays m = sellArrays(simdWidth, C, nrows, col, chunkStart, rl, clp, val, val_type);
+        std::string msg;
+        int coll = 0;
+        const int st = race::simdifyD2(m, E.phases[0].leafLo, E.phases[0].leafHi, diagFirst != 0, &coll, msg);
+        if (collisions) *collisions = coll;
+        throwSimdify(st, msg);
+    });
+}
+
+int race_simdify_schedule(int simdWidth, int C, int nrows, int *col, const int *chunkStart, const int *rl,
+                          const int *clp, void *val, int val_type, int diagFirst, const int *leafLo,
+                          const int *leafHi, int numLeaves, int *collisions) {
+    if (numLeaves < 0 || (numLeaves > 0 && (!leafLo || !leafHi))) return RACE_ERR_INVALID_ARG;
+    return guard(nullptr, [&] {
+        race::SellArrays m = sellArrays(simdWidth, C, nrows, col, chunkStart, rl, clp, val, val_type);
+        std::vector<int> lo(leafLo, leafLo + numLeaves), hi(leafHi, leafHi + numLeaves);
+        std::string msg;
+        int coll = 0;
+        const int st = race::simdifyD2(m, lo, hi, diagFirst != 0, &coll, msg);
+        if (collisions) *collisions = coll;
+        throwSimdify(st, msg);
+    });
+}
+
+int race_simdify_d1(int simdWidth, int C, int nrows, int *col, const int *chunkStart, const int *rl, const int *clp,
+                    void *val, int val_type, int dist2Compatible) {
+    (void)rl;
+    return guard(nullptr, [&] {
+        race::SellArrays m = sellArrays(simdWidth, C, nrows, col, chunkStart, rl, clp, val, val_type);
+        std::string msg;
+        throwSimdify(race::simdifyD1(m, dist2Compatible != 0, msg), msg);
     });
 }
 

@@ -40,6 +40,26 @@ def _host_i32(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.int32)
 
 
+_SELL_VAL_TYPE = {np.dtype(np.float64): VAL_F64, np.dtype(np.float32): VAL_F32, np.dtype(np.uint16): VAL_BF16}
+
+
+def _sell_args(col, chunkStart, rl, clp, val):
+    """C arguments of the simdify calls: col and val are rewritten in place,
+    so they must be writable C-contiguous host arrays (col int32; val
+    float64, float32, uint16 holding BF16 bits, or None)."""
+    for name, a in (("col", col), ("val", val)):
+        if a is not None and not (isinstance(a, np.ndarray) and a.flags.c_contiguous and a.flags.writeable):
+            raise TypeError(f"simdify: {name} must be a writable C-contiguous numpy array")
+    if col.dtype != np.int32:
+        raise TypeError("simdify: col must be int32")
+    if val is not None and val.dtype not in _SELL_VAL_TYPE:
+        raise TypeError("simdify: val must be float64, float32 or uint16 (BF16 bits)")
+    keep = [_host_i32(chunkStart), _host_i32(rl), _host_i32(clp)]
+    args = [col.ctypes.data] + [k.ctypes.data for k in keep] + \
+           [None if val is None else val.ctypes.data, VAL_F64 if val is None else _SELL_VAL_TYPE[val.dtype]]
+    return args, keep
+
+
 @dataclasses.dataclass
 class DeviceCsr:
     """A CRS matrix in device memory (torch tensors)."""
@@ -158,6 +178,34 @@ class Interface:
         v = C.c_int()
         self._check(lib().race_get_max_stage_depth(self._h, C.byref(v)))
         return v.value
+
+    def getHighestPower(self) -> int:
+        v = C.c_int()
+        self._check(lib().race_get_highest_power(self._h, C.byref(v)))
+        return v.value
+
+    # ---- SELL-C-sigma preparation (interface.h:179-185)
+    def simdify(self, simdWidth: int, C: int, nrows: int, col: np.ndarray, chunkStart, rl, clp,
+                val: Optional[np.ndarray], diagFirst: bool = False) -> bool:
+        """Interface::simdify: pads each row of each forward leaf, then orders
+        every SIMD group's entries so that its lanes hold different columns in
+        each slot. Host arrays in SELL-C layout, col/val rewritten in place.
+        False when a row cannot be placed (as the reference; the arrays are
+        then partly rearranged)."""
+        args, _keep = _sell_args(col, chunkStart, rl, clp, val)
+        rc = lib().race_simdify(self._h, int(simdWidth), int(C), int(nrows), *args, int(bool(diagFirst)), None)
+        if rc == _lib.RACE_ERR_INCOMPATIBILITY:
+            return False
+        self._check(rc)
+        return True
+
+    def simdifyD1(self, simdWidth: int, C: int, nrows: int, col: np.ndarray, chunkStart, rl, clp,
+                  val: Optional[np.ndarray], dist2Compatible: bool = False) -> bool:
+        """Interface::simdifyD1: moves each row's entries on the earlier rows
+        of its SIMD group to the row's last slots."""
+        args, _keep = _sell_args(col, chunkStart, rl, clp, val)
+        check(lib().race_simdify_d1(int(simdWidth), int(C), int(nrows), *args, int(bool(dist2Compatible))))
+        return True
 
     def getZoneTreeFlat(self) -> np.ndarray:
         n = C.c_int()

@@ -13,6 +13,15 @@ import numpy as np
 
 from race_gb300 import matgen
 
+def _arrow(n: int):
+    """Arrow matrix: row 0 full, every other row its diagonal and column 0."""
+    cols = [np.arange(n)] + [np.array([0, r]) for r in range(1, n)]
+    rp = np.concatenate([[0], np.cumsum([len(c) for c in cols])]).astype(np.int32)
+    col = np.concatenate(cols).astype(np.int32)
+    val = np.where(col == np.repeat(np.arange(n), np.diff(rp)), float(n), -1.0)
+    return matgen.Csr(n, rp, col, val, f"arrow_{n}")
+
+
 # name -> generator
 MATRICES = {
     "lap7_32": lambda: matgen.laplace3d_7pt(32),          # 32^3 7-point Laplacian (n=32,768)
@@ -29,6 +38,8 @@ MATRICES = {
     "islands_330": lambda: matgen.islands(0),
     # a single row
     "tiny_1": lambda: matgen.Csr(1, np.array([0, 1], np.int32), np.array([0], np.int32), np.array([3.0]), "tiny_1"),
+    # rows of two entries that share column 0: too few columns for wide SIMD groups
+    "arrow_64": lambda: _arrow(64),
 }
 
 # (matrix, dist, nthreads)
@@ -47,6 +58,62 @@ POWER_CASES = [
     ("st27_24", 8, 2e6), ("st27_40", 8, 8e6), ("lap7_32", 4, 1e6), ("aniso5_120x90", 4, 5e5),
     ("plaw_20k", 4, 1e6), ("band_5k", 6, 3e5), ("islands_330", 3, 2e4), ("tiny_1", 2, 1e4),
 ]
+
+# simdify cases on colored matrices (each golden entry stores its own
+# permutation and zone tree): (matrix, dist, nthreads, simdWidth, C, extra padded slots per chunk, flag, pass)
+# pass "d2": Interface::simdify, flag = diagFirst; pass "d1": simdifyD1,
+# flag = dist2Compatible. islands_330 with simdWidth 7 and tiny_1 have a
+# last SIMD group of one row; arrow_64 cannot be simdified for 4 lanes.
+SIMDIFY_CASES = [
+    ("lap7_16", 2, 16, 4, 8, 0, False, "d2"), ("lap7_16", 2, 16, 4, 8, 2, True, "d2"),
+    ("islands_330", 2, 16, 4, 4, 1, False, "d2"), ("band_5k", 2, 32, 8, 32, 0, True, "d2"),
+    ("aniso5_120x90", 2, 48, 32, 32, 0, False, "d2"), ("plaw_3k", 2, 16, 4, 8, 0, False, "d2"),
+    ("lap7_16", 2, 64, 8, 8, 0, False, "d2"),
+    ("aniso9_100x80", 1, 16, 4, 8, 0, False, "d1"), ("aniso9_100x80", 1, 16, 4, 8, 0, True, "d1"),
+    ("plaw_3k", 1, 32, 8, 32, 1, False, "d1"), ("lap7_16", 1, 8, 4, 4, 0, True, "d1"),
+    ("islands_330", 1, 8, 7, 14, 0, False, "d1"), ("tiny_1", 1, 4, 4, 4, 0, False, "d1"),
+    ("arrow_64", 2, 4, 4, 4, 0, False, "d2"), ("arrow_64", 1, 4, 4, 8, 0, False, "d1"),
+]
+
+
+def key_simdify(m, d, t, w, c, extra, flag, kind):
+    return f"simd__{kind}__{m}__d{d}__t{t}__w{w}__c{c}__e{extra}__f{int(flag)}"
+
+
+def sell_layout(csr, C, extra=0, diag_first=False):
+    """SELL-C-1 arrays of a CRS matrix in RACE simdify's layout (entry j of
+    row r at chunkStart[r // C] + r % C + j * C): col, val, chunkStart
+    (chunks + 1), rl, clp. Every chunk is `extra` slots longer than its
+    longest row; a row's padding points at the row itself, the padding rows
+    of the last chunk at column 0. val numbers the slots (0, 1, ...) so that
+    a rearranged val records where each entry came from. diag_first moves
+    each row's diagonal entry to slot 0."""
+    n = csr.n
+    rp = np.asarray(csr.row_ptr, np.int64)
+    rl = np.diff(rp).astype(np.int32)
+    nch = (n + C - 1) // C
+    padded = np.zeros(nch * C, np.int32)
+    padded[:n] = rl
+    clp = (padded.reshape(nch, C).max(axis=1) + extra).astype(np.int32)
+    cs = np.zeros(nch + 1, np.int64)
+    cs[1:] = np.cumsum(clp.astype(np.int64) * C)
+    col = np.zeros(int(cs[-1]), np.int32)
+    for c in range(nch):
+        own = np.arange(c * C, c * C + C)
+        col[cs[c]:cs[c + 1]] = np.tile(np.where(own < n, own, 0), clp[c])
+    src = np.asarray(csr.col, np.int32).copy()
+    if diag_first:
+        for r in range(n):
+            seg = src[rp[r]:rp[r + 1]]
+            d = np.flatnonzero(seg == r)
+            if d.size:
+                seg[[0, d[0]]] = seg[[d[0], 0]]
+    rows = np.repeat(np.arange(n), rl)
+    slot = np.arange(rp[-1]) - rp[rows]
+    col[cs[rows // C] + rows % C + slot * C] = src
+    val = np.arange(col.size, dtype=np.float64)
+    return col, val, cs.astype(np.int32), rl, clp
+
 
 # (matrix, dist) traversals of the whole range
 TRAVERSE_CASES = [(m, d) for m in ["lap7_16", "st27_16", "plaw_3k", "band_5k", "aniso9_100x80", "islands_330"] for d in (1, 2, 3)]

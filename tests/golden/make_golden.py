@@ -25,9 +25,10 @@ sys.path.insert(0, str(ROOT / "tests"))
 os.environ.setdefault("ORACLE_QUIET", "1")
 os.environ.setdefault("OMP_NUM_THREADS", "8")
 
-from cases import (COLOR_CASES, EXEC_CASES, MATRICES, POWER_CASES, TRAVERSE_CASES, arr_digest, digest, key_color,  # noqa: E402
-                   key_power, key_trav)
+from cases import (COLOR_CASES, EXEC_CASES, MATRICES, POWER_CASES, SIMDIFY_CASES, TRAVERSE_CASES, arr_digest,  # noqa: E402
+                   digest, key_color, key_power, key_simdify, key_trav, sell_layout)
 from oracle import refpy  # noqa: E402
+from oracle.refpy import RefInterface  # noqa: E402
 from race_gb300 import matgen  # noqa: E402
 
 OUT = pathlib.Path(__file__).resolve().parent / "golden.npz"
@@ -102,6 +103,29 @@ def main():
                 g[k + f"__out_{name}"] = b if kern in (0, 2) else x
         rc.close()
         print(k, "threads", int(g[k + "__threads"]), "eff %.3f" % float(g[k + "__eff"]))
+
+    # simdify / simdifyD1 through a colored RACE::Interface, on the matrix
+    # in the interface's own permutation (checked equal to the coloring's,
+    # whose zone tree gives the test its schedule)
+    for m, d, t, w, cl, extra, flag, kind in SIMDIFY_CASES:
+        A = M(m)
+        rc = refpy.RefColor(A, d, t)
+        p, ip = rc.perm()
+        tree = rc.tree_flat()
+        rc.close()
+        ri = RefInterface(A, d, t)
+        assert np.array_equal(ri.perm()[0], p), "interface and coloring permutations differ"
+        sell = sell_layout(A.permuted(p, ip), cl, extra, diag_first=(kind == "d2" and flag))
+        ok = ri.simdify(w, cl, sell, flag) if kind == "d2" else ri.simdify_d1(w, cl, sell, flag)
+        ri.close()
+        k = key_simdify(m, d, t, w, cl, extra, flag, kind)
+        g[k + "__digest"] = np.array(digest(A))
+        g[k + "__perm"] = p
+        g[k + "__tree"] = tree
+        g[k + "__ok"] = np.array(int(ok))
+        g[k + "__col"] = sell[0]
+        g[k + "__src"] = sell[1].astype(np.int32)
+        print(k, "ok" if ok else "cannot simdify")
 
     for m, p, c in POWER_CASES:
         A = M(m)

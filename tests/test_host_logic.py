@@ -137,7 +137,12 @@ int use(int n, int *rp, int *col, race_operands ops) {
     RACE::gb300::Batch b;
     b.add(ce, g);
     b.graphLaunch();
-    return rc + f + ce.executeFunctionAsync(f) + ce.getStatus() + b.getStatus() + ce.getNumThreads();
+    int scol[8] = {0}, cs[2] = {0, 8}, rl[4] = {2, 2, 2, 2}, clp[1] = {2};
+    double sval[8] = {0};
+    float fval[8] = {0};
+    bool ok = ce.simdify(4, 4, 4, scol, cs, rl, clp, sval, true) && ce.simdifyD1(4, 4, 4, scol, cs, rl, clp, fval);
+    return rc + f + ce.executeFunctionAsync(f) + ce.getStatus() + b.getStatus() + ce.getNumThreads() +
+           ce.getHighestPower() + (ok ? 1 : 0);
 }
 """)
     root = pathlib.Path(__file__).resolve().parents[1]
