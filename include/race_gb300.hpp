@@ -4,6 +4,8 @@
 // codes follow the reference; the callback is a built-in device kernel with
 // device operands instead of a host function pointer.
 #pragma once
+#include <cstdio>
+#include <cstdlib>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -25,6 +27,24 @@ enum Kernel {
     KACZ = RACE_K_KACZ,
     MPK = RACE_K_MPK
 };
+
+// Prints a zone tree in race_get_zone_tree's flat form ([numNodes], then per
+// node [nthreadsZ, idealNthreadsZ, totalSubBlocks, parentZ, effRowZ, stage,
+// reachedLimit, nValueZ, valueZ..., nChildren, children...]).
+inline void printZoneTreeFlat(const std::vector<int> &t) {
+    size_t k = 1;
+    for (int i = 0; i < t[0]; ++i) {
+        const int nth = t[k], ideal = t[k + 1], sub = t[k + 2], parent = t[k + 3], eff = t[k + 4], stage = t[k + 5],
+                  reached = t[k + 6];
+        k += 7;
+        printf("%d. Range:[", i);
+        for (int j = 0, nv = t[k++]; j < nv; ++j) printf("%d, ", t[k++]);
+        printf("] Children:[");
+        for (int j = 0, nc = t[k++]; j < nc; ++j) printf("%d, ", t[k++]);
+        printf("], Parent: %d, nthreads: %d, idealNThreads:%d, stage:%d, subBLocks:%d, effRow: %d, reachedLimit: %s\n",
+               parent, nth, ideal, stage, sub, eff, reached ? "true" : "false");
+    }
+}
 
 class Interface {
   public:
@@ -81,6 +101,17 @@ class Interface {
         race_get_max_stage_depth(e_, &v);
         return v;
     }
+    // printZoneTree (interface.cpp:328-331, zone_tree.cpp:307-339): one line
+    // per zone-tree node with its row ranges, children, parent, thread counts,
+    // stage, sub-blocks, effective rows and limit flag (no pinning or timing
+    // fields: they have no GPU meaning).
+    void printZoneTree() {
+        int len = 0;
+        if (race_get_zone_tree(e_, nullptr, 0, &len) != RACE_SUCCESS) return;
+        std::vector<int> t(len);
+        race_get_zone_tree(e_, t.data(), len, &len);
+        printZoneTreeFlat(t);
+    }
 
     // registerFunction with a device kernel (interface.h:149-157); returns the
     // function id, or the error code as the reference does.
@@ -136,6 +167,36 @@ class Interface {
         return race_simdify_d1(simdWidth, C, nrows, col, chunkStart, rl, clp, val, RACE_VAL_F32,
                                dist2Compatible ? 1 : 0) == RACE_SUCCESS;
     }
+    // getNumaSplitting (interface.cpp:1042-1053): the row split of the
+    // level groups over shared-cache domains, malloc()ed as in the
+    // reference. The reference always uses one domain (interface.cpp:207),
+    // so the split is {0, nrow}.
+    void getNumaSplitting(int **split, int *splitLen) {
+        *split = (int *)malloc(2 * sizeof(int));
+        (*split)[0] = 0;
+        (*split)[1] = nrow_;
+        *splitLen = 2;
+    }
+
+    // CPU thread and memory placement (interface.h:139, 172-177, 188-198):
+    // the GPU engine has no host threads to pin, put to sleep or run
+    // serially and no NUMA first touch, and its results do not depend on a
+    // thread count. Kept so that callers of the reference compile; they do
+    // nothing.
+    void sleep() {}
+    void pinThread(int threadId) { (void)threadId; }
+    void setSerial(int funcId) { (void)funcId; }
+    void unsetSerial(int funcId) { (void)funcId; }
+    void resetTime() {}
+    void numaInitRowPtr(int *rowPtr) { (void)rowPtr; }
+    void numaInitRowPtr(int **rowPtr) { (void)rowPtr; }
+    void numaInitMtxVec(int *rowPtr, int *col, double *val, double *x, int power = 1) {
+        (void)rowPtr, (void)col, (void)val, (void)x, (void)power;
+    }
+    void numaInitMtxVec(int **rowPtr, int **col, double **val, int power = 1) {
+        (void)rowPtr, (void)col, (void)val, (void)power;
+    }
+
     void setStream(void *cudaStream) { race_set_stream(e_, cudaStream); }
     race_engine *handle() { return e_; }
 

@@ -40,6 +40,28 @@ def _host_i32(a) -> np.ndarray:
     return np.ascontiguousarray(a, dtype=np.int32)
 
 
+def format_zone_tree(flat) -> str:
+    """printZoneTree's text (interface.cpp:328-331, zone_tree.cpp:307-339)
+    for a zone tree in race_get_zone_tree's flat form, one line per node;
+    the reference's pinning and timing fields have no GPU meaning and are
+    left out."""
+    t = [int(v) for v in flat]
+    lines, k = [], 1
+    for i in range(t[0]):
+        nth, ideal, sub, parent, eff, stage, reached = t[k:k + 7]
+        k += 7
+        nv = t[k]
+        rng = t[k + 1:k + 1 + nv]
+        k += 1 + nv
+        nc = t[k]
+        ch = t[k + 1:k + 1 + nc]
+        k += 1 + nc
+        lines.append(f"{i}. Range:[{''.join(f'{v}, ' for v in rng)}] Children:[{''.join(f'{c}, ' for c in ch)}], "
+                     f"Parent: {parent}, nthreads: {nth}, idealNThreads:{ideal}, stage:{stage}, subBLocks:{sub}, "
+                     f"effRow: {eff}, reachedLimit: {'true' if reached else 'false'}")
+    return "\n".join(lines) + ("\n" if lines else "")
+
+
 _SELL_VAL_TYPE = {np.dtype(np.float64): VAL_F64, np.dtype(np.float32): VAL_F32, np.dtype(np.uint16): VAL_BF16}
 
 
@@ -206,6 +228,14 @@ class Interface:
         args, _keep = _sell_args(col, chunkStart, rl, clp, val)
         check(lib().race_simdify_d1(int(simdWidth), int(C), int(nrows), *args, int(bool(dist2Compatible))))
         return True
+
+    def printZoneTree(self):
+        print(format_zone_tree(self.getZoneTreeFlat()), end="")
+
+    def getNumaSplitting(self) -> np.ndarray:
+        """Row split of the level groups over shared-cache domains; the
+        reference always uses one domain (interface.cpp:207, 1042-1053)."""
+        return np.array([0, self.nrow], np.int32)
 
     def getZoneTreeFlat(self) -> np.ndarray:
         n = C.c_int()

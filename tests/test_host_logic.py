@@ -141,6 +141,13 @@ int use(int n, int *rp, int *col, race_operands ops) {
     double sval[8] = {0};
     float fval[8] = {0};
     bool ok = ce.simdify(4, 4, 4, scol, cs, rl, clp, sval, true) && ce.simdifyD1(4, 4, 4, scol, cs, rl, clp, fval);
+    int *split = nullptr, splitLen = 0;
+    ce.getNumaSplitting(&split, &splitLen);
+    free(split);
+    ce.printZoneTree();
+    ce.setSerial(f);
+    ce.unsetSerial(f);
+    ce.numaInitMtxVec(rp, col, nullptr, nullptr, 4);
     return rc + f + ce.executeFunctionAsync(f) + ce.getStatus() + b.getStatus() + ce.getNumThreads() +
            ce.getHighestPower() + (ok ? 1 : 0);
 }
@@ -220,3 +227,39 @@ def test_wave_plan_rejects_bad_phase_tables():
     assert call(orc.K_GS, [1, 1], [0], [2]) == bad      # phase table not from 0
     assert call(orc.K_GS, [0, 1, 0], [0], [2]) == bad   # phases not monotonic
     assert call(5, [0, 1], [0], [2]) == bad             # MPK has no wave plan
+
+
+def test_print_zone_tree_cpp_and_python_agree(golden, tmp_path):
+    """printZoneTree of the C++ wrapper and of the Python mirror print the
+    same lines for the reference's zone trees (one line per node, ranges
+    and children as stored)."""
+    import shutil
+    import subprocess
+    from race_gb300.interface import format_zone_tree
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    src = tmp_path / "pz.cpp"
+    src.write_text("""
+#include <iostream>
+#include "race_gb300.hpp"
+int main() {
+    std::vector<int> t;
+    int v;
+    while (std::cin >> v) t.push_back(v);
+    RACE::gb300::printZoneTreeFlat(t);
+    return 0;
+}
+""")
+    root = pathlib.Path(__file__).resolve().parents[1]
+    exe = tmp_path / "pz"
+    r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", str(root / "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for key in ("color__lap7_16__d2__t16__tree", "color__islands_330__d1__t8__tree", "color__tiny_1__d1__t4__tree"):
+        tree = golden[key]
+        out = subprocess.run([str(exe)], input=" ".join(map(str, tree)), capture_output=True, text=True).stdout
+        py = format_zone_tree(tree)
+        assert out == py
+        assert len(py.splitlines()) == int(tree[0])
+        assert py.startswith("0. Range:[")
