@@ -88,6 +88,7 @@ typedef struct {
     int n_lvl_threads;
     int lvl_threads[16];
     int cache_violation_cutoff;
+    int max_recursion_stages; /* -1: the reference's default; 0: MPK partition without recursion */
 } race_params;
 
 int race_params_from_env(race_params *p);

@@ -371,17 +371,20 @@ static double orc_byte_per_nnz(int p, int nrow, long long nnz) {
  * dangerRow per group (rows before unlockRow are what the previous group's
  * next power needs; rows from dangerRow on need the next group).
  * levelPtr has totalLevel+1 row offsets starting at lo. Outputs have room
- * for totalLevel+1 entries. Returns the number of groups, or -1 when some
- * level is hopeless (its budget exceeds the cache by more than cutoff). */
+ * for totalLevel+1 entries. Returns the number of groups, or -1 when the
+ * stage has a hopeless region: two consecutive levels whose budgets exceed
+ * the cache by more than cutoff (identifyHopelessRegions,
+ * matrixPower.cpp:147-210; an isolated such level is grouped normally). */
 int orc_mpk_groups(int p, int nrow, long long nnz, double cacheSize, double safety, int cutoff, int totalLevel,
                    const int *levelPtr, const int *levelNnz, int *groupPtr, int *unlockRow, int *dangerRow) {
     double bpn = orc_byte_per_nnz(p, nrow, nnz);
     double cacheElem = cacheSize / bpn;
+    int prevViolated = -2;
     for (int l = 0; l < totalLevel; ++l) {
         double e = safety * (p + 1) * levelNnz[l];
-        if (e > cacheElem) {
-            int factor = (int)ceil(e / cacheElem);
-            if (factor > cutoff) return -1;
+        if (e > cacheElem && (int)ceil(e / cacheElem) > cutoff) {
+            if (l == prevViolated + 1) return -1;
+            prevViolated = l;
         }
     }
     int ng = 0;

@@ -46,7 +46,8 @@ class RaceError(RuntimeError):
 
 class race_params(C.Structure):
     _fields_ = [("n_eff", C.c_int), ("eff", C.c_double * 16), ("n_lvl_threads", C.c_int),
-                ("lvl_threads", C.c_int * 16), ("cache_violation_cutoff", C.c_int)]
+                ("lvl_threads", C.c_int * 16), ("cache_violation_cutoff", C.c_int),
+                ("max_recursion_stages", C.c_int)]
 
 
 class race_operands(C.Structure):

@@ -79,15 +79,23 @@ void Engine::powerPrepare(int hp, double cacheSize, double safety, const std::st
     else
         cutoff = (0 < (int)params.cacheViolationCutoff.size() - 1) ? params.cacheViolationCutoff[1]
                                                                     : params.cacheViolationCutoff[0];
-    int violated = 0;
-    for (int l = 0; l < L; ++l) {
+    // Levels over the cut-off form a hopeless region only where two of them
+    // are consecutive (identifyHopelessRegions, matrixPower.cpp:147-210);
+    // isolated ones are grouped like any other level.
+    bool hopeless = false;
+    for (int l = 0, prev = -2; l < L; ++l) {
         double e = safety * (P + 1) * ld.levelNnz[l];
-        if (e > cacheElem && static_cast<int>(std::ceil(e / cacheElem)) > cutoff) ++violated;
+        if (e > cacheElem && static_cast<int>(std::ceil(e / cacheElem)) > cutoff) {
+            hopeless = hopeless || l == prev + 1;
+            prev = l;
+        }
     }
-    if (violated > 1 && mtxType == "N")
+    if (hopeless && mtxType == "N")
         throw Error(RACE_ERR_NOT_IMPLEMENTED,
-                    "levels exceed the cache budget beyond the cut-off (hopeless regions); recursive MPK "
-                    "partitioning is not built: raise cacheSize or RACE_CACHE_VIOLATION_CUTOFF");
+                    "consecutive levels exceed the cache budget beyond the cut-off (a hopeless region); recursive "
+                    "MPK partitioning is not built: raise cacheSize or RACE_CACHE_VIOLATION_CUTOFF, or set "
+                    "RACE_MAX_RECURSION_STAGES=0 (race_params.max_recursion_stages) to partition without "
+                    "recursion as the reference then does");
     // consolidatePartition without hopeless regions (matrixPower.cpp:685-883)
     groupPtr.assign(1, levelPtr[0]);
     unlockRow.assign(1, L > 0 ? levelPtr[std::min(1, L)] : 0);
@@ -213,6 +221,7 @@ race::Params toParams(const race_params *p) {
     q.lvlThreads.assign(p->lvl_threads, p->lvl_threads + std::max(0, std::min(p->n_lvl_threads, 16)));
     q.cacheViolationCutoffDefault = p->cache_violation_cutoff > 0 ? p->cache_violation_cutoff : 50;
     q.cacheViolationCutoff.assign(1, q.cacheViolationCutoffDefault);
+    q.maxRecStages = p->max_recursion_stages >= 0 ? p->max_recursion_stages : -1;
     return q;
 }
 }  // namespace
@@ -228,6 +237,7 @@ int race_params_from_env(race_params *p) {
     p->n_lvl_threads = (int)std::min<size_t>(q.lvlThreads.size(), 16);
     for (int i = 0; i < p->n_lvl_threads; ++i) p->lvl_threads[i] = q.lvlThreads[i];
     p->cache_violation_cutoff = q.cacheViolationCutoffDefault;
+    p->max_recursion_stages = q.maxRecStages;
     return RACE_SUCCESS;
 }
 

@@ -145,6 +145,8 @@ class Interface:
                     cparams.lvl_threads[i] = v
             if "cache_violation_cutoff" in params:
                 cparams.cache_violation_cutoff = int(params["cache_violation_cutoff"])
+            if "max_recursion_stages" in params:
+                cparams.max_recursion_stages = int(params["max_recursion_stages"])
         h = C.c_void_p()
         check(lib().race_create(C.byref(h), self.nrow, int(nthreads), int(dist), rp.ctypes.data, cl.ctypes.data,
                                 int(bool(symm_hint)), None if ip is None else ip.ctypes.data,

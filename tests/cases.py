@@ -57,7 +57,16 @@ EXEC_CASES = {("lap7_16", 2, 16), ("aniso9_100x80", 1, 16), ("plaw_3k", 1, 32), 
 POWER_CASES = [
     ("st27_24", 8, 2e6), ("st27_40", 8, 8e6), ("lap7_32", 4, 1e6), ("aniso5_120x90", 4, 5e5),
     ("plaw_20k", 4, 1e6), ("band_5k", 6, 3e5), ("islands_330", 3, 2e4), ("tiny_1", 2, 1e4),
+    # levels over the cache cut-off, none of them consecutive: no hopeless
+    # region, so the reference partitions without recursion
+    ("band_5k", 8, 3300), ("band_5k", 6, 2500),
 ]
+
+# (matrix, power, cacheBytes) with consecutive levels over the cut-off: the
+# reference recurses into the hopeless region by default; with
+# RACE_MAX_RECURSION_STAGES=0 it partitions without recursion, as the engine
+# does with max_recursion_stages = 0
+POWER_FLAT_CASES = [("plaw_20k", 4, 1e4), ("lap7_32", 4, 1e4)]
 
 # simdify cases on colored matrices (each golden entry stores its own
 # permutation and zone tree): (matrix, dist, nthreads, simdWidth, C, extra padded slots per chunk, flag, pass)
@@ -136,6 +145,10 @@ def key_color(m, d, t):
 
 def key_power(m, p, c):
     return f"power__{m}__p{p}__c{int(c)}"
+
+
+def key_power_flat(m, p, c):
+    return f"powerflat__{m}__p{p}__c{int(c)}"
 
 
 def key_trav(m, d):

@@ -25,8 +25,9 @@ sys.path.insert(0, str(ROOT / "tests"))
 os.environ.setdefault("ORACLE_QUIET", "1")
 os.environ.setdefault("OMP_NUM_THREADS", "8")
 
-from cases import (COLOR_CASES, EXEC_CASES, MATRICES, POWER_CASES, SIMDIFY_CASES, TRAVERSE_CASES, arr_digest,  # noqa: E402
-                   digest, key_color, key_power, key_simdify, key_trav, sell_layout)
+from cases import (COLOR_CASES, EXEC_CASES, MATRICES, POWER_CASES, POWER_FLAT_CASES, SIMDIFY_CASES,  # noqa: E402
+                   TRAVERSE_CASES, arr_digest, digest, key_color, key_power, key_power_flat, key_simdify, key_trav,
+                   sell_layout)
 from oracle import refpy  # noqa: E402
 from oracle.refpy import RefInterface  # noqa: E402
 from race_gb300 import matgen  # noqa: E402
@@ -146,6 +147,29 @@ def main():
             g[k + "__out"] = rp.execute(P, x0)[1:]
         rp.close()
         print(k, "groups", len(tr[0]["lp"]) - 1, "leaves", len(tr))
+
+    # hopeless regions: the reference's default recursion (leaf count only)
+    # and its partition with RACE_MAX_RECURSION_STAGES=0
+    for m, p, c in POWER_FLAT_CASES:
+        A = M(m)
+        k = key_power_flat(m, p, c)
+        rp = refpy.RefPower(A, p, c)
+        g[k + "__default_leaves"] = np.array(len(rp.tree()))
+        rp.close()
+        os.environ["RACE_MAX_RECURSION_STAGES"] = "0"
+        try:
+            rp = refpy.RefPower(A, p, c)
+            perm, ip = rp.perm()
+            tr = rp.tree()
+            assert (rp.coverage() == 1).all()
+            rp.close()
+        finally:
+            del os.environ["RACE_MAX_RECURSION_STAGES"]
+        g[k + "__digest"] = np.array(digest(A))
+        g[k + "__perm"] = perm
+        g[k + "__lp"] = np.array(tr[0]["lp"], np.int32)
+        g[k + "__leaves"] = np.array(len(tr))
+        print(k, "default leaves", int(g[k + "__default_leaves"]), "flat groups", len(tr[0]["lp"]) - 1)
 
     # full-size MPK configuration: digests only
     A = matgen.stencil3d_27pt(128)

@@ -3,7 +3,7 @@ fixtures), numerics against the C oracle. Needs a GB300."""
 import numpy as np
 import pytest
 
-from cases import COLOR_CASES, POWER_CASES, arr_digest, digest, key_color, key_power
+from cases import COLOR_CASES, POWER_CASES, POWER_FLAT_CASES, arr_digest, digest, key_color, key_power, key_power_flat
 from oracle import oracle as orc
 from oracle.refpy import parse_zone_tree
 from race_gb300 import matgen
@@ -43,6 +43,26 @@ def test_power_partition_matches_reference(golden, mats, m, p, c):
     assert rc.RACEColor(p, c) == 0
     np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
     np.testing.assert_array_equal(rc.getPowerGroups(), golden[k + "__lp"])
+
+
+@pytest.mark.parametrize("m,p,c", POWER_FLAT_CASES)
+def test_power_partition_without_recursion(golden, mats, m, p, c):
+    """Consecutive levels over the cache cut-off: the reference recurses into
+    the hopeless region by default, which is not built here (RACEColor
+    returns RACE_ERR_NOT_IMPLEMENTED); with max_recursion_stages = 0 both
+    partition without recursion, and the permutation, the level groups and
+    the MPK agree."""
+    A = mats[m]
+    k = key_power_flat(m, p, c)
+    assert str(golden[k + "__digest"]) == digest(A)
+    assert int(golden[k + "__default_leaves"]) > 1 and int(golden[k + "__leaves"]) == 1
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, c) == 10  # RACE_ERR_NOT_IMPLEMENTED
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True, params={"max_recursion_stages": 0})
+    assert rc.RACEColor(p, c) == 0
+    np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
+    np.testing.assert_array_equal(rc.getPowerGroups(), golden[k + "__lp"])
+    _check_mpk(rc, A, p)
 
 
 def _upload(P, dtype=torch.float64):
@@ -244,6 +264,10 @@ def test_mpk_fp64_bit_exact(golden, mats, m, p, c):
     A = mats[m]
     rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
     assert rc.RACEColor(p, c) == 0
+    _check_mpk(rc, A, p)
+
+
+def _check_mpk(rc, A, p):
     perm, inv = rc.getPerm(), rc.getInvPerm()
     P = A.permuted(perm, inv)
     x0 = matgen.uniform_vector(A.n, 0)

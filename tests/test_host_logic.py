@@ -263,3 +263,16 @@ int main() {
         assert out == py
         assert len(py.splitlines()) == int(tree[0])
         assert py.startswith("0. Range:[")
+
+
+def test_params_from_env_reads_recursion_stages(monkeypatch):
+    """race_params_from_env reads RACE_MAX_RECURSION_STAGES like the
+    reference (matrixPowerRecursive.cpp:50-60): -1 when unset."""
+    L = _lib.lib()
+    p = _lib.race_params()
+    monkeypatch.delenv("RACE_MAX_RECURSION_STAGES", raising=False)
+    _lib.check(L.race_params_from_env(C.byref(p)))
+    assert p.max_recursion_stages == -1 and p.cache_violation_cutoff == 50 and p.n_eff == 1 and p.eff[0] == 40.0
+    monkeypatch.setenv("RACE_MAX_RECURSION_STAGES", "0")
+    _lib.check(L.race_params_from_env(C.byref(p)))
+    assert p.max_recursion_stages == 0

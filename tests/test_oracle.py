@@ -3,7 +3,8 @@
 import numpy as np
 import pytest
 
-from cases import EXEC_CASES, POWER_CASES, TRAVERSE_CASES, digest, key_color, key_power, key_trav
+from cases import (EXEC_CASES, POWER_CASES, POWER_FLAT_CASES, TRAVERSE_CASES, digest, key_color, key_power,
+                   key_power_flat, key_trav)
 from oracle import oracle as orc
 from race_gb300 import matgen
 
@@ -61,6 +62,22 @@ def test_mpk_partition_matches_reference(golden, mats, m, p, c):
     lp = np.concatenate([[0], np.cumsum(lr)]).astype(np.int32)
     g = orc.mpk_groups(p, A.n, A.nnz, c, 2.0, 50, lp, ln)
     assert g is not None
+    np.testing.assert_array_equal(g[0], golden[k + "__lp"])
+
+
+@pytest.mark.parametrize("m,p,c", POWER_FLAT_CASES)
+def test_mpk_flat_partition_matches_reference(golden, mats, m, p, c):
+    """A hopeless region (consecutive levels over the cut-off) makes the
+    single-stage grouping refuse; without recursion (cut-off disabled, as
+    RACE_MAX_RECURSION_STAGES=0 does) it equals the reference's groups."""
+    A = mats[m]
+    k = key_power_flat(m, p, c)
+    assert str(golden[k + "__digest"]) == digest(A)
+    perm, inv, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+    np.testing.assert_array_equal(perm, golden[k + "__perm"])
+    lp = np.concatenate([[0], np.cumsum(lr)]).astype(np.int32)
+    assert orc.mpk_groups(p, A.n, A.nnz, c, 2.0, 50, lp, ln) is None
+    g = orc.mpk_groups(p, A.n, A.nnz, c, 2.0, 2**31 - 1, lp, ln)
     np.testing.assert_array_equal(g[0], golden[k + "__lp"])
 
 
