@@ -47,6 +47,8 @@ CACHE_BYTES = 300e6
 # reference's perf data: AMD Rome 49.85 GF/s = 317.9 GB/s effective
 # (examples/matrixPower_perf_test/21_Jan_2021_rome1_nps1/mtxPower.csv:2131).
 PUBLISHED_GBS = 317.9
+# GB300's nominal FP64 (non-tensor) rate, 1/64 of FP32
+FP64_PEAK_TFLOPS = 1.25
 
 
 def spmv_bytes(n: int, nnz: int, val_bytes: int = 8) -> int:
@@ -442,7 +444,12 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "note": f"achieved = compulsory bytes ({compulsory}) per launch / launch time; "
-                                 f"peak {peak_kind}"},
+                                 f"peak {peak_kind}",
+                         # one FP64 fma per non-zero and power: the FP64 pipe bounds this kernel too
+                         "fp64_pipe": {"achieved_tflops": 2 * nnz * POWER / (ms64 * 1e-3) / 1e12,
+                                       "peak_tflops": FP64_PEAK_TFLOPS,
+                                       "frac": 2 * nnz * POWER / (ms64 * 1e-3) / 1e12 / FP64_PEAK_TFLOPS,
+                                       "peak_kind": "nominal GB300 FP64"}},
             "cpu_baseline": cpu,
             "clocks": clocks,
             "fp64_bit_exact_vs_plain_chain": exact,
