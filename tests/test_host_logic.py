@@ -276,3 +276,63 @@ def test_params_from_env_reads_recursion_stages(monkeypatch):
     monkeypatch.setenv("RACE_MAX_RECURSION_STAGES", "0")
     _lib.check(L.race_params_from_env(C.byref(p)))
     assert p.max_recursion_stages == 0
+
+
+def _conflicts(P, pp, lo, hi, dist):
+    """Rows of different leaves of one phase that are neighbours (dist 1) or
+    share a neighbour (dist 2) in the symmetrised pattern of P; RACE's
+    coloring guarantee, which the reference checks with
+    Interface::detectConflict (interface.cpp:655-815)."""
+    import scipy.sparse as sp
+    n = P.n
+    phase = np.full(n, -1, np.int64)
+    leaf = np.full(n, -1, np.int64)
+    for p in range(len(pp) - 1):
+        for l in range(pp[p], pp[p + 1]):
+            a, b = int(lo[l]), int(hi[l])
+            rows = np.arange(a, b) if a <= b else np.arange(b + 1, a + 1)
+            phase[rows], leaf[rows] = p, l
+    assert (phase >= 0).all()
+    S = sp.csr_matrix((np.ones(P.nnz), P.col, P.row_ptr), shape=(n, n))
+    S = ((S + S.T + sp.identity(n, format="csr")) > 0).tocoo()
+    i, j = S.row.astype(np.int64), S.col.astype(np.int64)
+    if dist == 1:
+        return int(((phase[i] == phase[j]) & (leaf[i] != leaf[j])).sum())
+    # distance 2: every row k sees the rows of {k} + N(k); per (phase, k)
+    # they must all lie in one leaf
+    key = phase[j] * n + i
+    order = np.lexsort((leaf[j], key))
+    k2, l2 = key[order], leaf[j][order]
+    return int(((k2[1:] == k2[:-1]) & (l2[1:] != l2[:-1])).sum())
+
+
+@pytest.mark.parametrize("m,d,t", COLOR_CASES)
+def test_phases_are_conflict_free(golden, mats, m, d, t):
+    """Leaves that run concurrently (one phase of the flattened zone tree)
+    never touch the same row's neighbourhood: no distance-1 neighbours for
+    D1 coloring, no shared neighbour for D2, in both sweep directions."""
+    A = mats[m]
+    k = key_color(m, d, t)
+    perm = golden[k + "__perm"]
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(A.n, dtype=np.int32)
+    P = A.permuted(perm, inv)
+    for rev in (False, True):
+        pp, lo, hi = _flatten(golden[k + "__tree"], d, rev, A.n)
+        assert _conflicts(P, pp, lo, hi, d) == 0
+
+
+def test_conflict_check_detects_a_bad_phase(golden, mats):
+    """The checker itself: merging two consecutive phases of a D2 schedule
+    (red and black blocks together) creates conflicts."""
+    A = mats["lap7_16"]
+    k = key_color("lap7_16", 2, 16)
+    perm = golden[k + "__perm"]
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(A.n, dtype=np.int32)
+    P = A.permuted(perm, inv)
+    pp, lo, hi = _flatten(golden[k + "__tree"], 2, False, A.n)
+    assert len(pp) > 2
+    merged = np.concatenate([[0], pp[2:]])  # phases 0 and 1 run together
+    assert _conflicts(P, merged, lo, hi, 2) > 0
+    assert _conflicts(P, pp, lo, hi, 2) == 0
