@@ -1,0 +1,173 @@
+// race_gb300_device.cuh -- header-only CUDA counterpart of RACE's callback
+// registration. The reference calls a host function on row ranges of its
+// schedule: f(start, end, args) for colored kernels and
+// f(start, end, pow, numa, args) for the matrix power (registerFunction,
+// include/interface.h:143-157; FuncManager::Run, src/functionManager.cpp).
+// Here the function is a __device__ functor (its members play the role of
+// `args`, holding device pointers) and the engine's schedule calls it on the
+// GPU:
+//
+//   struct MyGs {
+//       const int *rowPtr, *col; const double *val, *b; double *x;
+//       __device__ void operator()(int start, int end) const {...}
+//   };
+//   RACE::gb300::DeviceFunction<MyGs> gs(ce.handle(), MyGs{...});
+//   gs.execute(/*rev=*/false, stream);
+//
+// Colored functions: every phase of the engine's flattened zone tree is one
+// launch; each leaf of the phase is one call f(start, end) on one thread,
+// start > end meaning rows start, start-1, ..., end+1 (the reference's
+// reverse sweep convention). Leaves of one phase never conflict, so the
+// calls of a launch may run in any order, exactly as the reference's threads
+// do.
+//
+// Matrix power: DevicePowerFunction calls f(start, end, pow), pow = 1..p,
+// on the engine's MPK level groups in a wavefront of stride 2 (step s holds
+// power k of group s-2k, so every call of a step depends only on earlier
+// steps: rows of a group reference rows of the neighbouring groups only);
+// one launch per step, each group cut into ranges of at most rowsPerCall
+// rows. The matrix the functor reads must be permuted with the engine's
+// permutation (getPerm/getInvPerm), as for the built-in MPK.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "race_gb300.h"
+
+namespace RACE {
+namespace gb300 {
+
+namespace detail {
+
+template <class F>
+__global__ void kColorPhase(F f, const int *leafLo, const int *leafHi, int first, int last) {
+    for (int l = first + blockIdx.x * blockDim.x + threadIdx.x; l < last; l += gridDim.x * blockDim.x)
+        f(leafLo[l], leafHi[l]);
+}
+
+template <class F>
+__global__ void kPowerStep(F f, const int4 *calls, int count) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const int4 c = calls[i];
+        f(c.x, c.y, c.z);
+    }
+}
+
+constexpr int kThreads = 128;
+constexpr int kMaxBlocks = 152 * 8;
+
+inline int blocksFor(int count) { return std::max(1, std::min((count + kThreads - 1) / kThreads, kMaxBlocks)); }
+
+}  // namespace detail
+
+// A colored function over the engine's schedule (both directions). The
+// engine must be colored (race_color) and outlive this object.
+template <class F>
+class DeviceFunction {
+  public:
+    DeviceFunction(race_engine *e, const F &f) : f_(f) {
+        for (int dir = 0; dir < 2; ++dir) {
+            Schedule &d = sched_[dir];
+            int np = 0, nl = 0;
+            rc_ = race_get_phases(e, dir, nullptr, nullptr, nullptr, 0, &np, &nl);
+            if (rc_ != RACE_SUCCESS) return;
+            const int cap = std::max(np + 1, nl);
+            std::vector<int> lo(cap), hi(cap);
+            d.phasePtr.resize(cap);
+            rc_ = race_get_phases(e, dir, d.phasePtr.data(), lo.data(), hi.data(), cap, &np, &nl);
+            if (rc_ != RACE_SUCCESS) return;
+            d.phasePtr.resize(np + 1);
+            rc_ = race_get_device_phases(e, dir, &d.leafLo, &d.leafHi, &nl);
+            if (rc_ != RACE_SUCCESS) return;
+        }
+    }
+    // RACE_SUCCESS, or the error of the constructor's schedule queries.
+    int status() const { return rc_; }
+    // Enqueues the sweep on `stream` (no synchronisation); RACE_ERR_CUDA if a
+    // launch failed.
+    int execute(bool rev = false, cudaStream_t stream = 0) const {
+        if (rc_ != RACE_SUCCESS) return rc_;
+        const Schedule &d = sched_[rev ? 1 : 0];
+        for (size_t p = 0; p + 1 < d.phasePtr.size(); ++p) {
+            const int first = d.phasePtr[p], last = d.phasePtr[p + 1];
+            detail::kColorPhase<F><<<detail::blocksFor(last - first), detail::kThreads, 0, stream>>>(
+                f_, d.leafLo, d.leafHi, first, last);
+        }
+        return cudaGetLastError() == cudaSuccess ? RACE_SUCCESS : RACE_ERR_CUDA;
+    }
+
+  private:
+    struct Schedule {
+        std::vector<int> phasePtr;
+        const int *leafLo = nullptr, *leafHi = nullptr;
+    };
+    F f_;
+    Schedule sched_[2];
+    int rc_ = RACE_SUCCESS;
+};
+
+// A matrix-power function of `power` steps over the engine's level groups
+// (after RACEColor(highestPower, cacheSize, ...)). Owns one device table of
+// (start, end, pow) calls.
+template <class F>
+class DevicePowerFunction {
+  public:
+    DevicePowerFunction(race_engine *e, const F &f, int power, int rowsPerCall = 32) : f_(f), power_(power) {
+        if (power < 1 || rowsPerCall < 1) {
+            rc_ = RACE_ERR_INVALID_ARG;
+            return;
+        }
+        int len = 0;
+        rc_ = race_get_power_groups(e, nullptr, 0, &len);
+        if (rc_ != RACE_SUCCESS) return;
+        std::vector<int> gp(len);
+        rc_ = race_get_power_groups(e, gp.data(), len, &len);
+        if (rc_ != RACE_SUCCESS) return;
+        const int G = len - 1;
+        std::vector<int4> calls;
+        stepPtr_.assign(1, 0);
+        for (int st = 0; st < G + 2 * (power - 1); ++st) {
+            for (int k = 0; k < power; ++k) {
+                const int g = st - 2 * k;
+                if (g < 0 || g >= G) continue;
+                for (int r = gp[g]; r < gp[g + 1]; r += rowsPerCall)
+                    calls.push_back(make_int4(r, std::min(r + rowsPerCall, gp[g + 1]), k + 1, 0));
+            }
+            stepPtr_.push_back((int)calls.size());
+        }
+        if (!calls.empty()) {
+            if (cudaMalloc(&calls_, sizeof(int4) * calls.size()) != cudaSuccess ||
+                cudaMemcpy(calls_, calls.data(), sizeof(int4) * calls.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+                rc_ = RACE_ERR_CUDA;
+        }
+    }
+    ~DevicePowerFunction() {
+        if (calls_) cudaFree(calls_);
+    }
+    DevicePowerFunction(const DevicePowerFunction &) = delete;
+    DevicePowerFunction &operator=(const DevicePowerFunction &) = delete;
+    int status() const { return rc_; }
+    int getPower() const { return power_; }
+    int execute(cudaStream_t stream = 0) const {
+        if (rc_ != RACE_SUCCESS) return rc_;
+        for (size_t st = 0; st + 1 < stepPtr_.size(); ++st) {
+            const int count = stepPtr_[st + 1] - stepPtr_[st];
+            if (count == 0) continue;
+            detail::kPowerStep<F><<<detail::blocksFor(count), detail::kThreads, 0, stream>>>(
+                f_, calls_ + stepPtr_[st], count);
+        }
+        return cudaGetLastError() == cudaSuccess ? RACE_SUCCESS : RACE_ERR_CUDA;
+    }
+
+  private:
+    F f_;
+    int power_;
+    std::vector<int> stepPtr_;
+    int4 *calls_ = nullptr;
+    int rc_ = RACE_SUCCESS;
+};
+
+}  // namespace gb300
+}  // namespace RACE

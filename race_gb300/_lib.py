@@ -34,7 +34,7 @@ EXPORTS = [
     "race_batch_graph_launch", "race_batch_get_status", "race_batch_info", "race_batch_last_error",
     "race_mlp_create", "race_mlp_destroy", "race_mlp_num_params", "race_mlp_set_params", "race_mlp_get_params",
     "race_mlp_forward", "race_mlp_loss_grad", "race_mlp_adam_step", "race_mlp_last_error", "race_wave_plan",
-    "race_simdify", "race_simdify_schedule", "race_simdify_d1", "race_get_highest_power",
+    "race_simdify", "race_simdify_schedule", "race_simdify_d1", "race_get_highest_power", "race_get_device_phases",
 ]
 
 
@@ -96,6 +96,7 @@ def lib():
             "race_wave_plan": [i, i, vp, vp, vp, vp, vp, i, vp, vp, i, ip, ip],
             "race_simdify": [vp, i, i, i, vp, vp, vp, vp, vp, i, i, ip],
             "race_get_highest_power": [vp, ip],
+            "race_get_device_phases": [vp, i, C.POINTER(vp), C.POINTER(vp), ip],
             "race_simdify_schedule": [i, i, i, vp, vp, vp, vp, vp, i, i, vp, vp, i, ip],
             "race_simdify_d1": [i, i, i, vp, vp, vp, vp, vp, i, i],
         }

@@ -331,6 +331,15 @@ int race_get_phases(race_engine *e, int rev, int *phasePtr, int *leafLo, int *le
     return RACE_SUCCESS;
 }
 
+int race_get_device_phases(race_engine *e, int rev, const int **leafLo, const int **leafHi, int *numLeaves) {
+    if (!e || !leafLo || !leafHi || !numLeaves || !e->eng->colored) return RACE_ERR_INVALID_ARG;
+    const race::DevPhases &d = e->eng->dPhases[rev ? 1 : 0];
+    *leafLo = d.leafLo.p;
+    *leafHi = d.leafHi.p;
+    *numLeaves = d.numLeaves;
+    return RACE_SUCCESS;
+}
+
 int race_get_power_groups(race_engine *e, int *buf, int cap, int *len) {
     if (!e || !len || !e->eng->powerReady) return RACE_ERR_INVALID_ARG;
     const std::vector<int> &g = e->eng->groupPtr;

@@ -1,0 +1,105 @@
+"""Custom device functions through the engine's schedule
+(include/race_gb300_device.cuh), the GPU counterpart of the reference's
+host callbacks: the example GS body as a colored functor must equal the
+sequential walk of the engine's phases bit for bit, and the MPK body as a
+power functor must equal p sequential SpMVs bit for bit. The functors live
+in tests/device_functors.cu, compiled here with nvcc for sm_103a."""
+import ctypes as C
+import pathlib
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from race_gb300 import _lib, build, matgen
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+SRC = ROOT / "tests" / "device_functors.cu"
+NVCC = ["-std=c++17", "-O3", "--fmad=false", *build.ARCH, "-I", str(ROOT / "include")]
+
+
+def _nvcc():
+    try:
+        return build._nvcc()
+    except RuntimeError:
+        pytest.skip("no nvcc")
+
+
+def test_device_header_compiles(tmp_path):
+    """The header-only templates instantiate and compile for sm_103a."""
+    r = subprocess.run([_nvcc(), *NVCC, "-c", str(SRC), "-o", str(tmp_path / "fn.o")], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.fixture(scope="module")
+def fnlib(tmp_path_factory):
+    out = tmp_path_factory.mktemp("fn") / "libdevice_functors.so"
+    lib_path = _lib.LIB_PATH
+    subprocess.check_call([_nvcc(), *NVCC, "-shared", "-Xcompiler", "-fPIC", "--cudart", "shared", str(SRC),
+                           str(lib_path), "-Xlinker", f"-rpath,{lib_path.parent}", "-o", str(out)])
+    _lib.lib()  # the engine library first, so both refer to one copy
+    L = C.CDLL(str(out))
+    vp = C.c_void_p
+    L.fn_gs.argtypes = [vp, vp, vp, vp, vp, vp, C.c_int]
+    L.fn_mpk.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]
+    return L
+
+
+def test_device_functions_link_and_reject_a_null_engine(fnlib):
+    """The functor library links against the engine and loads; without an
+    engine the schedule queries fail before any launch."""
+    bad = _lib.RACE_ERR_INVALID_ARG
+    assert fnlib.fn_gs(None, None, None, None, None, None, 0) == bad
+    assert fnlib.fn_mpk(None, None, None, None, None, 10, 2, 32) == bad
+    assert fnlib.fn_mpk(None, None, None, None, None, 10, 0, 32) == bad  # power below 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,d,t", [("lap7_16", 2, 16), ("aniso9_100x80", 1, 16), ("plaw_3k", 1, 32),
+                                   ("islands_330", 2, 16)])
+def test_device_function_gs_matches_sequential_walk(mats, fnlib, m, d, t):
+    import torch
+
+    from race_gb300 import interface as ri
+    A = mats[m]
+    rc = ri.Interface(A.n, t, d, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor() == 0
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    dm = ri.DeviceCsr.from_csr(P)
+    x0 = matgen.uniform_vector(A.n, 0)
+    b0 = matgen.uniform_vector(A.n, 1)
+    for rev in (False, True):
+        x = torch.tensor(x0, device="cuda")
+        b = torch.tensor(b0, device="cuda")
+        assert fnlib.fn_gs(rc._h, dm.row_ptr.data_ptr(), dm.col.data_ptr(), dm.val.data_ptr(), b.data_ptr(),
+                           x.data_ptr(), int(rev)) == 0
+        xr, br = x0.copy(), b0.copy()
+        pp, lo, hi = rc.getPhases(rev)
+        for p in range(len(pp) - 1):
+            for leaf in range(pp[p], pp[p + 1]):
+                orc.run_kernel(orc.K_GS, int(lo[leaf]), int(hi[leaf]), P, xr, br)
+        np.testing.assert_array_equal(x.cpu().numpy(), xr)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,p,c", [("st27_24", 8, 2e6), ("aniso5_120x90", 4, 5e5), ("band_5k", 8, 3300),
+                                   ("plaw_20k", 4, 1e6)])
+def test_device_power_function_matches_spmv_chain(mats, fnlib, m, p, c):
+    import torch
+
+    from race_gb300 import interface as ri
+    A = mats[m]
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, c) == 0
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    dm = ri.DeviceCsr.from_csr(P)
+    x0 = matgen.uniform_vector(A.n, 0)
+    Y = orc.mpk_plain(P, x0, p)
+    for rows in (32, 7):
+        x = torch.zeros((p + 1) * A.n, dtype=torch.float64, device="cuda")
+        x[: A.n] = torch.tensor(x0, device="cuda")
+        assert fnlib.fn_mpk(rc._h, dm.row_ptr.data_ptr(), dm.col.data_ptr(), dm.val.data_ptr(), x.data_ptr(), A.n,
+                            p, rows) == 0
+        np.testing.assert_array_equal(x.cpu().numpy().reshape(p + 1, A.n), Y)
