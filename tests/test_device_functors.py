@@ -103,3 +103,24 @@ def test_device_power_function_matches_spmv_chain(mats, fnlib, m, p, c):
         assert fnlib.fn_mpk(rc._h, dm.row_ptr.data_ptr(), dm.col.data_ptr(), dm.val.data_ptr(), x.data_ptr(), A.n,
                             p, rows) == 0
         np.testing.assert_array_equal(x.cpu().numpy().reshape(p + 1, A.n), Y)
+
+
+def test_integration_cuda_example_compiles(tmp_path):
+    """The CUDA example in INTEGRATION.md compiles for sm_103a (the functor
+    at file scope, the calls wrapped in a function)."""
+    import re
+    blocks = re.findall(r"```cuda\n(.*?)```", (ROOT / "INTEGRATION.md").read_text(), re.S)
+    assert blocks
+    for i, b in enumerate(blocks):
+        top, _, calls = b.partition("// after")
+        src = tmp_path / f"ex{i}.cu"
+        src.write_text(f"""#include "race_gb300.hpp"
+{top}
+void example(RACE::gb300::Interface &ce, int *d_rowPtr, int *d_col, double *d_val, double *d_b, double *d_x,
+             cudaStream_t stream) {{
+// after{calls}
+}}
+""")
+        r = subprocess.run([_nvcc(), *NVCC, "-c", str(src), "-o", str(tmp_path / f"ex{i}.o")], capture_output=True,
+                           text=True)
+        assert r.returncode == 0, r.stderr
