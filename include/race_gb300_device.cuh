@@ -21,13 +21,14 @@
 // calls of a launch may run in any order, exactly as the reference's threads
 // do.
 //
-// Matrix power: DevicePowerFunction calls f(start, end, pow), pow = 1..p,
-// on the engine's MPK level groups in a wavefront of stride 2 (step s holds
-// power k of group s-2k, so every call of a step depends only on earlier
-// steps: rows of a group reference rows of the neighbouring groups only);
-// one launch per step, each group cut into ranges of at most rowsPerCall
-// rows. The matrix the functor reads must be permuted with the engine's
-// permutation (getPerm/getInvPerm), as for the built-in MPK.
+// Matrix power: DevicePowerFunction calls f(start, end, pow), pow = 1..p
+// (or f(start, end, pow, subPow) with sub-powers), on the engine's MPK level
+// groups in a wavefront of stride 2 (step s holds power k of group s-2k, so
+// every call of a step depends only on earlier steps: rows of a group
+// reference rows of the neighbouring groups only); one launch per step, each
+// group cut into ranges of at most rowsPerCall rows. The matrix the functor
+// reads must be permuted with the engine's permutation (getPerm/getInvPerm),
+// as for the built-in MPK.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -47,11 +48,45 @@ __global__ void kColorPhase(F f, const int *leafLo, const int *leafHi, int first
         f(leafLo[l], leafHi[l]);
 }
 
+// A power call: f(start, end, pow, subPow) when the functor takes four
+// arguments (main and sub power, both 1-based), else f(start, end, step)
+// with the 1-based step of power * subPower steps.
 template <class F>
-__global__ void kPowerStep(F f, const int4 *calls, int count) {
+__host__ __device__ auto invokePower(const F &f, int start, int end, int step, int subPower, int)
+    -> decltype(f(start, end, step, step), void()) {
+    f(start, end, (step - 1) / subPower + 1, (step - 1) % subPower + 1);
+}
+template <class F>
+__host__ __device__ void invokePower(const F &f, int start, int end, int step, int subPower, long) {
+    (void)subPower;
+    f(start, end, step);
+}
+
+template <class F>
+__global__ void kPowerStep(F f, const int4 *calls, int count, int subPower) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const int4 c = calls[i];
-        f(c.x, c.y, c.z);
+        invokePower(f, c.x, c.y, c.z, subPower, 0);
+    }
+}
+
+// The calls of a wavefront of `steps` powers over level groups (groupPtr:
+// groups+1 row offsets) with stride 2: wavefront step s holds power k+1 of
+// group s-2k (k = 0, 1, ...), each group cut into ranges of at most
+// rowsPerCall rows; calls[stepPtr[s] .. stepPtr[s+1]) are (start, end, k+1).
+inline void powerCalls(const std::vector<int> &groupPtr, int steps, int rowsPerCall, std::vector<int4> &calls,
+                       std::vector<int> &stepPtr) {
+    const int G = (int)groupPtr.size() - 1;
+    calls.clear();
+    stepPtr.assign(1, 0);
+    for (int st = 0; G > 0 && st < G + 2 * (steps - 1); ++st) {
+        for (int k = 0; k < steps; ++k) {
+            const int g = st - 2 * k;
+            if (g < 0 || g >= G) continue;
+            for (int r = groupPtr[g]; r < groupPtr[g + 1]; r += rowsPerCall)
+                calls.push_back(make_int4(r, std::min(r + rowsPerCall, groupPtr[g + 1]), k + 1, 0));
+        }
+        stepPtr.push_back((int)calls.size());
     }
 }
 
@@ -108,14 +143,18 @@ class DeviceFunction {
     int rc_ = RACE_SUCCESS;
 };
 
-// A matrix-power function of `power` steps over the engine's level groups
-// (after RACEColor(highestPower, cacheSize, ...)). Owns one device table of
-// (start, end, pow) calls.
+// A matrix-power function of `power` powers, each of `subPower` sub-steps
+// (registerFunction(f, args, power, subPower), interface.h:149-153: the
+// wavefront runs power * subPower steps), over the engine's level groups
+// (after RACEColor(highestPower, cacheSize, safety, mtxType,
+// highestSubPower)). The functor takes (start, end, pow, subPow) or, for
+// subPower 1, (start, end, pow). Owns one device table of calls.
 template <class F>
 class DevicePowerFunction {
   public:
-    DevicePowerFunction(race_engine *e, const F &f, int power, int rowsPerCall = 32) : f_(f), power_(power) {
-        if (power < 1 || rowsPerCall < 1) {
+    DevicePowerFunction(race_engine *e, const F &f, int power, int rowsPerCall = 32, int subPower = 1)
+        : f_(f), power_(power), subPower_(subPower) {
+        if (power < 1 || subPower < 1 || rowsPerCall < 1) {
             rc_ = RACE_ERR_INVALID_ARG;
             return;
         }
@@ -125,18 +164,8 @@ class DevicePowerFunction {
         std::vector<int> gp(len);
         rc_ = race_get_power_groups(e, gp.data(), len, &len);
         if (rc_ != RACE_SUCCESS) return;
-        const int G = len - 1;
         std::vector<int4> calls;
-        stepPtr_.assign(1, 0);
-        for (int st = 0; st < G + 2 * (power - 1); ++st) {
-            for (int k = 0; k < power; ++k) {
-                const int g = st - 2 * k;
-                if (g < 0 || g >= G) continue;
-                for (int r = gp[g]; r < gp[g + 1]; r += rowsPerCall)
-                    calls.push_back(make_int4(r, std::min(r + rowsPerCall, gp[g + 1]), k + 1, 0));
-            }
-            stepPtr_.push_back((int)calls.size());
-        }
+        detail::powerCalls(gp, power * subPower, rowsPerCall, calls, stepPtr_);
         if (!calls.empty()) {
             if (cudaMalloc(&calls_, sizeof(int4) * calls.size()) != cudaSuccess ||
                 cudaMemcpy(calls_, calls.data(), sizeof(int4) * calls.size(), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -150,20 +179,21 @@ class DevicePowerFunction {
     DevicePowerFunction &operator=(const DevicePowerFunction &) = delete;
     int status() const { return rc_; }
     int getPower() const { return power_; }
+    int getSubPower() const { return subPower_; }
     int execute(cudaStream_t stream = 0) const {
         if (rc_ != RACE_SUCCESS) return rc_;
         for (size_t st = 0; st + 1 < stepPtr_.size(); ++st) {
             const int count = stepPtr_[st + 1] - stepPtr_[st];
             if (count == 0) continue;
             detail::kPowerStep<F><<<detail::blocksFor(count), detail::kThreads, 0, stream>>>(
-                f_, calls_ + stepPtr_[st], count);
+                f_, calls_ + stepPtr_[st], count, subPower_);
         }
         return cudaGetLastError() == cudaSuccess ? RACE_SUCCESS : RACE_ERR_CUDA;
     }
 
   private:
     F f_;
-    int power_;
+    int power_, subPower_;
     std::vector<int> stepPtr_;
     int4 *calls_ = nullptr;
     int rc_ = RACE_SUCCESS;

@@ -124,3 +124,39 @@ void example(RACE::gb300::Interface &ce, int *d_rowPtr, int *d_col, double *d_va
         r = subprocess.run([_nvcc(), *NVCC, "-c", str(src), "-o", str(tmp_path / f"ex{i}.o")], capture_output=True,
                            text=True)
         assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("key,power,sub,rows", [("power__st27_24__p8__c2000000", 8, 1, 32),
+                                                ("power__band_5k__p8__c3300", 2, 3, 7),
+                                                ("power__tiny_1__p2__c10000", 2, 2, 32),
+                                                ("power__islands_330__p3__c20000", 3, 2, 5)])
+def test_power_call_schedule(golden, tmp_path, key, power, sub, rows):
+    """The matrix-power call table on the reference's level groups: every
+    row gets every (power, sub-power) exactly once, in order; the call of
+    group g at flat step q runs in wavefront step g + 2(q-1), so everything it
+    reads (flat step q-1 of groups g-1..g+1) ran in an earlier step; and a
+    four-argument functor sees (pow, subPow) = ((q-1)/sub+1, (q-1)%sub+1)."""
+    exe = tmp_path / "pc"
+    r = subprocess.run([_nvcc(), *NVCC, str(ROOT / "tests" / "power_calls_check.cu"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    gp = golden[key + "__lp"]
+    out = subprocess.run([str(exe), str(power), str(sub), str(rows)], input=" ".join(map(str, gp)),
+                         capture_output=True, text=True, check=True).stdout.split("\n")
+    steps = int(out[0])
+    T = power * sub
+    G = len(gp) - 1
+    assert steps == G + 2 * (T - 1)
+    n = int(gp[-1])
+    seen = np.zeros((T, n), np.int32)
+    group_of = np.searchsorted(gp, np.arange(n), side="right") - 1
+    for line in out[1:]:
+        if not line:
+            continue
+        s, start, end, q, pw, sp = map(int, line.split())
+        assert 0 <= start < end <= n and end - start <= rows
+        g = group_of[start]
+        assert group_of[end - 1] == g and s == g + 2 * (q - 1)
+        seen[q - 1, start:end] += 1
+        assert (pw, sp) == ((q - 1) // sub + 1, (q - 1) % sub + 1)
+    assert (seen == 1).all()
