@@ -68,6 +68,12 @@ POWER_CASES = [
 # does with max_recursion_stages = 0
 POWER_FLAT_CASES = [("plaw_20k", 4, 1e4), ("lap7_32", 4, 1e4)]
 
+# (matrix, triangle, power, cacheBytes): the lower ("L") or upper ("U")
+# triangle of the matrix, partitioned with mtxType L / U (one row per level,
+# traverse_GAP_graphSoA.cpp:316-335)
+POWER_TRI_CASES = [("lap7_16", "L", 4, 2e4), ("lap7_16", "U", 4, 2e4), ("plaw_3k", "L", 3, 1e5),
+                   ("plaw_3k", "U", 8, 5e4)]
+
 # simdify cases on colored matrices (each golden entry stores its own
 # permutation and zone tree): (matrix, dist, nthreads, simdWidth, C, extra padded slots per chunk, flag, pass)
 # pass "d2": Interface::simdify, flag = diagFirst; pass "d1": simdifyD1,
@@ -145,6 +151,20 @@ def key_color(m, d, t):
 
 def key_power(m, p, c):
     return f"power__{m}__p{p}__c{int(c)}"
+
+
+def key_power_tri(m, tri, p, c):
+    return f"powertri__{m}__{tri}__p{p}__c{int(c)}"
+
+
+def triangle(csr, tri: str):
+    """Lower ("L", col <= row) or upper ("U", col >= row) triangle of a CRS
+    matrix, entries in their original order within each row."""
+    rows = np.repeat(np.arange(csr.n), np.diff(csr.row_ptr))
+    keep = csr.col <= rows if tri == "L" else csr.col >= rows
+    rp = np.zeros(csr.n + 1, np.int32)
+    np.cumsum(np.bincount(rows[keep], minlength=csr.n), out=rp[1:])
+    return matgen.Csr(csr.n, rp, csr.col[keep].astype(np.int32), csr.val[keep].copy(), f"{csr.name}_{tri}")
 
 
 def key_power_flat(m, p, c):

@@ -25,9 +25,9 @@ sys.path.insert(0, str(ROOT / "tests"))
 os.environ.setdefault("ORACLE_QUIET", "1")
 os.environ.setdefault("OMP_NUM_THREADS", "8")
 
-from cases import (COLOR_CASES, EXEC_CASES, MATRICES, POWER_CASES, POWER_FLAT_CASES, SIMDIFY_CASES,  # noqa: E402
-                   TRAVERSE_CASES, arr_digest, digest, key_color, key_power, key_power_flat, key_simdify, key_trav,
-                   sell_layout)
+from cases import (COLOR_CASES, EXEC_CASES, MATRICES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES,  # noqa: E402
+                   SIMDIFY_CASES, TRAVERSE_CASES, arr_digest, digest, key_color, key_power, key_power_flat,
+                   key_power_tri, key_simdify, key_trav, sell_layout, triangle)
 from oracle import refpy  # noqa: E402
 from oracle.refpy import RefInterface  # noqa: E402
 from race_gb300 import matgen  # noqa: E402
@@ -170,6 +170,21 @@ def main():
         g[k + "__lp"] = np.array(tr[0]["lp"], np.int32)
         g[k + "__leaves"] = np.array(len(tr))
         print(k, "default leaves", int(g[k + "__default_leaves"]), "flat groups", len(tr[0]["lp"]) - 1)
+
+    # triangular matrix power: mtxType L / U on the lower / upper triangle
+    for m, tri, p, c in POWER_TRI_CASES:
+        T = triangle(M(m), tri)
+        k = key_power_tri(m, tri, p, c)
+        rp = refpy.RefPower(T, p, c, mtx_type=tri)
+        perm, ip = rp.perm()
+        tr = rp.tree()
+        assert (rp.coverage() == 1).all()
+        rp.close()
+        g[k + "__digest"] = np.array(digest(T))
+        g[k + "__perm"] = perm
+        g[k + "__lp"] = np.array(tr[0]["lp"], np.int32)
+        g[k + "__leaves"] = np.array(len(tr))
+        print(k, "groups", len(tr[0]["lp"]) - 1)
 
     # full-size MPK configuration: digests only
     A = matgen.stencil3d_27pt(128)

@@ -3,8 +3,8 @@
 import numpy as np
 import pytest
 
-from cases import (EXEC_CASES, POWER_CASES, POWER_FLAT_CASES, TRAVERSE_CASES, digest, key_color, key_power,
-                   key_power_flat, key_trav)
+from cases import (EXEC_CASES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES, TRAVERSE_CASES, digest, key_color,
+                   key_power, key_power_flat, key_power_tri, key_trav, triangle)
 from oracle import oracle as orc
 from race_gb300 import matgen
 
@@ -78,6 +78,23 @@ def test_mpk_flat_partition_matches_reference(golden, mats, m, p, c):
     lp = np.concatenate([[0], np.cumsum(lr)]).astype(np.int32)
     assert orc.mpk_groups(p, A.n, A.nnz, c, 2.0, 50, lp, ln) is None
     g = orc.mpk_groups(p, A.n, A.nnz, c, 2.0, 2**31 - 1, lp, ln)
+    np.testing.assert_array_equal(g[0], golden[k + "__lp"])
+
+
+@pytest.mark.parametrize("m,tri,p,c", POWER_TRI_CASES)
+def test_mpk_triangular_partition_matches_reference(golden, mats, m, tri, p, c):
+    """mtxType L / U: one row per level, forward or backward
+    (traverse_GAP_graphSoA.cpp:316-335), so the permutation is the identity
+    or the reversal and the single-stage grouping of the rows' non-zeros
+    gives the reference's level groups."""
+    T = triangle(mats[m], tri)
+    k = key_power_tri(m, tri, p, c)
+    assert str(golden[k + "__digest"]) == digest(T)
+    rows = np.arange(T.n, dtype=np.int32)
+    order = rows if tri == "L" else rows[::-1]
+    np.testing.assert_array_equal(golden[k + "__perm"], order)
+    lens = np.diff(T.row_ptr)[order]
+    g = orc.mpk_groups(p, T.n, T.nnz, c, 2.0, 50, np.arange(T.n + 1, dtype=np.int32), lens)
     np.testing.assert_array_equal(g[0], golden[k + "__lp"])
 
 
