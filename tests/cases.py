@@ -50,6 +50,16 @@ COLOR_CASES = [
     ("tiny_1", 1, 4),
 ]
 
+# distance-2 colorings with RACE::THREE_BLOCK (three blocks per thread,
+# macros.h:29-38): (matrix, nthreads); reference sweep outputs are stored for
+# all of them
+COLOR3_CASES = [("lap7_16", 16), ("band_5k", 32), ("plaw_3k", 16), ("islands_330", 8), ("aniso5_120x90", 48)]
+
+
+def key_color3(m, t):
+    return f"color3__{m}__t{t}"
+
+
 # coloring cases whose reference sweep outputs are stored
 EXEC_CASES = {("lap7_16", 2, 16), ("aniso9_100x80", 1, 16), ("plaw_3k", 1, 32), ("islands_330", 2, 16)}
 

@@ -25,9 +25,9 @@ sys.path.insert(0, str(ROOT / "tests"))
 os.environ.setdefault("ORACLE_QUIET", "1")
 os.environ.setdefault("OMP_NUM_THREADS", "8")
 
-from cases import (COLOR_CASES, EXEC_CASES, MATRICES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES,  # noqa: E402
+from cases import (COLOR3_CASES, COLOR_CASES, EXEC_CASES, MATRICES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES,  # noqa: E402
                    SIMDIFY_CASES, TRAVERSE_CASES, arr_digest, digest, key_color, key_power, key_power_flat,
-                   key_power_tri, key_simdify, key_trav, sell_layout, triangle)
+                   key_color3, key_power_tri, key_simdify, key_trav, sell_layout, triangle)
 from oracle import refpy  # noqa: E402
 from oracle.refpy import RefInterface  # noqa: E402
 from race_gb300 import matgen  # noqa: E402
@@ -127,6 +127,53 @@ def main():
         g[k + "__col"] = sell[0]
         g[k + "__src"] = sell[1].astype(np.int32)
         print(k, "ok" if ok else "cannot simdify")
+
+    # load balancer with THREE_BLOCK (distance 2 only)
+    lb3_rows = []
+    for m, d in TRAVERSE_CASES:
+        if d != 2:
+            continue
+        lr = g[key_trav(m, d) + "__levelRow"]
+        ln = g[key_trav(m, d) + "__levelNnz"]
+        for nt in (2, 5, 8, 33, 128):
+            for eff in (40.0, 10.0):
+                for tgt in (0, 1):
+                    r = refpy.lb(lr, ln, nt, eff, d, 1, tgt, 7)
+                    flat = [len(r["scale"])] + r["scale"] + [len(r["numBlocks"])] + r["zonePtr"] + \
+                           [len(r["subZonePtr"]) - 1] + r["subZonePtr"] + r["numBlocks"]
+                    lb3_rows.append((m, nt, eff, tgt, flat))
+    g["lb3__index"] = np.array([f"{m}|{nt}|{eff}|{tgt}" for m, nt, eff, tgt, _ in lb3_rows])
+    lens = np.array([len(f) for *_, f in lb3_rows], np.int32)
+    g["lb3__offsets"] = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    g["lb3__data"] = np.concatenate([np.array(f, np.int32) for *_, f in lb3_rows])
+    print("lb three-block cases", len(lb3_rows))
+
+    # distance-2 colorings with THREE_BLOCK, and the reference executor's
+    # sweeps on them
+    for m, t in COLOR3_CASES:
+        A = M(m)
+        rc = refpy.RefColor(A, 2, t, d2type=1)
+        k = key_color3(m, t)
+        p, ip = rc.perm()
+        g[k + "__digest"] = np.array(digest(A))
+        g[k + "__perm"] = p
+        g[k + "__tree"] = rc.tree_flat()
+        g[k + "__threads"] = np.array(rc.threads())
+        g[k + "__eff"] = np.array(rc.efficiency())
+        g[k + "__stage"] = np.array(rc.max_stage())
+        g[k + "__serial"] = rc.serial_part()
+        P = A.permuted(p, ip)
+        U = P.upper()
+        x0 = matgen.uniform_vector(A.n, 0)
+        b0 = matgen.uniform_vector(A.n, 1)
+        for kern, name, mat, rev in [(2, "symmspmv", U, False), (3, "gs", P, False), (3, "gsrev", P, True),
+                                     (4, "kacz", P, False), (1, "spmtv", P, False)]:
+            x = x0.copy()
+            b = np.zeros(A.n) if kern in (1, 2) else b0.copy()
+            rc.execute(kern, rev, mat, x, b)
+            g[k + f"__out_{name}"] = b if kern in (1, 2) else x
+        rc.close()
+        print(k, "threads", int(g[k + "__threads"]))
 
     for m, p, c in POWER_CASES:
         A = M(m)

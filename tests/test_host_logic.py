@@ -8,7 +8,7 @@ import re
 import numpy as np
 import pytest
 
-from cases import COLOR_CASES, EXEC_CASES, key_color
+from cases import COLOR3_CASES, COLOR_CASES, EXEC_CASES, digest, key_color, key_color3
 from oracle import oracle as orc
 from oracle.refpy import parse_zone_tree
 from race_gb300 import _lib, matgen
@@ -31,17 +31,29 @@ def test_library_exports_every_declared_symbol():
     assert sorted(_lib.EXPORTS) == declared
 
 
-def _lb(levelRow, levelNnz, nt, eff, dist, tgt, base=7):
+def _lb(levelRow, levelNnz, nt, eff, dist, tgt, base=7, d2type=0):
     L = _lib.lib()
     lr = np.ascontiguousarray(levelRow, np.int32)
     ln = np.ascontiguousarray(levelNnz, np.int32)
     n = C.c_int()
-    _lib.check(L.race_lb_balance(lr.ctypes.data, ln.ctypes.data, lr.size, nt, eff, dist, 0, tgt, base, None, 0,
+    _lib.check(L.race_lb_balance(lr.ctypes.data, ln.ctypes.data, lr.size, nt, eff, dist, d2type, tgt, base, None, 0,
                                  C.byref(n)))
     out = np.zeros(n.value, np.int32)
-    _lib.check(L.race_lb_balance(lr.ctypes.data, ln.ctypes.data, lr.size, nt, eff, dist, 0, tgt, base,
+    _lib.check(L.race_lb_balance(lr.ctypes.data, ln.ctypes.data, lr.size, nt, eff, dist, d2type, tgt, base,
                                  out.ctypes.data, n.value, C.byref(n)))
     return out
+
+
+def test_load_balancer_three_block_matches_reference(golden):
+    """RACE::THREE_BLOCK (three blocks per thread, gap 1; macros.h:29-38)."""
+    idx = golden["lb3__index"]
+    off = golden["lb3__offsets"]
+    data = golden["lb3__data"]
+    for i, key in enumerate(idx):
+        m, nt, eff, tgt = str(key).split("|")
+        k = f"trav__{m}__d2"
+        got = _lb(golden[k + "__levelRow"], golden[k + "__levelNnz"], int(nt), float(eff), 2, int(tgt), d2type=1)
+        np.testing.assert_array_equal(got, data[off[i]:off[i + 1]], err_msg=str(key))
 
 
 def test_load_balancer_matches_reference(golden):
@@ -55,15 +67,15 @@ def test_load_balancer_matches_reference(golden):
         np.testing.assert_array_equal(got, data[off[i]:off[i + 1]], err_msg=str(key))
 
 
-def _flatten(tree_flat, dist, rev, n):
+def _flatten(tree_flat, dist, rev, n, d2type=0):
     L = _lib.lib()
     t = np.ascontiguousarray(tree_flat, np.int32)
     npz, nl = C.c_int(), C.c_int()
-    _lib.check(L.race_flatten_zone_tree(t.ctypes.data, t.size, dist, 0, int(rev), n, n, None, None, None, 0,
+    _lib.check(L.race_flatten_zone_tree(t.ctypes.data, t.size, dist, d2type, int(rev), n, n, None, None, None, 0,
                                         C.byref(npz), C.byref(nl)))
     cap = max(nl.value, npz.value + 1)
     pp = np.zeros(cap, np.int32); lo = np.zeros(cap, np.int32); hi = np.zeros(cap, np.int32)
-    _lib.check(L.race_flatten_zone_tree(t.ctypes.data, t.size, dist, 0, int(rev), n, n, pp.ctypes.data,
+    _lib.check(L.race_flatten_zone_tree(t.ctypes.data, t.size, dist, d2type, int(rev), n, n, pp.ctypes.data,
                                         lo.ctypes.data, hi.ctypes.data, cap, C.byref(npz), C.byref(nl)))
     return pp[:npz.value + 1], lo[:nl.value], hi[:nl.value]
 
@@ -364,3 +376,34 @@ void example(int n, int *rowPtr, int *col, int *d_rowPtr, int *d_col, double *d_
         r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wno-unused-variable", "-I", str(root / "include"),
                             str(src)], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("m,t", COLOR3_CASES)
+def test_three_block_phases_reproduce_reference(golden, mats, m, t):
+    """THREE_BLOCK zone trees of the reference, flattened with three blocks
+    per thread: every row once, distance-2 conflict-free phases in both
+    directions, and the phase walk gives the reference executor's outputs
+    bit for bit (GS both ways, KACZ, SymmSpMV, SpMTV)."""
+    A = mats[m]
+    k = key_color3(m, t)
+    assert str(golden[k + "__digest"]) == digest(A)
+    perm = golden[k + "__perm"]
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(A.n, dtype=np.int32)
+    P = A.permuted(perm, inv)
+    U = P.upper()
+    assert int(golden[k + "__serial"][1]) <= int(golden[k + "__serial"][0])  # no serial part
+    for rev in (False, True):
+        pp, lo, hi = _flatten(golden[k + "__tree"], 2, rev, A.n, d2type=1)
+        assert _conflicts(P, pp, lo, hi, 2) == 0
+    x0 = matgen.uniform_vector(A.n, 0)
+    b0 = matgen.uniform_vector(A.n, 1)
+    for kern, name, mat, rev in [(orc.K_SYMMSPMV, "symmspmv", U, False), (orc.K_GS, "gs", P, False),
+                                 (orc.K_GS, "gsrev", P, True), (orc.K_KACZ, "kacz", P, False),
+                                 (orc.K_SPMTV, "spmtv", P, False)]:
+        scatter = kern in (orc.K_SYMMSPMV, orc.K_SPMTV)
+        x, b = x0.copy(), (np.zeros(A.n) if scatter else b0.copy())
+        pp, lo, hi = _flatten(golden[k + "__tree"], 2, rev, A.n, d2type=1)
+        _run_phases(pp, lo, hi, kern, mat, x, b)
+        np.testing.assert_array_equal(b if scatter else x, golden[k + f"__out_{name}"], err_msg=name)
+
