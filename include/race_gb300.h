@@ -286,6 +286,22 @@ int race_lb_balance(const int *levelRow, const int *levelNnz, int totalLevel, in
 int race_flatten_zone_tree(const int *tree, int treeLen, int dist, int d2type, int rev, int serialLo, int serialHi,
                            int *phasePtr, int *leafLo, int *leafHi, int cap, int *numPhases, int *numLeaves);
 
+/* Host-only: RACE's level recursion (level_recursion.cpp:149-376, the
+ * zone tree of race_color) with the traversal supplied by the caller instead
+ * of the engine's GPU BFS. `trav` runs one traversal of rows [lo,hi) of the
+ * current permuted index space (BFS levels, stable level sort composed into
+ * the caller's running permutation) and writes the per-level row and
+ * non-zero counts (at most cap levels; returns 0, or nonzero to abort);
+ * `rangeNnz` returns the non-zeros of rows [lo,hi) in the current
+ * permutation. Writes the serialised zone tree (format of
+ * race_get_zone_tree) when cap >= *treeLen. For tests and for callers with
+ * their own traversal. */
+typedef int (*race_traverse_fn)(void *user, int lo, int hi, int *levelRow, int *levelNnz, int cap, int *totalLevel);
+typedef long long (*race_range_nnz_fn)(void *user, int lo, int hi);
+int race_zone_tree_host(int nrow, int nthreads, int dist, int d2type, int lbTarget, const race_params *params,
+                        race_traverse_fn trav, race_range_nnz_fn rangeNnz, void *user, int *treeBuf, int cap,
+                        int *treeLen, int *availableThreads);
+
 /* Host-only: the wave plan of built-in kernel `kernel` on a CRS pattern
  * (host arrays) for a phase table (as from race_get_phases): rows grouped
  * into conflict-free waves that keep RACE's order between every pair of

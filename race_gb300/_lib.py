@@ -35,6 +35,7 @@ EXPORTS = [
     "race_mlp_create", "race_mlp_destroy", "race_mlp_num_params", "race_mlp_set_params", "race_mlp_get_params",
     "race_mlp_forward", "race_mlp_loss_grad", "race_mlp_adam_step", "race_mlp_last_error", "race_wave_plan",
     "race_simdify", "race_simdify_schedule", "race_simdify_d1", "race_get_highest_power", "race_get_device_phases",
+    "race_zone_tree_host",
 ]
 
 
@@ -54,6 +55,11 @@ class race_operands(C.Structure):
     _fields_ = [("n", C.c_int), ("rowPtr", C.c_void_p), ("col", C.c_void_p), ("val", C.c_void_p),
                 ("val_type", C.c_int), ("x", C.c_void_p), ("b", C.c_void_p), ("vec_type", C.c_int)]
 
+
+# callback types of race_zone_tree_host
+TRAVERSE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int,
+                          C.POINTER(C.c_int))
+RANGE_NNZ_FN = C.CFUNCTYPE(C.c_longlong, C.c_void_p, C.c_int, C.c_int)
 
 _lib = None
 
@@ -97,6 +103,8 @@ def lib():
             "race_simdify": [vp, i, i, i, vp, vp, vp, vp, vp, i, i, ip],
             "race_get_highest_power": [vp, ip],
             "race_get_device_phases": [vp, i, C.POINTER(vp), C.POINTER(vp), ip],
+            "race_zone_tree_host": [i, i, i, i, i, C.POINTER(race_params), TRAVERSE_FN, RANGE_NNZ_FN, vp, vp, i, ip,
+                                    ip],
             "race_simdify_schedule": [i, i, i, vp, vp, vp, vp, vp, i, i, vp, vp, i, ip],
             "race_simdify_d1": [i, i, i, vp, vp, vp, vp, vp, i, i],
         }

@@ -502,6 +502,44 @@ int race_flatten_zone_tree(const int *tree, int treeLen, int dist, int d2type, i
     });
 }
 
+int race_zone_tree_host(int nrow, int nthreads, int dist, int d2type, int lbTarget, const race_params *params,
+                        race_traverse_fn trav, race_range_nnz_fn rangeNnz, void *user, int *treeBuf, int cap,
+                        int *treeLen, int *availableThreads) {
+    if (nrow < 0 || nthreads < 1 || (dist != race::DIST_ONE && dist != race::DIST_TWO) || !trav || !rangeNnz ||
+        !treeLen || !availableThreads)
+        return RACE_ERR_INVALID_ARG;
+    return guard(nullptr, [&] {
+        auto traverse = [&](int lo, int hi) {
+            race::LevelData ld;
+            if (hi <= lo) return ld;
+            // a distance-2 BFS may pass through rows outside [lo,hi) and an
+            // island restart adds an empty level, so allow twice the graph
+            const int levelCap = 2 * nrow + 2;
+            ld.levelRow.assign(levelCap, 0);
+            ld.levelNnz.assign(levelCap, 0);
+            int total = 0;
+            if (trav(user, lo, hi, ld.levelRow.data(), ld.levelNnz.data(), levelCap, &total) != 0 || total < 0 ||
+                total > levelCap)
+                throw Error(RACE_ERR_GRAPH_TRAVERSAL, "the caller's traversal failed");
+            ld.levelRow.resize(total);
+            ld.levelNnz.resize(total);
+            ld.totalLevel = total;
+            for (int l = 0; l < total; ++l) {
+                ld.nrow += ld.levelRow[l];
+                ld.nnz += ld.levelNnz[l];
+            }
+            return ld;
+        };
+        race::LevelRecursion lr(nrow, nthreads, dist, d2type, lbTarget, toParams(params), traverse,
+                                [&](int lo, int hi) { return rangeNnz(user, lo, hi); });
+        lr.levelBalancing();
+        std::vector<int> v = race::serializeZoneTree(lr.tree);
+        *treeLen = (int)v.size();
+        *availableThreads = lr.availableThreads;
+        if (treeBuf && cap >= (int)v.size()) memcpy(treeBuf, v.data(), sizeof(int) * v.size());
+    });
+}
+
 int race_wave_plan(int kernel, int n, const int *rowPtr, const int *col, const int *phasePtr, const int *leafLo,
                    const int *leafHi, int numPhases, int *wavePtr, int *rows, int cap, int *numWaves, int *numRows) {
     if (!rowPtr || !col || !phasePtr || !leafLo || !leafHi || n < 0 || numPhases < 0 || !numWaves || !numRows)

@@ -407,3 +407,57 @@ def test_three_block_phases_reproduce_reference(golden, mats, m, t):
         _run_phases(pp, lo, hi, kern, mat, x, b)
         np.testing.assert_array_equal(b if scatter else x, golden[k + f"__out_{name}"], err_msg=name)
 
+
+
+def _zone_tree_host(A, d, t, d2type, cap):
+    """The engine's level recursion (race_zone_tree_host) driven by the
+    oracle's traversal, which keeps the running permutation here."""
+    L = _lib.lib()
+    lens = np.diff(A.row_ptr).astype(np.int64)
+    state = {"tp": np.arange(A.n, dtype=np.int32), "ti": np.arange(A.n, dtype=np.int32), "err": None}
+
+    @_lib.TRAVERSE_FN
+    def trav(user, lo, hi, lr_ptr, ln_ptr, lcap, total):
+        try:
+            tp, ti, lr, ln, _ = orc.traverse(A, d, lo, hi, state["tp"], state["ti"])
+            state["tp"], state["ti"] = tp, ti
+            if len(lr) > lcap:
+                return 1
+            np.ctypeslib.as_array(lr_ptr, shape=(lcap,))[: len(lr)] = lr
+            np.ctypeslib.as_array(ln_ptr, shape=(lcap,))[: len(ln)] = ln
+            total[0] = len(lr)
+            return 0
+        except Exception as ex:  # report instead of unwinding through C
+            state["err"] = ex
+            return 1
+
+    @_lib.RANGE_NNZ_FN
+    def rnnz(user, lo, hi):
+        return int(lens[state["tp"][lo:hi]].sum())
+
+    buf = np.zeros(cap, np.int32)
+    tlen, avail = C.c_int(), C.c_int()
+    rc = L.race_zone_tree_host(A.n, t, d, d2type, 1, None, trav, rnnz, None, buf.ctypes.data, cap, C.byref(tlen),
+                               C.byref(avail))
+    assert state["err"] is None, state["err"]
+    _lib.check(rc)
+    assert tlen.value <= cap
+    return buf[: tlen.value], avail.value, state["tp"]
+
+
+@pytest.mark.parametrize("m,d,t,d2type", [c + (0,) for c in COLOR_CASES]
+                         + [(m, 2, t, 1) for m, t in COLOR3_CASES])
+def test_level_recursion_on_host_matches_reference(golden, mats, m, d, t, d2type, monkeypatch):
+    """The engine's restatement of RACE's level recursion and zone tree
+    (coloring.cpp), run on the CPU with the oracle's traversal in place of
+    the GPU BFS: the zone tree, the thread count and the permutation equal
+    the reference's (TWO_BLOCK and THREE_BLOCK)."""
+    for var in ("RACE_EFFICIENCY", "RACE_THREADS", "RACE_CACHE_VIOLATION_CUTOFF", "RACE_MAX_RECURSION_STAGES"):
+        monkeypatch.delenv(var, raising=False)
+    A = mats[m]
+    k = key_color(m, d, t) if d2type == 0 else key_color3(m, t)
+    gold = golden[k + "__tree"]
+    tree, avail, perm = _zone_tree_host(A, d, t, d2type, 2 * gold.size + 1024)
+    np.testing.assert_array_equal(tree, gold)
+    assert avail == int(golden[k + "__threads"])
+    np.testing.assert_array_equal(perm, golden[k + "__perm"])
