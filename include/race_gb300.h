@@ -131,7 +131,8 @@ int race_get_zone_tree(race_engine *e, int *buf, int cap, int *len);
 int race_get_phases(race_engine *e, int rev, int *phasePtr, int *leafLo, int *leafHi, int cap, int *numPhases,
                     int *numLeaves);
 /* The same leaf ranges in device memory owned by the engine (valid until
- * race_destroy), for custom device functions (race_gb300_device.cuh). */
+ * race_color runs again or race_destroy), for custom device functions
+ * (race_gb300_device.cuh). */
 int race_get_device_phases(race_engine *e, int rev, const int **leafLo, const int **leafHi, int *numLeaves);
 /* MPK level groups (consolidated levelPtr of the reference's MPLeaf::lp,
  * matrixPowerRecursive.h:27-62), *len = groups+1. */

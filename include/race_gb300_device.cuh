@@ -98,7 +98,8 @@ inline int blocksFor(int count) { return std::max(1, std::min((count + kThreads 
 }  // namespace detail
 
 // A colored function over the engine's schedule (both directions). The
-// engine must be colored (race_color) and outlive this object.
+// engine must be colored (race_color) and outlive this object, and must not
+// be colored again while it is used (the schedule is read at construction).
 template <class F>
 class DeviceFunction {
   public:
