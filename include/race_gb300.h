@@ -287,6 +287,19 @@ int race_lb_balance(const int *levelRow, const int *levelNnz, int totalLevel, in
 int race_flatten_zone_tree(const int *tree, int treeLen, int dist, int d2type, int rev, int serialLo, int serialHi,
                            int *phasePtr, int *leafLo, int *leafHi, int cap, int *numPhases, int *numLeaves);
 
+/* Host-only: RACE's single-stage MPK partition (mtxPower::findPartition,
+ * matrixPower.cpp:505-605) of BFS levels levelRow/levelNnz (totalLevel
+ * levels from row 0): cache-violating levels, hopeless regions
+ * (identifyHopelessRegions, :147-503) and the consolidated level groups
+ * (consolidatePartition, :685-940). power = highestPower * highestSubPower;
+ * graphRows/graphNnz give the bytes per non-zero; cutoff is the cache
+ * violation cut-off (INT_MAX: no hopeless regions). Writes groupPtr
+ * (numGroups+1 row offsets, the reference's MPLeaf::lp) and hopeless
+ * (numHopeless group indices, MPLeaf::hid) when cap is large enough for both. */
+int race_mpk_stage_partition(const int *levelRow, const int *levelNnz, int totalLevel, int graphRows,
+                             long long graphNnz, int power, double cacheSize, double safety, int cutoff, int *groupPtr,
+                             int *hopeless, int cap, int *numGroups, int *numHopeless);
+
 /* Host-only: RACE's level recursion (level_recursion.cpp:149-376, the
  * zone tree of race_color) with the traversal supplied by the caller instead
  * of the engine's GPU BFS. `trav` runs one traversal of rows [lo,hi) of the

@@ -7,6 +7,7 @@
 #include <numeric>
 
 #include "engine.h"
+#include "partition.h"
 #include "simdify.h"
 
 namespace race {
@@ -498,6 +499,28 @@ int race_flatten_zone_tree(const int *tree, int treeLen, int dist, int d2type, i
             memcpy(phasePtr, pt.phasePtr.data(), sizeof(int) * pt.phasePtr.size());
             memcpy(leafLo, pt.leafLo.data(), sizeof(int) * pt.leafLo.size());
             memcpy(leafHi, pt.leafHi.data(), sizeof(int) * pt.leafHi.size());
+        }
+    });
+}
+
+int race_mpk_stage_partition(const int *levelRow, const int *levelNnz, int totalLevel, int graphRows,
+                             long long graphNnz, int power, double cacheSize, double safety, int cutoff, int *groupPtr,
+                             int *hopeless, int cap, int *numGroups, int *numHopeless) {
+    if (totalLevel < 0 || (totalLevel > 0 && (!levelRow || !levelNnz)) || graphRows < 1 || graphNnz < 1 ||
+        power < 1 || !(cacheSize > 0) || !numGroups || !numHopeless)
+        return RACE_ERR_INVALID_ARG;
+    return guard(nullptr, [&] {
+        race::LevelData ld;
+        ld.totalLevel = totalLevel;
+        ld.levelRow.assign(levelRow, levelRow + totalLevel);
+        ld.levelNnz.assign(levelNnz, levelNnz + totalLevel);
+        const race::StagePartition sp =
+            race::stagePartition(ld, 0, power, graphRows, graphNnz, cacheSize, safety, cutoff);
+        *numGroups = (int)sp.groupPtr.size() - 1;
+        *numHopeless = (int)sp.hopeless.size();
+        if (groupPtr && hopeless && cap >= (int)sp.groupPtr.size() && cap >= (int)sp.hopeless.size()) {
+            memcpy(groupPtr, sp.groupPtr.data(), sizeof(int) * sp.groupPtr.size());
+            if (!sp.hopeless.empty()) memcpy(hopeless, sp.hopeless.data(), sizeof(int) * sp.hopeless.size());
         }
     });
 }

@@ -78,6 +78,17 @@ POWER_CASES = [
 # does with max_recursion_stages = 0
 POWER_FLAT_CASES = [("plaw_20k", 4, 1e4), ("lap7_32", 4, 1e4)]
 
+# (matrix, power, cacheBytes) with hopeless regions at the default settings:
+# the reference's stage-0 level groups and hopeless groups (before its
+# recursion, which reorders rows inside groups only) are stored
+HOPELESS_CASES = POWER_FLAT_CASES + [("band_5k", 8, 3000), ("band_5k", 8, 2500), ("band_5k", 8, 3200),
+                                     ("plaw_3k", 4, 2e3), ("lap7_16", 4, 2e4), ("st27_24", 8, 1e5)]
+
+
+def key_hopeless(m, p, c):
+    return f"hopeless__{m}__p{p}__c{int(c)}"
+
+
 # (matrix, triangle, power, cacheBytes): the lower ("L") or upper ("U")
 # triangle of the matrix, partitioned with mtxType L / U (one row per level,
 # traverse_GAP_graphSoA.cpp:316-335)

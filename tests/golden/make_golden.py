@@ -25,9 +25,9 @@ sys.path.insert(0, str(ROOT / "tests"))
 os.environ.setdefault("ORACLE_QUIET", "1")
 os.environ.setdefault("OMP_NUM_THREADS", "8")
 
-from cases import (COLOR3_CASES, COLOR_CASES, EXEC_CASES, MATRICES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES,  # noqa: E402
+from cases import (COLOR3_CASES, COLOR_CASES, EXEC_CASES, HOPELESS_CASES, MATRICES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES,  # noqa: E402
                    SIMDIFY_CASES, TRAVERSE_CASES, arr_digest, digest, key_color, key_power, key_power_flat,
-                   key_color3, key_power_tri, key_simdify, key_trav, sell_layout, triangle)
+                   key_color3, key_hopeless, key_power_tri, key_simdify, key_trav, sell_layout, triangle)
 from oracle import refpy  # noqa: E402
 from oracle.refpy import RefInterface  # noqa: E402
 from race_gb300 import matgen  # noqa: E402
@@ -217,6 +217,20 @@ def main():
         g[k + "__lp"] = np.array(tr[0]["lp"], np.int32)
         g[k + "__leaves"] = np.array(len(tr))
         print(k, "default leaves", int(g[k + "__default_leaves"]), "flat groups", len(tr[0]["lp"]) - 1)
+
+    # default partitions with hopeless regions: stage-0 level groups and the
+    # consolidated hopeless groups
+    for m, p, c in HOPELESS_CASES:
+        A = M(m)
+        k = key_hopeless(m, p, c)
+        rp = refpy.RefPower(A, p, c)
+        tr = rp.tree()
+        rp.close()
+        g[k + "__digest"] = np.array(digest(A))
+        g[k + "__lp"] = np.array(tr[0]["lp"], np.int32)
+        g[k + "__hid"] = np.array(tr[0]["hid"], np.int32)
+        g[k + "__leaves"] = np.array(len(tr))
+        print(k, "groups", len(tr[0]["lp"]) - 1, "hopeless", tr[0]["hid"], "leaves", len(tr))
 
     # triangular matrix power: mtxType L / U on the lower / upper triangle
     for m, tri, p, c in POWER_TRI_CASES:

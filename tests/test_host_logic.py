@@ -461,3 +461,46 @@ def test_level_recursion_on_host_matches_reference(golden, mats, m, d, t, d2type
     np.testing.assert_array_equal(tree, gold)
     assert avail == int(golden[k + "__threads"])
     np.testing.assert_array_equal(perm, golden[k + "__perm"])
+
+
+def _stage_partition(lr, ln, n, nnz, power, cache, cutoff=50):
+    L = _lib.lib()
+    lr = np.ascontiguousarray(lr, np.int32)
+    ln = np.ascontiguousarray(ln, np.int32)
+    ng, nh = C.c_int(), C.c_int()
+    args = [lr.ctypes.data, ln.ctypes.data, lr.size, n, nnz, power, float(cache), 2.0, cutoff]
+    _lib.check(L.race_mpk_stage_partition(*args, None, None, 0, C.byref(ng), C.byref(nh)))
+    cap = max(ng.value + 1, nh.value, 1)
+    gp, hid = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
+    _lib.check(L.race_mpk_stage_partition(*args, gp.ctypes.data, hid.ctypes.data, cap, C.byref(ng), C.byref(nh)))
+    return gp[: ng.value + 1], hid[: nh.value]
+
+
+def test_stage_partition_matches_reference(golden, mats):
+    """The single-stage MPK partition with hopeless regions
+    (race_mpk_stage_partition) on the BFS levels of the oracle's traversal
+    gives the reference's level groups (MPLeaf::lp) and hopeless groups
+    (MPLeaf::hid): cases without hopeless regions, cases with them (whose
+    reference partition then recurses inside those groups), and partitions
+    without recursion (cut-off disabled)."""
+    from cases import HOPELESS_CASES, POWER_CASES, POWER_FLAT_CASES, key_hopeless, key_power, key_power_flat
+    cases = [(mpc, key_power(*mpc), 50, golden[key_power(*mpc) + "__hid"][:-1]) for mpc in POWER_CASES]  # -1 ends
+    cases += [(mpc, key_hopeless(*mpc), 50, golden[key_hopeless(*mpc) + "__hid"]) for mpc in HOPELESS_CASES]
+    cases += [(mpc, key_power_flat(*mpc), 2**31 - 1, np.zeros(0, np.int32)) for mpc in POWER_FLAT_CASES]
+    with_hopeless = 0
+    for (m, p, c), k, cutoff, want_hid in cases:
+        A = mats[m]
+        _, _, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+        gp, hid = _stage_partition(lr, ln, A.n, A.nnz, p, c, cutoff)
+        np.testing.assert_array_equal(gp, golden[k + "__lp"], err_msg=k)
+        np.testing.assert_array_equal(hid, want_hid, err_msg=k)
+        with_hopeless += hid.size > 0
+    assert with_hopeless >= 6
+    # triangular matrices (mtxType L / U): one row per level
+    from cases import POWER_TRI_CASES, key_power_tri, triangle
+    for m, tri, p, c in POWER_TRI_CASES:
+        T = triangle(mats[m], tri)
+        lens = np.diff(T.row_ptr).astype(np.int32)
+        order = lens if tri == "L" else lens[::-1]
+        gp, hid = _stage_partition(np.ones(T.n, np.int32), order, T.n, T.nnz, p, c)
+        np.testing.assert_array_equal(gp, golden[key_power_tri(m, tri, p, c) + "__lp"])
