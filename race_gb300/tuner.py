@@ -20,7 +20,7 @@ of power p) and learns from the search:
   forward, MSE gradient, Adam); it picks the feasible config with the
   lowest predicted time;
 * ``Tuner.choose``: the MLP's choice, or the search (the fallback when no
-  model is loaded, and the judge of the model's regret:
+  model is loaded, and the yardstick of the model's regret:
   regret = t(chosen) / t(best searched) - 1).
 
 A second task, ``SWEEP_TASK``, tunes RACE's coloring for a symmetric
