@@ -45,6 +45,8 @@ def lib():
         L = C.CDLL(str(LIB))
         L.orc_bfs.restype = C.c_int
         L.orc_bfs.argtypes = [C.c_int, IP, IP, IP, IP, C.c_int, C.c_int, C.c_int, IP]
+        L.orc_bfs_boundary.restype = C.c_int
+        L.orc_bfs_boundary.argtypes = [C.c_int, IP, IP, IP, IP, C.c_int, C.c_int, C.c_int, IP, IP, IP]
         L.orc_level_data.argtypes = [IP, IP, IP, C.c_int, C.c_int, C.c_int, IP, IP]
         L.orc_level_permute.argtypes = [C.c_int, IP, C.c_int, C.c_int, C.c_int, IP, IP]
         for nm in ["orc_spmv_range", "orc_spmtv_range", "orc_symmspmv_range"]:
@@ -97,6 +99,30 @@ def traverse(csr, dist: int, lo: int, hi: int, total_perm=None, total_inv=None):
     lib().orc_level_data(_i32(csr.row_ptr), tp, d, lo, hi, L, lr, ln)
     lib().orc_level_permute(n, d, lo, hi, L, tp, ti)
     return tp, ti, lr[:L], ln[:L], d
+
+
+def traverse_boundary(csr, lo: int, hi: int, regions, total_perm, total_inv):
+    """One traversal of a recursion stage of the MPK partition: rows [lo,hi)
+    with boundary regions [(lo_k, hi_k), ...] (orc_bfs_boundary), then the
+    range and every boundary region each stably sorted by level and composed
+    into the running permutation (permuteGraph, traverse_GAP_graphSoA.cpp:
+    506-575). Returns the new (total_perm, total_inv, levels of [lo,hi),
+    number of levels)."""
+    n = csr.n
+    tp = _i32(total_perm).copy()
+    ti = _i32(total_inv).copy()
+    blo = _i32([a for a, _ in regions] or [0])
+    bhi = _i32([b for _, b in regions] or [0])
+    d = np.zeros(n, np.int32)
+    L = lib().orc_bfs_boundary(n, _i32(csr.row_ptr), _i32(csr.col), tp, ti, lo, hi, len(regions), blo, bhi, d)
+    if L < 0:
+        raise RuntimeError("oracle BFS: some rows went missing")
+    lr = np.zeros(L, np.int32)
+    ln = np.zeros(L, np.int32)
+    lib().orc_level_data(_i32(csr.row_ptr), tp, d, lo, hi, L, lr, ln)
+    for a, b in [(lo, hi)] + list(regions):
+        lib().orc_level_permute(n, d, a, b, L, tp, ti)
+    return tp, ti, lr, ln, L
 
 
 def run_kernel(kernel: int, start: int, end: int, csr, x, b):

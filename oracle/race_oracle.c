@@ -129,6 +129,97 @@ int orc_bfs(int n, const int *rowPtr, const int *col, const int *totalPerm, cons
     return currLvl;
 }
 
+/* BFS of the rows [lo,hi) of a recursion stage of the MPK partition
+ * together with its boundary regions [bLo[k], bHi[k]) (Traverse with a
+ * boundaryRange and dist POWER, traverse_GAP_graphSoA.cpp:31-90, 135-221,
+ * 236-330): from row lo, a child inside [lo,hi) takes the next level and
+ * counts toward the range; a child in a boundary region also takes the next
+ * level and carries the search on but does not count; other rows are not
+ * visited. When the search dies out before the range is covered, the first
+ * unvisited row of the range restarts it on the same level (no extra level
+ * for POWER). Boundary rows left unvisited get the level after the last one
+ * (createLevelData, :452-472). Returns the number of levels (at least 1),
+ * or -1 if rows of the range went missing. */
+int orc_bfs_boundary(int n, const int *rowPtr, const int *col, const int *totalPerm, const int *totalInvPerm, int lo,
+                     int hi, int nb, const int *bLo, const int *bHi, int *dist_out) {
+    char *inB = (char *)calloc((size_t)n + 1, 1);
+    for (int k = 0; k < nb; ++k)
+        for (int i = bLo[k]; i < bHi[k]; ++i) inB[i] = 1;
+    int *parent = (int *)malloc(sizeof(int) * (size_t)n);
+    int *queue = (int *)malloc(sizeof(int) * ((size_t)n + 1));
+    for (int i = 0; i < n; ++i) {
+        dist_out[i] = -1;
+        parent[i] = -1;
+    }
+    int qlo = 0, qhi = 0, qin = 0, counter = 0, currLvl = 0;
+    if (lo < hi) {
+        queue[qin++] = lo;
+        dist_out[lo] = 0;
+        parent[lo] = 0;
+        counter = 1;
+    }
+    qhi = qin;
+    int prevIslandStop = lo;
+    while (qlo != qhi) {
+        currLvl += 1;
+        for (int q = qlo; q < qhi; ++q) {
+            int u = queue[q];
+            int pu = totalPerm[u];
+            for (int idx = rowPtr[pu]; idx < rowPtr[pu + 1]; ++idx) {
+                int child = col[idx];
+                if (child >= n) continue;
+                child = totalInvPerm[child];
+                if (parent[child] != -1) continue;
+                if (child >= lo && child < hi) {
+                    parent[child] = u;
+                    queue[qin++] = child;
+                    dist_out[child] = currLvl;
+                    counter++;
+                } else if (inB[child]) {
+                    parent[child] = u;
+                    queue[qin++] = child;
+                    dist_out[child] = currLvl;
+                }
+            }
+        }
+        qlo = qhi;
+        qhi = qin;
+        if (qlo == qhi && counter != (hi - lo)) {
+            for (int i = prevIslandStop; i < hi; ++i) {
+                if (dist_out[i] == -1) {
+                    queue[qin++] = i;
+                    counter++;
+                    qlo = qhi;
+                    qhi = qin;
+                    dist_out[i] = currLvl;
+                    parent[i] = i;
+                    prevIslandStop = i;
+                    break;
+                }
+            }
+            if (qlo == qhi) {
+                currLvl = -1;
+                break;
+            }
+        }
+    }
+    if (currLvl >= 0) {
+        int untouched = 0;
+        for (int k = 0; k < nb; ++k)
+            for (int i = bLo[k]; i < bHi[k]; ++i)
+                if (dist_out[i] == -1) {
+                    dist_out[i] = currLvl;
+                    untouched = 1;
+                }
+        currLvl += untouched;
+        if (currLvl < 1) currLvl = 1;
+    }
+    free(inB);
+    free(parent);
+    free(queue);
+    return currLvl;
+}
+
 /* Per-level row and nnz counts over [lo,hi) (findLevelData,
  * traverse_GAP_graphSoA.cpp:385-447). Row lengths are taken from the original
  * row totalPerm[i]. */

@@ -225,11 +225,13 @@ def main():
         k = key_hopeless(m, p, c)
         rp = refpy.RefPower(A, p, c)
         tr = rp.tree()
+        perm, _ = rp.perm()
         rp.close()
         g[k + "__digest"] = np.array(digest(A))
         g[k + "__lp"] = np.array(tr[0]["lp"], np.int32)
         g[k + "__hid"] = np.array(tr[0]["hid"], np.int32)
         g[k + "__leaves"] = np.array(len(tr))
+        g[k + "__perm"] = perm  # after the recursion into the hopeless groups
         print(k, "groups", len(tr[0]["lp"]) - 1, "hopeless", tr[0]["hid"], "leaves", len(tr))
 
     # triangular matrix power: mtxType L / U on the lower / upper triangle

@@ -166,3 +166,29 @@ def test_mlp_oracle_gradient_matches_finite_differences():
         fd[i] = (mlp_ref.loss_grad(tp, X, T, dims)[0] - mlp_ref.loss_grad(tm, X, T, dims)[0]) / (2 * h)
     assert np.max(np.abs(fd - g)) <= 1e-6 * max(1.0, np.max(np.abs(g)))
     assert loss > 0
+
+
+def test_mpk_recursion_permutation_matches_reference(golden, mats):
+    """The reference's default MPK partition recurses once into every
+    hopeless group (RACE_MAX_RECURSION_STAGES unset: one stage past the
+    cut-off list, matrixPowerRecursive.cpp:50-60). Its permutation is the
+    stage-0 BFS permutation followed, per hopeless group h of the level
+    groups lp, by a BFS of the group's rows from its first row through the
+    boundary groups h-w..h+w (w = ceil(p/2)-1, matrixPowerRecursive.cpp:
+    199-298), each region then sorted by level. The oracle restates this and
+    must give the reference's permutation."""
+    import math
+
+    from cases import HOPELESS_CASES, key_hopeless
+    for m, p, c in HOPELESS_CASES:
+        A = mats[m]
+        k = key_hopeless(m, p, c)
+        assert int(golden[k + "__leaves"]) == 1 + len(golden[k + "__hid"])  # one recursion stage
+        tp, ti, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+        lp = golden[k + "__lp"]
+        w = math.ceil(p / 2) - 1
+        for h in golden[k + "__hid"]:
+            regions = [(int(lp[h + r]), int(lp[h + r + 1])) for r in range(-w, w + 1)
+                       if r != 0 and lp[h + r + 1] > lp[h + r]]
+            tp, ti, _, _, _ = orc.traverse_boundary(A, int(lp[h]), int(lp[h + 1]), regions, tp, ti)
+        np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
