@@ -300,6 +300,17 @@ int race_mpk_stage_partition(const int *levelRow, const int *levelNnz, int total
                              long long graphNnz, int power, double cacheSize, double safety, int cutoff, int *groupPtr,
                              int *hopeless, int cap, int *numGroups, int *numHopeless);
 
+/* Host-only: the permutation of the MPK partition's recursion into its
+ * hopeless groups (one stage, the reference's default;
+ * matrixPowerRecursive.cpp:156-298): for each hopeless group, a BFS of its
+ * rows through the boundary groups ceil(power/2)-1 on either side, then the
+ * group and those boundary groups sorted by level. rowPtr/col: the
+ * traversal pattern (original rows); totalPerm/totalInvPerm (n each, new
+ * index -> original row and back) are updated in place; groupPtr and
+ * hopeless as from race_mpk_stage_partition. */
+int race_mpk_recursion_permute(int n, const int *rowPtr, const int *col, int *totalPerm, int *totalInvPerm,
+                               const int *groupPtr, int numGroups, const int *hopeless, int numHopeless, int power);
+
 /* Host-only: RACE's level recursion (level_recursion.cpp:149-376, the
  * zone tree of race_color) with the traversal supplied by the caller instead
  * of the engine's GPU BFS. `trav` runs one traversal of rows [lo,hi) of the

@@ -91,12 +91,31 @@ void Engine::powerPrepare(int hp, double cacheSize, double safety, const std::st
             prev = l;
         }
     }
-    if (hopeless && mtxType == "N")
-        throw Error(RACE_ERR_NOT_IMPLEMENTED,
-                    "consecutive levels exceed the cache budget beyond the cut-off (a hopeless region); recursive "
-                    "MPK partitioning is not built: raise cacheSize or RACE_CACHE_VIOLATION_CUTOFF, or set "
-                    "RACE_MAX_RECURSION_STAGES=0 (race_params.max_recursion_stages) to partition without "
-                    "recursion as the reference then does");
+    if (hopeless) {
+        // Hopeless regions: the reference's stage-0 groups around them
+        // (stagePartition) and, for mtxType N, its one-stage recursion, which
+        // reorders the rows of each hopeless group and of its boundary groups
+        // (recursePermutation). Every group keeps its row range, so the
+        // MPK's neighbour-group dependencies still hold.
+        if (mtxType == "N" && maxRec > 1)
+            throw Error(RACE_ERR_NOT_IMPLEMENTED,
+                        "MPK recursion deeper than one stage (RACE_MAX_RECURSION_STAGES > 1 or a list of cut-offs) is "
+                        "not built");
+        const StagePartition sp = stagePartition(ld, 0, P, n, nnz, cacheSize, safety, cutoff);
+        if (mtxType == "N" && !sp.hopeless.empty()) {
+            if (!recursePermutation(n, hRowPtr.data(), hCol.data(), hPerm, hInvPerm, sp.groupPtr, sp.hopeless, P))
+                throw Error(RACE_ERR_GRAPH_TRAVERSAL, "rows of a hopeless group went missing in its traversal");
+            dPerm.upload(hPerm.data(), n, stream);
+            dInvPerm.upload(hInvPerm.data(), n, stream);
+            RACE_CUDA(cudaStreamSynchronize(stream));
+            powerLevelsCached = false;  // the BFS levels no longer follow the row order
+        }
+        groupPtr = sp.groupPtr;
+        unlockRow = sp.unlockRow;
+        dangerRow = sp.dangerRow;
+        powerReady = true;
+        return;
+    }
     // consolidatePartition without hopeless regions (matrixPower.cpp:685-883)
     groupPtr.assign(1, levelPtr[0]);
     unlockRow.assign(1, L > 0 ? levelPtr[std::min(1, L)] : 0);
@@ -522,6 +541,23 @@ int race_mpk_stage_partition(const int *levelRow, const int *levelNnz, int total
             memcpy(groupPtr, sp.groupPtr.data(), sizeof(int) * sp.groupPtr.size());
             if (!sp.hopeless.empty()) memcpy(hopeless, sp.hopeless.data(), sizeof(int) * sp.hopeless.size());
         }
+    });
+}
+
+int race_mpk_recursion_permute(int n, const int *rowPtr, const int *col, int *totalPerm, int *totalInvPerm,
+                               const int *groupPtr, int numGroups, const int *hopeless, int numHopeless, int power) {
+    if (n < 0 || !rowPtr || !col || !totalPerm || !totalInvPerm || !groupPtr || numGroups < 0 || numHopeless < 0 ||
+        (numHopeless > 0 && !hopeless) || power < 1 || groupPtr[0] < 0 || groupPtr[numGroups] > n)
+        return RACE_ERR_INVALID_ARG;
+    for (int g = 0; g < numGroups; ++g)
+        if (groupPtr[g + 1] < groupPtr[g]) return RACE_ERR_INVALID_ARG;
+    return guard(nullptr, [&] {
+        std::vector<int> tp(totalPerm, totalPerm + n), ti(totalInvPerm, totalInvPerm + n);
+        std::vector<int> gp(groupPtr, groupPtr + numGroups + 1), hid(hopeless, hopeless + numHopeless);
+        if (!race::recursePermutation(n, rowPtr, col, tp, ti, gp, hid, power))
+            throw Error(RACE_ERR_GRAPH_TRAVERSAL, "rows of a hopeless group went missing in its traversal");
+        memcpy(totalPerm, tp.data(), sizeof(int) * n);
+        memcpy(totalInvPerm, ti.data(), sizeof(int) * n);
     });
 }
 

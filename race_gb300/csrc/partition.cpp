@@ -189,4 +189,92 @@ StagePartition stagePartition(const LevelData &ld, int startRow, int power, int 
     return sp;
 }
 
+bool recursePermutation(int n, const int *rowPtr, const int *col, std::vector<int> &totalPerm,
+                        std::vector<int> &totalInvPerm, const std::vector<int> &groupPtr,
+                        const std::vector<int> &hopeless, int power) {
+    const int G = (int)groupPtr.size() - 1;
+    const int w = (power + 1) / 2 - 1;  // ceil(power/2) - 1 (workingBoundaryLength_base)
+    std::vector<int> level(n, -1);
+    std::vector<char> seen(n, 0), boundary(n, 0);
+    std::vector<int> frontier, next, sorted;
+    for (int h : hopeless) {
+        if (h < 0 || h >= G) return false;
+        const int lo = groupPtr[h], hi = groupPtr[h + 1];
+        std::vector<std::pair<int, int>> regions{{lo, hi}};
+        for (int r = -w; r <= w; ++r) {
+            const int g = h + r;
+            if (r == 0 || g < 0 || g >= G || groupPtr[g + 1] <= groupPtr[g]) continue;
+            regions.emplace_back(groupPtr[g], groupPtr[g + 1]);
+            for (int i = groupPtr[g]; i < groupPtr[g + 1]; ++i) boundary[i] = 1;
+        }
+        // BFS from lo (the rows are new indices; their neighbours are looked
+        // up through the running permutation)
+        int counted = 0, lvl = 0, restart = lo;
+        frontier.clear();
+        if (lo < hi) {
+            frontier.push_back(lo);
+            seen[lo] = 1;
+            level[lo] = 0;
+            counted = 1;
+        }
+        while (!frontier.empty()) {
+            ++lvl;
+            next.clear();
+            for (int u : frontier) {
+                const int pu = totalPerm[u];
+                for (int idx = rowPtr[pu]; idx < rowPtr[pu + 1]; ++idx) {
+                    if (col[idx] >= n) continue;
+                    const int c = totalInvPerm[col[idx]];
+                    if (seen[c]) continue;
+                    const bool inside = c >= lo && c < hi;
+                    if (!inside && !boundary[c]) continue;
+                    seen[c] = 1;
+                    level[c] = lvl;
+                    next.push_back(c);
+                    counted += inside;
+                }
+            }
+            frontier.swap(next);
+            if (frontier.empty() && counted != hi - lo) {
+                while (restart < hi && seen[restart]) ++restart;
+                if (restart == hi) return false;
+                seen[restart] = 1;
+                level[restart] = lvl;
+                frontier.push_back(restart);
+                ++counted;
+            }
+        }
+        int levels = lvl;
+        bool untouched = false;
+        for (size_t k = 1; k < regions.size(); ++k)
+            for (int i = regions[k].first; i < regions[k].second; ++i)
+                if (!seen[i]) {
+                    level[i] = lvl;
+                    untouched = true;
+                }
+        levels += untouched ? 1 : 0;
+        levels = std::max(levels, 1);
+        // stable sort of each region by level, composed into the permutation
+        for (const auto &rg : regions) {
+            const int a = rg.first, b = rg.second;
+            std::vector<int> start(levels + 1, 0);
+            for (int i = a; i < b; ++i) ++start[level[i] + 1];
+            for (int l = 0; l < levels; ++l) start[l + 1] += start[l];
+            sorted.assign(b - a, 0);
+            for (int i = a; i < b; ++i) sorted[start[level[i]]++] = totalPerm[i];
+            for (int i = a; i < b; ++i) {
+                totalPerm[i] = sorted[i - a];
+                totalInvPerm[totalPerm[i]] = i;
+            }
+        }
+        for (const auto &rg : regions)
+            for (int i = rg.first; i < rg.second; ++i) {
+                seen[i] = 0;
+                boundary[i] = 0;
+                level[i] = -1;
+            }
+    }
+    return true;
+}
+
 }  // namespace race

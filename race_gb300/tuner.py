@@ -11,7 +11,9 @@ of power p) and learns from the search:
 * ``CONFIGS``: power per block p in {1, 2, 4, 8} times cache budget in
   {8, 32, 128, 512} MB (p = 1 takes one budget: it has no blocking);
 * ``search``: times every config on the engine (median of repetitions);
-  configs whose partition RACE rejects (hopeless regions) are infeasible;
+  configs whose partition the engine refuses are infeasible (the committed
+  searches predate the partition of hopeless regions: 3 of their 3,900 MPK
+  entries are marked infeasible for that reason);
 * ``matrix_features`` / ``config_features``: 24 structural features of the
   matrix (sizes, row lengths, index distances, BFS level profile from row 0,
   RACE's root) and 8 of the config, 32 inputs in total;

@@ -48,16 +48,13 @@ def test_power_partition_matches_reference(golden, mats, m, p, c):
 @pytest.mark.parametrize("m,p,c", POWER_FLAT_CASES)
 def test_power_partition_without_recursion(golden, mats, m, p, c):
     """Consecutive levels over the cache cut-off: the reference recurses into
-    the hopeless region by default, which is not built here (RACEColor
-    returns RACE_ERR_NOT_IMPLEMENTED); with max_recursion_stages = 0 both
-    partition without recursion, and the permutation, the level groups and
-    the MPK agree."""
+    the hopeless region by default (tests/test_zz_recursion.py); with
+    max_recursion_stages = 0 both partition without recursion, and the
+    permutation, the level groups and the MPK agree."""
     A = mats[m]
     k = key_power_flat(m, p, c)
     assert str(golden[k + "__digest"]) == digest(A)
     assert int(golden[k + "__default_leaves"]) > 1 and int(golden[k + "__leaves"]) == 1
-    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
-    assert rc.RACEColor(p, c) == 10  # RACE_ERR_NOT_IMPLEMENTED
     rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True, params={"max_recursion_stages": 0})
     assert rc.RACEColor(p, c) == 0
     np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])

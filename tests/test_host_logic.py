@@ -504,3 +504,25 @@ def test_stage_partition_matches_reference(golden, mats):
         order = lens if tri == "L" else lens[::-1]
         gp, hid = _stage_partition(np.ones(T.n, np.int32), order, T.n, T.nnz, p, c)
         np.testing.assert_array_equal(gp, golden[key_power_tri(m, tri, p, c) + "__lp"])
+
+
+def test_mpk_recursion_matches_reference(golden, mats):
+    """The engine's partition of a matrix with hopeless regions, computed on
+    the host from the oracle's stage-0 BFS: level groups and hopeless groups
+    (race_mpk_stage_partition) and the recursion's permutation
+    (race_mpk_recursion_permute) equal the reference's default partition."""
+    from cases import HOPELESS_CASES, key_hopeless
+    L = _lib.lib()
+    for m, p, c in HOPELESS_CASES:
+        A = mats[m]
+        k = key_hopeless(m, p, c)
+        tp, ti, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+        gp, hid = _stage_partition(lr, ln, A.n, A.nnz, p, c)
+        np.testing.assert_array_equal(gp, golden[k + "__lp"])
+        rp, cl = np.ascontiguousarray(A.row_ptr, np.int32), np.ascontiguousarray(A.col, np.int32)
+        tp, ti = np.ascontiguousarray(tp, np.int32), np.ascontiguousarray(ti, np.int32)
+        hid = np.ascontiguousarray(hid, np.int32)
+        _lib.check(L.race_mpk_recursion_permute(A.n, rp.ctypes.data, cl.ctypes.data, tp.ctypes.data, ti.ctypes.data,
+                                                gp.ctypes.data, gp.size - 1, hid.ctypes.data, hid.size, p))
+        np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
+        np.testing.assert_array_equal(ti[tp], np.arange(A.n))

@@ -1,0 +1,55 @@
+"""MPK partitions with hopeless regions at the default settings, on the GPU:
+the engine's RACEColor(p, cacheSize) gives the reference's level groups and,
+after its one-stage recursion into the hopeless groups, the reference's
+permutation; the MPK on that partition equals p sequential SpMVs bit for
+bit. (The host parts are checked on the CPU in test_host_logic.py; this file
+runs last among the GPU tests.)"""
+import numpy as np
+import pytest
+
+from cases import HOPELESS_CASES, digest, key_hopeless
+from oracle import oracle as orc
+from race_gb300 import matgen
+
+torch = pytest.importorskip("torch")
+
+from race_gb300 import interface as ri  # noqa: E402
+
+HUB_ROW_LEN = 256  # rows longer than this are summed by a warp (mpk.cu kHubRowLen)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,p,c", HOPELESS_CASES)
+def test_default_partition_with_hopeless_regions(golden, mats, m, p, c):
+    A = mats[m]
+    k = key_hopeless(m, p, c)
+    assert str(golden[k + "__digest"]) == digest(A)
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, c) == 0
+    np.testing.assert_array_equal(rc.getPowerGroups(), golden[k + "__lp"])
+    perm, inv = rc.getPerm(), rc.getInvPerm()
+    np.testing.assert_array_equal(perm, golden[k + "__perm"])
+    np.testing.assert_array_equal(inv[perm], np.arange(A.n))
+    P = A.permuted(perm, inv)
+    x0 = matgen.uniform_vector(A.n, 0)
+    Y = orc.mpk_plain(P, x0, p)
+    x = torch.zeros((p + 1) * A.n, dtype=torch.float64, device="cuda")
+    x[: A.n] = torch.tensor(x0, device="cuda")
+    fid = rc.registerFunction(ri.MPK, ri.Operands(ri.DeviceCsr.from_csr(P), x), power=p)
+    assert fid >= 0
+    assert rc.executeFunction(fid) == 0
+    got = x.cpu().numpy().reshape(p + 1, A.n)
+    hubs = np.diff(P.row_ptr) > HUB_ROW_LEN
+    if not hubs.any():
+        np.testing.assert_array_equal(got, Y)
+    else:
+        for kk in range(1, p + 1):
+            assert np.max(np.abs(got[kk] - Y[kk])) <= 1e-12 * np.max(np.abs(Y[kk]))
+
+
+@pytest.mark.gpu
+def test_deeper_recursion_is_refused(mats):
+    """More than one recursion stage is not built."""
+    A = mats["band_5k"]
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True, params={"max_recursion_stages": 2})
+    assert rc.RACEColor(8, 3000) == 10  # RACE_ERR_NOT_IMPLEMENTED
