@@ -138,14 +138,18 @@ def search(A, reps: int = 5, warmup: int = 2, stream=None) -> np.ndarray:
     from . import interface as ri
     rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
     times = np.full(len(CONFIGS), np.inf)
-    P = None
+    perm = None
+    x0 = torch.tensor(matgen.uniform_vector(A.n, 0), device="cuda")
     for ci, (p, c) in enumerate(CONFIGS):
         if rc.RACEColor(p, c * 1e6) != 0:
             continue
-        if P is None:  # the permutation is fixed by the first partition
-            P = A.permuted(rc.getPerm(), rc.getInvPerm())
+        # The permutation normally stays the one of the first partition; a
+        # partition with hopeless regions reorders rows inside groups.
+        cur = rc.getPerm()
+        if perm is None or not np.array_equal(cur, perm):
+            perm = cur
+            P = A.permuted(perm, rc.getInvPerm())
             dm = ri.DeviceCsr.from_csr(P, "cuda", torch.float64)
-            x0 = torch.tensor(matgen.uniform_vector(A.n, 0), device="cuda")
         x = torch.zeros((p + 1) * A.n, dtype=torch.float64, device="cuda")
         fid = rc.registerFunction(ri.MPK, ri.Operands(dm, x), power=p)
         x[: A.n].copy_(x0)
