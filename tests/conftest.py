@@ -35,3 +35,31 @@ def mats():
             return _MATS[name]
 
     return _M()
+
+
+@pytest.fixture(scope="session")
+def fnlib(tmp_path_factory):
+    """tests/device_functors.cu (functors through the engine's schedule,
+    include/race_gb300_device.cuh) built with nvcc for sm_103a and linked
+    against the engine library."""
+    import ctypes as C
+    import subprocess
+
+    from race_gb300 import _lib, build
+    try:
+        nvcc = build._nvcc()
+    except RuntimeError:
+        pytest.skip("no nvcc")
+    out = tmp_path_factory.mktemp("fn") / "libdevice_functors.so"
+    lib_path = _lib.LIB_PATH
+    subprocess.check_call([nvcc, "-std=c++17", "-O3", "--fmad=false", *build.ARCH, "-I", str(ROOT / "include"),
+                           "-shared", "-Xcompiler", "-fPIC", "--cudart", "shared",
+                           str(ROOT / "tests" / "device_functors.cu"), str(lib_path), "-Xlinker",
+                           f"-rpath,{lib_path.parent}", "-o", str(out)])
+    _lib.lib()  # the engine library first, so both refer to one copy
+    L = C.CDLL(str(out))
+    vp = C.c_void_p
+    L.fn_gs.argtypes = [vp, vp, vp, vp, vp, vp, C.c_int]
+    L.fn_mpk.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]
+    L.fn_count_subpower.argtypes = [vp, vp, C.c_int, C.c_int, vp]
+    return L

@@ -40,6 +40,21 @@ struct MpkFn {
     }
 };
 
+// MAT_NUM_VEC_ACCESSES_w_subPower (examples/src/helpers/sparsemat.cpp:1399-1412)
+// with the sub-power count as a member: every row is visited once per
+// (pow, subPow), in order; a visit out of order counts an error.
+struct CountFn {
+    double *x;
+    int subPower;
+    int *errors;
+    __device__ void operator()(int start, int end, int pow, int subPow) const {
+        for (int row = start; row < end; ++row) {
+            x[row] += 1;
+            if (x[row] != (double)((pow - 1) * subPower + subPow)) atomicAdd(errors, 1);
+        }
+    }
+};
+
 int finish(int rc) {
     if (rc == RACE_SUCCESS && cudaDeviceSynchronize() != cudaSuccess) rc = RACE_ERR_CUDA;
     return rc;
@@ -57,6 +72,12 @@ extern "C" int fn_gs(race_engine *e, const int *rowPtr, const int *col, const do
 extern "C" int fn_mpk(race_engine *e, const int *rowPtr, const int *col, const double *val, double *x, int n, int power,
                       int rowsPerCall) {
     RACE::gb300::DevicePowerFunction<MpkFn> f(e, MpkFn{rowPtr, col, val, x, n}, power, rowsPerCall);
+    if (f.status() != RACE_SUCCESS) return f.status();
+    return finish(f.execute(0));
+}
+
+extern "C" int fn_count_subpower(race_engine *e, double *x, int power, int subPower, int *errors) {
+    RACE::gb300::DevicePowerFunction<CountFn> f(e, CountFn{x, subPower, errors}, power, 32, subPower);
     if (f.status() != RACE_SUCCESS) return f.status();
     return finish(f.execute(0));
 }

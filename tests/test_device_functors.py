@@ -3,8 +3,8 @@
 host callbacks: the example GS body as a colored functor must equal the
 sequential walk of the engine's phases bit for bit, and the MPK body as a
 power functor must equal p sequential SpMVs bit for bit. The functors live
-in tests/device_functors.cu, compiled here with nvcc for sm_103a."""
-import ctypes as C
+in tests/device_functors.cu, compiled with nvcc for sm_103a (the fnlib
+fixture of conftest.py)."""
 import pathlib
 import subprocess
 
@@ -33,20 +33,6 @@ def test_device_header_compiles(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
-@pytest.fixture(scope="module")
-def fnlib(tmp_path_factory):
-    out = tmp_path_factory.mktemp("fn") / "libdevice_functors.so"
-    lib_path = _lib.LIB_PATH
-    subprocess.check_call([_nvcc(), *NVCC, "-shared", "-Xcompiler", "-fPIC", "--cudart", "shared", str(SRC),
-                           str(lib_path), "-Xlinker", f"-rpath,{lib_path.parent}", "-o", str(out)])
-    _lib.lib()  # the engine library first, so both refer to one copy
-    L = C.CDLL(str(out))
-    vp = C.c_void_p
-    L.fn_gs.argtypes = [vp, vp, vp, vp, vp, vp, C.c_int]
-    L.fn_mpk.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]
-    return L
-
-
 def test_device_functions_link_and_reject_a_null_engine(fnlib):
     """The functor library links against the engine and loads; without an
     engine the schedule queries fail before any launch."""
@@ -54,6 +40,7 @@ def test_device_functions_link_and_reject_a_null_engine(fnlib):
     assert fnlib.fn_gs(None, None, None, None, None, None, 0) == bad
     assert fnlib.fn_mpk(None, None, None, None, None, 10, 2, 32) == bad
     assert fnlib.fn_mpk(None, None, None, None, None, 10, 0, 32) == bad  # power below 1
+    assert fnlib.fn_count_subpower(None, None, 2, 2, None) == bad
 
 
 @pytest.mark.gpu

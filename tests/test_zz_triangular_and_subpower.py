@@ -1,0 +1,54 @@
+"""Matrix-power cases run through device functors on the GPU (after the
+other GPU tests): triangular partitions (mtxType L / U) and their MPK, and
+sub-powers. Their host parts are checked on the CPU (test_oracle.py,
+test_device_functors.py)."""
+import numpy as np
+import pytest
+
+from cases import POWER_TRI_CASES, digest, key_power_tri, triangle
+from oracle import oracle as orc
+from race_gb300 import matgen
+
+torch = pytest.importorskip("torch")
+
+from race_gb300 import interface as ri  # noqa: E402
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,tri,p,c", POWER_TRI_CASES)
+def test_triangular_partition_and_functor_mpk(golden, mats, fnlib, m, tri, p, c):
+    """The engine's L / U partition equals the reference's, and the MPK body
+    as a device power functor on the permuted triangle (lower triangular in
+    RACE's order) equals p sequential SpMVs bit for bit."""
+    T = triangle(mats[m], tri)
+    k = key_power_tri(m, tri, p, c)
+    assert str(golden[k + "__digest"]) == digest(T)
+    rc = ri.Interface(T.n, 1, ri.POWER, T.row_ptr, T.col, symm_hint=True)
+    assert rc.RACEColor(p, c, mtxType=tri) == 0
+    np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
+    np.testing.assert_array_equal(rc.getPowerGroups(), golden[k + "__lp"])
+    P = T.permuted(rc.getPerm(), rc.getInvPerm())
+    dm = ri.DeviceCsr.from_csr(P)
+    x0 = matgen.uniform_vector(T.n, 0)
+    Y = orc.mpk_plain(P, x0, p)
+    x = torch.zeros((p + 1) * T.n, dtype=torch.float64, device="cuda")
+    x[: T.n] = torch.tensor(x0, device="cuda")
+    assert fnlib.fn_mpk(rc._h, dm.row_ptr.data_ptr(), dm.col.data_ptr(), dm.val.data_ptr(), x.data_ptr(), T.n,
+                        p, 32) == 0
+    np.testing.assert_array_equal(x.cpu().numpy().reshape(p + 1, T.n), Y)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,p,sub,c", [("st27_24", 4, 2, 2e6), ("aniso5_120x90", 2, 3, 5e5)])
+def test_subpower_functor_visits_every_row_in_order(mats, fnlib, m, p, sub, c):
+    """registerFunction(f, args, power, subPower) counterpart: every row is
+    called once per (pow, subPow), in order (the reference example's
+    counting kernel)."""
+    A = mats[m]
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, c, highestSubPower=sub) == 0
+    x = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert fnlib.fn_count_subpower(rc._h, x.data_ptr(), p, sub, err.data_ptr()) == 0
+    assert int(err.item()) == 0
+    assert bool((x == p * sub).all())
