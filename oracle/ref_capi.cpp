@@ -198,6 +198,27 @@ extern "C" {
 
 /* ---------------- coloring ---------------- */
 
+/* Coloring of a graph whose running permutation starts at initPerm (the
+ * Interface ctor's initPerm/initInvPerm, graph_SoA.cpp:63-79); NULL for the
+ * identity. */
+void *refc_color_init(int n, int *rowPtr, int *col, int dist, int nthreads, int symm_hint, int d2type, int lbtarget,
+                      int *initPerm, int *initInvPerm) {
+    Quiet q;
+    ColorHandle *h = new ColorHandle;
+    h->n = n;
+    h->requested = nthreads;
+    h->dist = (RACE::dist)dist;
+    h->graph = new RACE::Graph(n, n, rowPtr, col, h->dist, symm_hint != 0, initPerm, initInvPerm);
+    LevelRecursion lr(h->graph, nthreads, h->dist, (RACE::d2Method)d2type, (RACE::LBTarget)lbtarget);
+    lr.levelBalancing();
+    h->available = lr.getAvailableThreads();
+    int len;
+    lr.getPerm(&h->perm, &len);
+    lr.getInvPerm(&h->invPerm, &len);
+    h->tree = lr.getZoneTree();
+    return h;
+}
+
 void *refc_color(int n, int *rowPtr, int *col, int dist, int nthreads, int symm_hint, int d2type, int lbtarget) {
     Quiet q;
     ColorHandle *h = new ColorHandle;

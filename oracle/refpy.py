@@ -32,6 +32,8 @@ def lib():
         L = C.CDLL(str(LIB_PATH))
         L.refc_color.restype = C.c_void_p
         L.refc_color.argtypes = [C.c_int, IP, IP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.refc_color_init.restype = C.c_void_p
+        L.refc_color_init.argtypes = [C.c_int, IP, IP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, IP, IP]
         L.refc_color_free.argtypes = [C.c_void_p]
         L.refc_color_perm.argtypes = [C.c_void_p, IP, IP]
         L.refc_color_threads.argtypes = [C.c_void_p]
@@ -134,10 +136,18 @@ class RefInterface:
 class RefColor:
     """Reference coloring of one matrix (RACE::Interface with dist ONE/TWO)."""
 
-    def __init__(self, csr, dist: int, nthreads: int, symm_hint: bool = True, d2type: int = 0, lbtarget: int = 1):
+    def __init__(self, csr, dist: int, nthreads: int, symm_hint: bool = True, d2type: int = 0, lbtarget: int = 1,
+                 init_perm=None):
         self.n = csr.n
         self._rp, self._col = _i32(csr.row_ptr), _i32(csr.col)
-        self.h = lib().refc_color(csr.n, self._rp, self._col, dist, nthreads, int(symm_hint), d2type, lbtarget)
+        if init_perm is None:
+            self.h = lib().refc_color(csr.n, self._rp, self._col, dist, nthreads, int(symm_hint), d2type, lbtarget)
+        else:
+            self._ip = _i32(init_perm)
+            self._iip = np.empty_like(self._ip)
+            self._iip[self._ip] = np.arange(csr.n, dtype=np.int32)
+            self.h = lib().refc_color_init(csr.n, self._rp, self._col, dist, nthreads, int(symm_hint), d2type,
+                                           lbtarget, self._ip, self._iip)
 
     def close(self):
         if self.h:

@@ -56,6 +56,19 @@ COLOR_CASES = [
 COLOR3_CASES = [("lap7_16", 16), ("band_5k", 32), ("plaw_3k", 16), ("islands_330", 8), ("aniso5_120x90", 48)]
 
 
+# colorings that start from an initial permutation (the Interface ctor's
+# initPerm): (matrix, dist, nthreads); the permutation is a seeded shuffle
+COLOR_INIT_CASES = [("lap7_16", 2, 16), ("aniso9_100x80", 1, 16), ("plaw_3k", 2, 16), ("islands_330", 1, 8)]
+
+
+def init_perm(n: int, seed: int = 5) -> np.ndarray:
+    return np.random.default_rng(seed).permutation(n).astype(np.int32)
+
+
+def key_color_init(m, d, t):
+    return f"colorinit__{m}__d{d}__t{t}"
+
+
 def key_color3(m, t):
     return f"color3__{m}__t{t}"
 

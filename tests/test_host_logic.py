@@ -409,12 +409,16 @@ def test_three_block_phases_reproduce_reference(golden, mats, m, t):
 
 
 
-def _zone_tree_host(A, d, t, d2type, cap):
+def _zone_tree_host(A, d, t, d2type, cap, init=None):
     """The engine's level recursion (race_zone_tree_host) driven by the
-    oracle's traversal, which keeps the running permutation here."""
+    oracle's traversal, which keeps the running permutation here (starting
+    from `init`, the identity by default)."""
     L = _lib.lib()
     lens = np.diff(A.row_ptr).astype(np.int64)
-    state = {"tp": np.arange(A.n, dtype=np.int32), "ti": np.arange(A.n, dtype=np.int32), "err": None}
+    tp0 = np.arange(A.n, dtype=np.int32) if init is None else np.ascontiguousarray(init, np.int32)
+    ti0 = np.empty_like(tp0)
+    ti0[tp0] = np.arange(A.n, dtype=np.int32)
+    state = {"tp": tp0, "ti": ti0, "err": None}
 
     @_lib.TRAVERSE_FN
     def trav(user, lo, hi, lr_ptr, ln_ptr, lcap, total):
@@ -526,3 +530,19 @@ def test_mpk_recursion_matches_reference(golden, mats):
                                                 gp.ctypes.data, gp.size - 1, hid.ctypes.data, hid.size, p))
         np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
         np.testing.assert_array_equal(ti[tp], np.arange(A.n))
+
+
+def test_level_recursion_from_an_initial_permutation(golden, mats):
+    """Coloring that starts from an initial permutation (the Interface
+    ctor's initPerm, graph_SoA.cpp:63-79): the engine's level recursion
+    gives the reference's zone tree, thread count and composed permutation."""
+    from cases import COLOR_INIT_CASES, key_color_init
+    for m, d, t in COLOR_INIT_CASES:
+        A = mats[m]
+        k = key_color_init(m, d, t)
+        assert str(golden[k + "__digest"]) == digest(A)
+        gold = golden[k + "__tree"]
+        tree, avail, perm = _zone_tree_host(A, d, t, 0, 2 * gold.size + 1024, init=golden[k + "__init"])
+        np.testing.assert_array_equal(tree, gold, err_msg=k)
+        assert avail == int(golden[k + "__threads"])
+        np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)

@@ -1,13 +1,13 @@
-"""Distance-2 coloring with RACE::THREE_BLOCK on the GPU: the engine's
-permutation, zone tree and thread count equal the reference's, and its
-bit-exact sweeps reproduce the reference executor's outputs. (The load
-balancer, the level recursion and the phase semantics for THREE_BLOCK are
-checked on the CPU in test_host_logic.py; this file runs after the other
-GPU tests.)"""
+"""Coloring variants on the GPU, against the reference: distance-2 coloring
+with RACE::THREE_BLOCK (permutation, zone tree, thread count, and bit-exact
+sweeps reproducing the reference executor's outputs) and coloring from an
+initial permutation. (Their host parts, the load balancer, the level
+recursion and the phase semantics, are checked on the CPU in
+test_host_logic.py; this file runs after the other GPU tests.)"""
 import numpy as np
 import pytest
 
-from cases import COLOR3_CASES, digest, key_color3
+from cases import COLOR3_CASES, COLOR_INIT_CASES, digest, key_color3, key_color_init
 from race_gb300 import matgen
 
 torch = pytest.importorskip("torch")
@@ -50,3 +50,22 @@ def test_three_block_coloring_and_sweeps(golden, mats, m, t):
             np.testing.assert_array_equal(out, ref, err_msg=name)
         else:  # rows above 512 entries run with a warp reduction
             assert np.max(np.abs(out - ref)) <= 1e-12 * np.max(np.abs(ref)), name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,d,t", COLOR_INIT_CASES)
+def test_coloring_from_an_initial_permutation(golden, mats, m, d, t):
+    """Interface(..., initPerm, initInvPerm): the coloring starts from the
+    caller's permutation, and the permutation, zone tree and thread count
+    equal the reference's."""
+    A = mats[m]
+    k = key_color_init(m, d, t)
+    ip0 = golden[k + "__init"]
+    inv0 = np.empty_like(ip0)
+    inv0[ip0] = np.arange(A.n, dtype=np.int32)
+    rc = ri.Interface(A.n, t, d, A.row_ptr, A.col, symm_hint=True, initPerm=ip0, initInvPerm=inv0)
+    assert rc.RACEColor() == 0
+    np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
+    np.testing.assert_array_equal(rc.getZoneTreeFlat(), golden[k + "__tree"])
+    assert rc.getNumThreads() == int(golden[k + "__threads"])
+    assert rc.getEfficiency() == float(golden[k + "__eff"])
