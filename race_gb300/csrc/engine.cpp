@@ -239,6 +239,9 @@ race::Params toParams(const race_params *p) {
     race::Params q;
     q.effVec.assign(p->eff, p->eff + std::max(1, std::min(p->n_eff, 16)));
     q.lvlThreads.assign(p->lvl_threads, p->lvl_threads + std::max(0, std::min(p->n_lvl_threads, 16)));
+    // as from the environment: a thread request for a stage drops its
+    // efficiency threshold to 0 (level_recursion.cpp:86-90)
+    for (size_t lvl = 1; lvl < q.lvlThreads.size() + 1 && lvl < q.effVec.size(); ++lvl) q.effVec[lvl] = 0;
     q.cacheViolationCutoffDefault = p->cache_violation_cutoff > 0 ? p->cache_violation_cutoff : 50;
     q.cacheViolationCutoff.assign(1, q.cacheViolationCutoffDefault);
     q.maxRecStages = p->max_recursion_stages >= 0 ? p->max_recursion_stages : -1;

@@ -69,6 +69,23 @@ def key_color_init(m, d, t):
     return f"colorinit__{m}__d{d}__t{t}"
 
 
+# colorings with RACE's environment knobs (level_recursion.cpp:48-90: a
+# per-stage efficiency list after the default 40, and per-stage thread
+# requests that drop that stage's efficiency to 0): (matrix, dist, nthreads,
+# environment)
+COLOR_ENV_CASES = [
+    ("lap7_32", 2, 64, {"RACE_EFFICIENCY": "60,30"}),
+    ("lap7_32", 1, 256, {"RACE_EFFICIENCY": "10"}),
+    ("band_5k", 2, 32, {"RACE_THREADS": "4", "RACE_EFFICIENCY": "40"}),
+    ("plaw_3k", 1, 32, {"RACE_THREADS": "8,2", "RACE_EFFICIENCY": "50,50"}),
+    ("lap7_16", 2, 16, {"RACE_EFFICIENCY": "80"}),
+]
+
+
+def key_color_env(m, d, t, env):
+    return f"colorenv__{m}__d{d}__t{t}__" + "_".join(f"{k}={v}" for k, v in sorted(env.items()))
+
+
 def key_color3(m, t):
     return f"color3__{m}__t{t}"
 

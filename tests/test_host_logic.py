@@ -409,7 +409,7 @@ def test_three_block_phases_reproduce_reference(golden, mats, m, t):
 
 
 
-def _zone_tree_host(A, d, t, d2type, cap, init=None):
+def _zone_tree_host(A, d, t, d2type, cap, init=None, params=None):
     """The engine's level recursion (race_zone_tree_host) driven by the
     oracle's traversal, which keeps the running permutation here (starting
     from `init`, the identity by default)."""
@@ -441,8 +441,8 @@ def _zone_tree_host(A, d, t, d2type, cap, init=None):
 
     buf = np.zeros(cap, np.int32)
     tlen, avail = C.c_int(), C.c_int()
-    rc = L.race_zone_tree_host(A.n, t, d, d2type, 1, None, trav, rnnz, None, buf.ctypes.data, cap, C.byref(tlen),
-                               C.byref(avail))
+    rc = L.race_zone_tree_host(A.n, t, d, d2type, 1, None if params is None else C.byref(params), trav, rnnz, None,
+                               buf.ctypes.data, cap, C.byref(tlen), C.byref(avail))
     assert state["err"] is None, state["err"]
     _lib.check(rc)
     assert tlen.value <= cap
@@ -545,4 +545,49 @@ def test_level_recursion_from_an_initial_permutation(golden, mats):
         tree, avail, perm = _zone_tree_host(A, d, t, 0, 2 * gold.size + 1024, init=golden[k + "__init"])
         np.testing.assert_array_equal(tree, gold, err_msg=k)
         assert avail == int(golden[k + "__threads"])
+        np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)
+
+
+def test_level_recursion_under_environment_knobs(golden, mats, monkeypatch):
+    """RACE_EFFICIENCY (per-stage list after the default 40) and
+    RACE_THREADS (per-stage thread requests, which zero that stage's
+    efficiency), read by the engine like the reference
+    (level_recursion.cpp:48-90): same zone tree, threads and permutation."""
+    from cases import COLOR_ENV_CASES, key_color_env
+    for m, d, t, env in COLOR_ENV_CASES:
+        for var in ("RACE_EFFICIENCY", "RACE_THREADS"):
+            monkeypatch.delenv(var, raising=False)
+        for var, val in env.items():
+            monkeypatch.setenv(var, val)
+        A = mats[m]
+        k = key_color_env(m, d, t, env)
+        gold = golden[k + "__tree"]
+        tree, avail, perm = _zone_tree_host(A, d, t, 0, 2 * gold.size + 1024)
+        np.testing.assert_array_equal(tree, gold, err_msg=k)
+        assert avail == int(golden[k + "__threads"]), k
+        np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)
+
+
+def test_level_recursion_with_explicit_params(golden, mats, monkeypatch):
+    """The same knobs passed in race_params instead of the environment
+    (thread requests zero their stages' efficiency there too)."""
+    from cases import COLOR_ENV_CASES, key_color_env
+    for var in ("RACE_EFFICIENCY", "RACE_THREADS", "RACE_CACHE_VIOLATION_CUTOFF", "RACE_MAX_RECURSION_STAGES"):
+        monkeypatch.delenv(var, raising=False)
+    for m, d, t, env in COLOR_ENV_CASES:
+        prm = _lib.race_params()
+        _lib.check(_lib.lib().race_params_from_env(C.byref(prm)))
+        eff = [40] + [int(v) for v in env.get("RACE_EFFICIENCY", "").split(",") if v]
+        thr = [int(v) for v in env.get("RACE_THREADS", "").split(",") if v]
+        prm.n_eff = len(eff)
+        for i, v in enumerate(eff):
+            prm.eff[i] = v
+        prm.n_lvl_threads = len(thr)
+        for i, v in enumerate(thr):
+            prm.lvl_threads[i] = v
+        A = mats[m]
+        k = key_color_env(m, d, t, env)
+        gold = golden[k + "__tree"]
+        tree, avail, perm = _zone_tree_host(A, d, t, 0, 2 * gold.size + 1024, params=prm)
+        np.testing.assert_array_equal(tree, gold, err_msg=k)
         np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)
