@@ -82,6 +82,15 @@ COLOR_ENV_CASES = [
 ]
 
 
+# colorings that balance rows instead of non-zeros (RACE::ROW load-balancer
+# target): (matrix, dist, nthreads)
+COLOR_ROW_CASES = [("lap7_32", 2, 64), ("plaw_3k", 1, 32), ("band_5k", 2, 32), ("aniso5_120x90", 2, 48)]
+
+
+def key_color_row(m, d, t):
+    return f"colorrow__{m}__d{d}__t{t}"
+
+
 def key_color_env(m, d, t, env):
     return f"colorenv__{m}__d{d}__t{t}__" + "_".join(f"{k}={v}" for k, v in sorted(env.items()))
 

@@ -409,7 +409,7 @@ def test_three_block_phases_reproduce_reference(golden, mats, m, t):
 
 
 
-def _zone_tree_host(A, d, t, d2type, cap, init=None, params=None):
+def _zone_tree_host(A, d, t, d2type, cap, init=None, params=None, lb_target=1):
     """The engine's level recursion (race_zone_tree_host) driven by the
     oracle's traversal, which keeps the running permutation here (starting
     from `init`, the identity by default)."""
@@ -441,8 +441,8 @@ def _zone_tree_host(A, d, t, d2type, cap, init=None, params=None):
 
     buf = np.zeros(cap, np.int32)
     tlen, avail = C.c_int(), C.c_int()
-    rc = L.race_zone_tree_host(A.n, t, d, d2type, 1, None if params is None else C.byref(params), trav, rnnz, None,
-                               buf.ctypes.data, cap, C.byref(tlen), C.byref(avail))
+    rc = L.race_zone_tree_host(A.n, t, d, d2type, lb_target, None if params is None else C.byref(params), trav, rnnz,
+                               None, buf.ctypes.data, cap, C.byref(tlen), C.byref(avail))
     assert state["err"] is None, state["err"]
     _lib.check(rc)
     assert tlen.value <= cap
@@ -590,4 +590,20 @@ def test_level_recursion_with_explicit_params(golden, mats, monkeypatch):
         gold = golden[k + "__tree"]
         tree, avail, perm = _zone_tree_host(A, d, t, 0, 2 * gold.size + 1024, params=prm)
         np.testing.assert_array_equal(tree, gold, err_msg=k)
+        np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)
+
+
+def test_level_recursion_balancing_rows(golden, mats, monkeypatch):
+    """LBTarget ROW (balance rows, not non-zeros): the engine's level
+    recursion equals the reference's zone tree, threads and permutation."""
+    from cases import COLOR_ROW_CASES, key_color_row
+    for var in ("RACE_EFFICIENCY", "RACE_THREADS"):
+        monkeypatch.delenv(var, raising=False)
+    for m, d, t in COLOR_ROW_CASES:
+        A = mats[m]
+        k = key_color_row(m, d, t)
+        gold = golden[k + "__tree"]
+        tree, avail, perm = _zone_tree_host(A, d, t, 0, 2 * gold.size + 1024, lb_target=0)
+        np.testing.assert_array_equal(tree, gold, err_msg=k)
+        assert avail == int(golden[k + "__threads"]), k
         np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)
