@@ -91,6 +91,34 @@ def key_color_row(m, d, t):
     return f"colorrow__{m}__d{d}__t{t}"
 
 
+# colorings of matrices whose pattern is not symmetric (a triangle), with
+# symm_hint false, so that RACE first adds the missing transposed entries
+# (makeSymmetricGraph, graph.cpp:47-142): (matrix, triangle, dist, nthreads)
+COLOR_UNSYM_CASES = [("lap7_16", "U", 2, 16), ("plaw_3k", "L", 1, 32), ("aniso9_100x80", "L", 2, 16)]
+
+
+def key_color_unsym(m, tri, d, t):
+    return f"colorunsym__{m}__{tri}__d{d}__t{t}"
+
+
+def symmetrized_pattern(csr):
+    """makeSymmetricGraph: every entry (r, c), c != r, without its pair adds
+    (c, r) after row c's own entries (in the order the entries are met)."""
+    n = csr.n
+    rp = np.asarray(csr.row_ptr, np.int64)
+    col = np.asarray(csr.col, np.int64)
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    present = set(zip(rows.tolist(), col.tolist()))
+    extra = [[] for _ in range(n)]
+    for r, c in zip(rows.tolist(), col.tolist()):
+        if c != r and (c, r) not in present:
+            extra[c].append(r)
+    cols = [np.concatenate([col[rp[r]:rp[r + 1]], np.array(extra[r], np.int64)]) for r in range(n)]
+    nrp = np.concatenate([[0], np.cumsum([len(c) for c in cols])]).astype(np.int32)
+    ncol = np.concatenate(cols).astype(np.int32)
+    return matgen.Csr(n, nrp, ncol, np.ones(ncol.size), csr.name + "_sym")
+
+
 def key_color_env(m, d, t, env):
     return f"colorenv__{m}__d{d}__t{t}__" + "_".join(f"{k}={v}" for k, v in sorted(env.items()))
 

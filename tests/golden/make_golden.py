@@ -25,9 +25,11 @@ sys.path.insert(0, str(ROOT / "tests"))
 os.environ.setdefault("ORACLE_QUIET", "1")
 os.environ.setdefault("OMP_NUM_THREADS", "8")
 
-from cases import (COLOR3_CASES, COLOR_CASES, COLOR_ENV_CASES, COLOR_INIT_CASES, COLOR_ROW_CASES, EXEC_CASES, HOPELESS_CASES, MATRICES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES,  # noqa: E402
+from cases import (COLOR3_CASES, COLOR_CASES, COLOR_ENV_CASES, COLOR_INIT_CASES, COLOR_ROW_CASES,  # noqa: E402
+                   COLOR_UNSYM_CASES, EXEC_CASES, HOPELESS_CASES, MATRICES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES,  # noqa: E402
                    SIMDIFY_CASES, TRAVERSE_CASES, arr_digest, digest, key_color, key_power, key_power_flat,
-                   init_perm, key_color3, key_color_env, key_color_init, key_color_row, key_hopeless, key_power_tri, key_simdify, key_trav, sell_layout, triangle)
+                   init_perm, key_color3, key_color_env, key_color_init, key_color_row, key_color_unsym,
+                   key_hopeless, key_power_tri, key_simdify, key_trav, sell_layout, triangle)
 from oracle import refpy  # noqa: E402
 from oracle.refpy import RefInterface  # noqa: E402
 from race_gb300 import matgen  # noqa: E402
@@ -127,6 +129,19 @@ def main():
         g[k + "__col"] = sell[0]
         g[k + "__src"] = sell[1].astype(np.int32)
         print(k, "ok" if ok else "cannot simdify")
+
+    # colorings of unsymmetric patterns (symm_hint false)
+    for m, tri, d, t in COLOR_UNSYM_CASES:
+        T = triangle(M(m), tri)
+        rc = refpy.RefColor(T, d, t, symm_hint=False)
+        k = key_color_unsym(m, tri, d, t)
+        p, ip = rc.perm()
+        g[k + "__digest"] = np.array(digest(T))
+        g[k + "__perm"] = p
+        g[k + "__tree"] = rc.tree_flat()
+        g[k + "__threads"] = np.array(rc.threads())
+        rc.close()
+        print(k, "threads", int(g[k + "__threads"]))
 
     # colorings that balance rows (LBTarget ROW)
     for m, d, t in COLOR_ROW_CASES:

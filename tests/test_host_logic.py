@@ -607,3 +607,23 @@ def test_level_recursion_balancing_rows(golden, mats, monkeypatch):
         np.testing.assert_array_equal(tree, gold, err_msg=k)
         assert avail == int(golden[k + "__threads"]), k
         np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)
+
+
+def test_level_recursion_on_unsymmetric_patterns(golden, mats, monkeypatch):
+    """Matrices whose pattern is not symmetric, colored with symm_hint
+    false: with RACE's symmetrisation (the missing transposed entries added,
+    graph.cpp:47-142) as the traversal graph, the engine's level recursion
+    gives the reference's zone tree, threads and permutation."""
+    from cases import COLOR_UNSYM_CASES, key_color_unsym, symmetrized_pattern, triangle
+    for var in ("RACE_EFFICIENCY", "RACE_THREADS"):
+        monkeypatch.delenv(var, raising=False)
+    for m, tri, d, t in COLOR_UNSYM_CASES:
+        T = triangle(mats[m], tri)
+        k = key_color_unsym(m, tri, d, t)
+        assert str(golden[k + "__digest"]) == digest(T)
+        S = symmetrized_pattern(T)
+        gold = golden[k + "__tree"]
+        tree, avail, perm = _zone_tree_host(S, d, t, 0, 2 * gold.size + 1024)
+        np.testing.assert_array_equal(tree, gold, err_msg=k)
+        assert avail == int(golden[k + "__threads"]), k
+        np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)

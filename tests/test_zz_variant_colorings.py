@@ -1,13 +1,14 @@
 """Coloring variants on the GPU, against the reference: distance-2 coloring
 with RACE::THREE_BLOCK (permutation, zone tree, thread count, and bit-exact
-sweeps reproducing the reference executor's outputs) and coloring from an
-initial permutation. (Their host parts, the load balancer, the level
+sweeps reproducing the reference executor's outputs), coloring from an
+initial permutation, of unsymmetric patterns and balancing rows. (Their host parts, the load balancer, the level
 recursion and the phase semantics, are checked on the CPU in
 test_host_logic.py; this file runs after the other GPU tests.)"""
 import numpy as np
 import pytest
 
-from cases import COLOR3_CASES, COLOR_INIT_CASES, digest, key_color3, key_color_init
+from cases import (COLOR3_CASES, COLOR_INIT_CASES, COLOR_ROW_CASES, COLOR_UNSYM_CASES, digest, key_color3,
+                   key_color_init, key_color_row, key_color_unsym, triangle)
 from race_gb300 import matgen
 
 torch = pytest.importorskip("torch")
@@ -69,3 +70,30 @@ def test_coloring_from_an_initial_permutation(golden, mats, m, d, t):
     np.testing.assert_array_equal(rc.getZoneTreeFlat(), golden[k + "__tree"])
     assert rc.getNumThreads() == int(golden[k + "__threads"])
     assert rc.getEfficiency() == float(golden[k + "__eff"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,tri,d,t", COLOR_UNSYM_CASES)
+def test_coloring_of_unsymmetric_patterns(golden, mats, m, tri, d, t):
+    """symm_hint false on a pattern that is not symmetric: the engine adds
+    the missing transposed entries on the GPU and colors like the
+    reference."""
+    T = triangle(mats[m], tri)
+    k = key_color_unsym(m, tri, d, t)
+    rc = ri.Interface(T.n, t, d, T.row_ptr, T.col, symm_hint=False)
+    assert rc.RACEColor() == 0
+    np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
+    np.testing.assert_array_equal(rc.getZoneTreeFlat(), golden[k + "__tree"])
+    assert rc.getNumThreads() == int(golden[k + "__threads"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,d,t", COLOR_ROW_CASES)
+def test_coloring_balancing_rows(golden, mats, m, d, t):
+    """LBTarget ROW on the GPU engine."""
+    A = mats[m]
+    k = key_color_row(m, d, t)
+    rc = ri.Interface(A.n, t, d, A.row_ptr, A.col, symm_hint=True, lbTarget=ri.ROW)
+    assert rc.RACEColor() == 0
+    np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
+    np.testing.assert_array_equal(rc.getZoneTreeFlat(), golden[k + "__tree"])
