@@ -627,3 +627,36 @@ def test_level_recursion_on_unsymmetric_patterns(golden, mats, monkeypatch):
         np.testing.assert_array_equal(tree, gold, err_msg=k)
         assert avail == int(golden[k + "__threads"]), k
         np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)
+
+
+def test_host_partition_entry_points_reject_bad_input():
+    L = _lib.lib()
+    bad = _lib.RACE_ERR_INVALID_ARG
+    lr = np.array([1, 2], np.int32)
+    ln = np.array([3, 5], np.int32)
+    ng, nh = C.c_int(), C.c_int()
+    ok = L.race_mpk_stage_partition(lr.ctypes.data, ln.ctypes.data, 2, 3, 8, 2, 1e6, 2.0, 50, None, None, 0,
+                                    C.byref(ng), C.byref(nh))
+    assert ok == _lib.RACE_SUCCESS and (ng.value, nh.value) == (1, 0)
+    assert L.race_mpk_stage_partition(lr.ctypes.data, ln.ctypes.data, 2, 0, 8, 2, 1e6, 2.0, 50, None, None, 0,
+                                      C.byref(ng), C.byref(nh)) == bad  # no rows
+    assert L.race_mpk_stage_partition(lr.ctypes.data, ln.ctypes.data, 2, 3, 8, 0, 1e6, 2.0, 50, None, None, 0,
+                                      C.byref(ng), C.byref(nh)) == bad  # power 0
+    assert L.race_mpk_stage_partition(None, None, 2, 3, 8, 2, 1e6, 2.0, 50, None, None, 0, C.byref(ng),
+                                      C.byref(nh)) == bad
+    rp = np.array([0, 1, 2, 3], np.int32)
+    cl = np.array([0, 1, 2], np.int32)
+    tp = np.arange(3, dtype=np.int32)
+    ti = np.arange(3, dtype=np.int32)
+    gp = np.array([0, 1, 3], np.int32)
+    hid = np.array([5], np.int32)
+    args = [3, rp.ctypes.data, cl.ctypes.data, tp.ctypes.data, ti.ctypes.data, gp.ctypes.data, 2]
+    assert L.race_mpk_recursion_permute(*args, None, 0, 2) == _lib.RACE_SUCCESS  # nothing hopeless: unchanged
+    np.testing.assert_array_equal(tp, [0, 1, 2])
+    assert L.race_mpk_recursion_permute(*args, hid.ctypes.data, 1, 2) != _lib.RACE_SUCCESS  # no group 5
+    gp_bad = np.array([0, 2, 1], np.int32)
+    assert L.race_mpk_recursion_permute(3, rp.ctypes.data, cl.ctypes.data, tp.ctypes.data, ti.ctypes.data,
+                                        gp_bad.ctypes.data, 2, None, 0, 2) == bad  # groups not monotonic
+    tl, av = C.c_int(), C.c_int()
+    assert L.race_zone_tree_host(3, 4, 3, 0, 1, None, _lib.TRAVERSE_FN(0), _lib.RANGE_NNZ_FN(0), None, None, 0,
+                                 C.byref(tl), C.byref(av)) == bad  # dist POWER has no zone tree
