@@ -1,7 +1,8 @@
 /* C-ABI harness around the RACE reference classes, compiled together with the
  * reference sources where they lie (see oracle/build_ref.sh). It exists only
  * to produce golden data (levels, permutations, zone trees, MPK schedules,
- * sweep outputs) and to pin the C restatement in oracle/race_oracle.c.
+ * sweep outputs, simdify outputs) and to pin the C restatement in
+ * oracle/race_oracle.c.
  * TEST INFRASTRUCTURE ONLY: nothing in the product links or loads this.
  *
  * Pre-processing follows RACE::Interface exactly, minus CPU pinning:

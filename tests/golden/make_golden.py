@@ -6,7 +6,12 @@ Run on the build host (where the reference sources are):
 
 Stored per case: matrix digest, permutation and inverse, zone tree (flat),
 threads/efficiency/stage depth, MPK level groups and the reference's sweep
-and MPK outputs for a few small cases. The reference's executor runs on
+and MPK outputs for a few small cases; coloring variants (THREE_BLOCK, an
+initial permutation, row balancing, environment knobs, unsymmetric
+patterns); MPK partitions with hopeless regions (level groups, hopeless
+groups, the permutation after the recursion), without recursion, and of
+triangular matrices; the load balancer on level histograms; simdify /
+simdifyD1 outputs. The reference's executor runs on
 OpenMP threads; its outputs are deterministic for valid colorings.
 Full-size configurations are stored as digests only.
 """
