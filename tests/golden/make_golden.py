@@ -292,7 +292,11 @@ def main():
         k = key_hopeless(m, p, c)
         rp = refpy.RefPower(A, p, c)
         tr = rp.tree()
-        perm, _ = rp.perm()
+        perm, ip = rp.perm()
+        cov = rp.coverage()
+        assert (cov == 1).all()
+        if (m, p, c) in (("band_5k", 8, 3000), ("plaw_3k", 4, 2e3)):  # the reference executor, recursive partition
+            g[key_hopeless(m, p, c) + "__out"] = rp.execute(A.permuted(perm, ip), matgen.uniform_vector(A.n, 0))[1:]
         rp.close()
         g[k + "__digest"] = np.array(digest(A))
         g[k + "__lp"] = np.array(tr[0]["lp"], np.int32)

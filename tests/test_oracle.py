@@ -192,3 +192,23 @@ def test_mpk_recursion_permutation_matches_reference(golden, mats):
                        if r != 0 and lp[h + r + 1] > lp[h + r]]
             tp, ti, _, _, _ = orc.traverse_boundary(A, int(lp[h]), int(lp[h + 1]), regions, tp, ti)
         np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
+
+
+def test_reference_mpk_on_recursive_partitions_equals_spmv_chain(golden, mats):
+    """On the reference's own recursive partitions (hopeless groups
+    re-traversed), its MPK executor still gives p sequential SpMVs bit for
+    bit, so an engine with the same permutation gives the same outputs."""
+    from cases import HOPELESS_CASES, key_hopeless
+    checked = 0
+    for m, p, c in HOPELESS_CASES:
+        k = key_hopeless(m, p, c)
+        if k + "__out" not in golden:
+            continue
+        A = mats[m]
+        perm = golden[k + "__perm"]
+        inv = np.empty_like(perm)
+        inv[perm] = np.arange(A.n, dtype=np.int32)
+        Y = orc.mpk_plain(A.permuted(perm, inv), matgen.uniform_vector(A.n, 0), p)
+        np.testing.assert_array_equal(Y[1:], golden[k + "__out"], err_msg=k)
+        checked += 1
+    assert checked == 2
