@@ -63,7 +63,7 @@ enum { RACE_VAL_F64 = 0, RACE_VAL_F32 = 1, RACE_VAL_BF16 = 2 };
  * LEAF: one warp per RACE leaf, rows in order, warp-shuffle row reductions.
  * AUTO (default): per function and direction, whichever is estimated
  * cheaper. */
-enum { RACE_SWEEP_AUTO = 0, RACE_SWEEP_WAVE = 1, RACE_SWEEP_LEAF = 2 };
+enum { RACE_SWEEP_AUTO = 0, RACE_SWEEP_WAVE = 1, RACE_SWEEP_LEAF = 2, RACE_SWEEP_GATHER = 3 };
 
 typedef struct race_engine race_engine;
 
@@ -152,6 +152,12 @@ int race_execute_function(race_engine *e, int func_id, int rev);
  * synchronous. */
 int race_execute_function_async(race_engine *e, int func_id, int rev);
 int race_get_status(race_engine *e);
+/* RACE_SWEEP_GATHER runs SpMV, SpMTV and SymmSpMV without the coloring's
+ * phases: every entry of b is produced by one thread in one launch, from the
+ * updates RACE's sequential walk makes to it, replayed in that walk's order
+ * (identical results, bit for bit; the gather plan is built at the first
+ * such call per direction). GS and KACZ, which depend on earlier rows, run
+ * as in RACE_SWEEP_AUTO. */
 /* Sweep execution mode of this engine (RACE_SWEEP_*), and the schedule
  * sizes of a registered sweep function in one direction: waves and the
  * largest wave, phases and the longest leaf, and the mode AUTO picks. No
@@ -326,6 +332,14 @@ typedef long long (*race_range_nnz_fn)(void *user, int lo, int hi);
 int race_zone_tree_host(int nrow, int nthreads, int dist, int d2type, int lbTarget, const race_params *params,
                         race_traverse_fn trav, race_range_nnz_fn rangeNnz, void *user, int *treeBuf, int cap,
                         int *treeLen, int *availableThreads);
+
+/* Host-only: the gather plan of RACE_SWEEP_GATHER for SpMTV or SymmSpMV on
+ * a CRS pattern and a phase table: for every entry y of b, the updates
+ * ptr[y] .. ptr[y+1] in RACE's execution order, each a matrix entry (-1:
+ * row y's own SymmSpMV update) and the row whose x it reads. Written when
+ * cap >= *numUpdates and cap >= n + 1. */
+int race_gather_plan(int kernel, int n, const int *rowPtr, const int *col, const int *phasePtr, const int *leafLo,
+                     const int *leafHi, int numPhases, int *ptr, int *entry, int *row, int cap, int *numUpdates);
 
 /* Host-only: the wave plan of built-in kernel `kernel` on a CRS pattern
  * (host arrays) for a phase table (as from race_get_phases): rows grouped

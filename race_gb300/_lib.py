@@ -35,7 +35,7 @@ EXPORTS = [
     "race_mlp_create", "race_mlp_destroy", "race_mlp_num_params", "race_mlp_set_params", "race_mlp_get_params",
     "race_mlp_forward", "race_mlp_loss_grad", "race_mlp_adam_step", "race_mlp_last_error", "race_wave_plan",
     "race_simdify", "race_simdify_schedule", "race_simdify_d1", "race_get_highest_power", "race_get_device_phases",
-    "race_zone_tree_host", "race_mpk_stage_partition", "race_mpk_recursion_permute",
+    "race_zone_tree_host", "race_mpk_stage_partition", "race_mpk_recursion_permute", "race_gather_plan",
 ]
 
 
@@ -107,6 +107,7 @@ def lib():
                                     ip],
             "race_mpk_stage_partition": [vp, vp, i, i, C.c_longlong, i, C.c_double, C.c_double, i, vp, vp, i, ip, ip],
             "race_mpk_recursion_permute": [i, vp, vp, vp, vp, vp, i, vp, i, i],
+            "race_gather_plan": [i, i, vp, vp, vp, vp, vp, i, vp, vp, vp, i, ip],
             "race_simdify_schedule": [i, i, i, vp, vp, vp, vp, vp, i, i, vp, vp, i, ip],
             "race_simdify_d1": [i, i, i, vp, vp, vp, vp, vp, i, i],
         }

@@ -392,7 +392,7 @@ int race_get_status(race_engine *e) {
 }
 
 int race_set_sweep_mode(race_engine *e, int mode) {
-    if (!e || mode < RACE_SWEEP_AUTO || mode > RACE_SWEEP_LEAF) return RACE_ERR_INVALID_ARG;
+    if (!e || mode < RACE_SWEEP_AUTO || mode > RACE_SWEEP_GATHER) return RACE_ERR_INVALID_ARG;
     e->eng->sweepMode = mode;
     return RACE_SUCCESS;
 }
@@ -599,6 +599,34 @@ int race_zone_tree_host(int nrow, int nthreads, int dist, int d2type, int lbTarg
         *treeLen = (int)v.size();
         *availableThreads = lr.availableThreads;
         if (treeBuf && cap >= (int)v.size()) memcpy(treeBuf, v.data(), sizeof(int) * v.size());
+    });
+}
+
+int race_gather_plan(int kernel, int n, const int *rowPtr, const int *col, const int *phasePtr, const int *leafLo,
+                     const int *leafHi, int numPhases, int *ptr, int *entry, int *row, int cap, int *numUpdates) {
+    if (!rowPtr || !col || !phasePtr || !leafLo || !leafHi || n < 0 || numPhases < 0 || !numUpdates ||
+        (kernel != RACE_K_SPMTV && kernel != RACE_K_SYMMSPMV) || phasePtr[0] != 0)
+        return RACE_ERR_INVALID_ARG;
+    for (int p = 0; p < numPhases; ++p)
+        if (phasePtr[p + 1] < phasePtr[p]) return RACE_ERR_INVALID_ARG;
+    for (int l = 0; l < phasePtr[numPhases]; ++l) {
+        const int lo = leafLo[l], hi = leafHi[l];
+        if (!(lo <= hi ? (lo >= 0 && hi <= n) : (hi >= -1 && lo < n))) return RACE_ERR_INVALID_ARG;
+    }
+    return guard(nullptr, [&] {
+        race::PhaseTable pt;
+        pt.phasePtr.assign(phasePtr, phasePtr + numPhases + 1);
+        pt.leafLo.assign(leafLo, leafLo + pt.phasePtr.back());
+        pt.leafHi.assign(leafHi, leafHi + pt.phasePtr.back());
+        race::GatherPlan gp = race::buildGatherPlan(kernel, n, rowPtr, col, pt);
+        *numUpdates = (int)gp.entry.size();
+        if (ptr && entry && row && cap >= (int)gp.entry.size() && cap >= n + 1) {
+            memcpy(ptr, gp.ptr.data(), sizeof(int) * gp.ptr.size());
+            if (!gp.entry.empty()) {
+                memcpy(entry, gp.entry.data(), sizeof(int) * gp.entry.size());
+                memcpy(row, gp.row.data(), sizeof(int) * gp.row.size());
+            }
+        }
     });
 }
 

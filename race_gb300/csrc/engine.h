@@ -11,7 +11,12 @@
 
 namespace race {
 
-enum SweepMode { SWEEP_AUTO = RACE_SWEEP_AUTO, SWEEP_WAVE = RACE_SWEEP_WAVE, SWEEP_LEAF = RACE_SWEEP_LEAF };
+enum SweepMode {
+    SWEEP_AUTO = RACE_SWEEP_AUTO,
+    SWEEP_WAVE = RACE_SWEEP_WAVE,
+    SWEEP_LEAF = RACE_SWEEP_LEAF,
+    SWEEP_GATHER = RACE_SWEEP_GATHER
+};
 
 // Device copy of a phase table for the persistent sweep kernel.
 struct DevPhases {
@@ -99,6 +104,13 @@ struct DevWaves {
     DevBuf<double> segScratch;
 };
 
+// Device copy of a gather plan (waves.h) of one sweep direction, built at
+// the first gather-mode call.
+struct DevGather {
+    bool built = false;
+    DevBuf<int> ptr, entry, row;
+};
+
 struct FuncEntry {
     int kernel = 0;
     race_operands ops{};
@@ -106,6 +118,7 @@ struct FuncEntry {
     std::unique_ptr<MpkPlan> mpk;
     std::unique_ptr<BlockPlan> block;  // block MPK (race_register_mpk_block)
     DevWaves waves[2];  // forward, reverse
+    DevGather gather[2];
 };
 
 class Engine {

@@ -536,6 +536,84 @@ void launch(bool waveMode, SweepArgs &a, int maxWork, cudaStream_t s) {
     }
 }
 
+// Gather execution (RACE_SWEEP_GATHER): one thread per entry of b, which
+// replays the updates RACE's sequential walk makes to it, in that walk's
+// order (GatherPlan, waves.h), with the kernel bodies' own operations, so
+// the results equal the wave executor's bit for bit; no phases, no grid
+// barriers. SpMV needs no plan: its rows are independent.
+template <typename VT, typename XT>
+__global__ void kGather(int kernel, int n, const int *__restrict__ ptr, const int *__restrict__ entry,
+                        const int *__restrict__ src, const int *__restrict__ rowPtr, const int *__restrict__ col,
+                        const void *val_, const XT *__restrict__ x, XT *__restrict__ b) {
+    const VT *val = (const VT *)val_;
+    for (int y = blockIdx.x * blockDim.x + threadIdx.x; y < n; y += gridDim.x * blockDim.x) {
+        if (kernel == RACE_K_SPMV) {  // kernels.cpp:5-15
+            XT t = XT(0);
+            for (int j = rowPtr[y]; j < rowPtr[y + 1]; ++j) t = mac(ld<VT, XT>(val, j), x[col[j]], t);
+            b[y] = t;
+            continue;
+        }
+        XT acc = b[y];
+        for (int k = ptr[y]; k < ptr[y + 1]; ++k) {
+            const int e = entry[k];
+            if (e >= 0) {  // b[y] += a x[src] of another row (SpMTV :107-115, SymmSpMV :403-417)
+                acc = mac(ld<VT, XT>(val, e), x[src[k]], acc);
+            } else {  // row y's own SymmSpMV update: diagonal, then its off-diagonal dot product
+                const int s = rowPtr[y], end = rowPtr[y + 1];
+                acc = mac(ld<VT, XT>(val, s), x[y], acc);
+                XT t = XT(0);
+                for (int j = s + 1; j < end; ++j) t = mac(ld<VT, XT>(val, j), x[col[j]], t);
+                acc += t;
+            }
+        }
+        b[y] = acc;
+    }
+}
+
+template <typename VT, typename XT>
+void launchGather(const FuncEntry &f, const DevGather &g, cudaStream_t s) {
+    const race_operands &o = f.ops;
+    const int n = o.n;
+    if (n == 0) return;
+    const int blocks = std::min(ceilDiv(n, 256), 152 * 16);
+    kGather<VT, XT><<<blocks, 256, 0, s>>>(f.kernel, n, g.ptr.p, g.entry.p, g.row.p, o.rowPtr, o.col, o.val,
+                                            (const XT *)o.x, (XT *)o.b);
+    RACE_CUDA(cudaGetLastError());
+}
+
+void runGather(Engine &e, FuncEntry &f, int dir) {
+    const race_operands &ops = f.ops;
+    DevGather &g = f.gather[dir];
+    if (!g.built && f.kernel != RACE_K_SPMV) {
+        const int n = ops.n;
+        std::vector<int> rp(n + 1);
+        RACE_CUDA(cudaMemcpyAsync(rp.data(), ops.rowPtr, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, e.stream));
+        RACE_CUDA(cudaStreamSynchronize(e.stream));
+        std::vector<int> cl(std::max(rp[n], 1));
+        RACE_CUDA(cudaMemcpyAsync(cl.data(), ops.col, sizeof(int) * (size_t)rp[n], cudaMemcpyDeviceToHost, e.stream));
+        RACE_CUDA(cudaStreamSynchronize(e.stream));
+        const GatherPlan gp = buildGatherPlan(f.kernel, n, rp.data(), cl.data(), e.phases[dir]);
+        g.ptr.upload(gp.ptr.data(), gp.ptr.size(), e.stream);
+        g.entry.upload(gp.entry.empty() ? nullptr : gp.entry.data(), std::max<size_t>(gp.entry.size(), 1), e.stream);
+        g.row.upload(gp.row.empty() ? nullptr : gp.row.data(), std::max<size_t>(gp.row.size(), 1), e.stream);
+        RACE_CUDA(cudaStreamSynchronize(e.stream));
+        g.built = true;
+    }
+    if (ops.vec_type == RACE_VAL_F64) {
+        if (ops.val_type != RACE_VAL_F64) throw Error(RACE_ERR_INVALID_ARG, "FP64 vectors need FP64 values");
+        launchGather<double, double>(f, g, e.stream);
+    } else if (ops.vec_type == RACE_VAL_F32) {
+        if (ops.val_type == RACE_VAL_F32)
+            launchGather<float, float>(f, g, e.stream);
+        else if (ops.val_type == RACE_VAL_BF16)
+            launchGather<__nv_bfloat16, float>(f, g, e.stream);
+        else
+            throw Error(RACE_ERR_INVALID_ARG, "FP32 vectors need FP32 or BF16 values");
+    } else {
+        throw Error(RACE_ERR_INVALID_ARG, "unknown vector type");
+    }
+}
+
 }  // namespace
 
 // Execution mode of one sweep direction: the engine's setting, or (auto)
@@ -634,8 +712,13 @@ void buildSweepWaves(Engine &e, FuncEntry &f) {
 void runSweep(Engine &e, FuncEntry &f, bool rev) {
     const race_operands &ops = f.ops;
     const int dir = rev ? 1 : 0;
-    const bool waveMode = useWaveMode(e, f, dir);
     RACE_CUDA(cudaMemsetAsync(e.dStatus.p, 0, sizeof(int) * 4, e.stream));
+    if (e.sweepMode == SWEEP_GATHER &&
+        (f.kernel == RACE_K_SPMV || f.kernel == RACE_K_SPMTV || f.kernel == RACE_K_SYMMSPMV)) {
+        runGather(e, f, dir);
+        return;
+    }
+    const bool waveMode = useWaveMode(e, f, dir);
     SweepArgs a{f.kernel, ops.rowPtr, ops.col, ops.val, ops.x, ops.b, nullptr, nullptr, nullptr, 0,
                 (unsigned *)(e.dStatus.p + 2), e.dStatus.p};
     int maxWork = 0;

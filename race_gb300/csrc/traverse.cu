@@ -282,7 +282,7 @@ Engine::Engine(int nrow, int nthreads, int dist_, const int *rowPtr, const int *
     if (const char *st = getenv("RACE_GPU_MPK_STRIDE")) mpkStride = atoi(st) == 1 ? 1 : 2;
     if (const char *sm = getenv("RACE_GPU_SWEEP_MODE")) {
         std::string m(sm);
-        sweepMode = m == "leaf" ? SWEEP_LEAF : m == "wave" ? SWEEP_WAVE : SWEEP_AUTO;
+        sweepMode = m == "leaf" ? SWEEP_LEAF : m == "wave" ? SWEEP_WAVE : m == "gather" ? SWEEP_GATHER : SWEEP_AUTO;
     }
     RACE_CUDA(cudaStreamSynchronize(stream));
 }

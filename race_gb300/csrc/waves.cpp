@@ -102,4 +102,47 @@ WavePlan buildWavePlan(int kernel, int n, const int *rowPtr, const int *col, con
     return wp;
 }
 
+GatherPlan buildGatherPlan(int kernel, int n, const int *rowPtr, const int *col, const PhaseTable &pt) {
+    GatherPlan gp;
+    if (kernel != RACE_K_SPMTV && kernel != RACE_K_SYMMSPMV) return gp;
+    // rows in RACE's execution order
+    std::vector<int> order;
+    order.reserve(n);
+    for (size_t l = 0; l < pt.leafLo.size(); ++l) {
+        const int lo = pt.leafLo[l], hi = pt.leafHi[l];
+        if (lo <= hi)
+            for (int r = lo; r < hi; ++r) order.push_back(r);
+        else
+            for (int r = lo; r > hi; --r) order.push_back(r);
+    }
+    // count, then fill the updates of every b entry in execution order
+    const bool symm = kernel == RACE_K_SYMMSPMV;
+    std::vector<int> count(n + 1, 0);
+    for (int r : order) {
+        const int first = symm ? rowPtr[r] + 1 : rowPtr[r];
+        if (symm) ++count[r + 1];
+        for (int j = first; j < rowPtr[r + 1]; ++j)
+            if (col[j] >= 0 && col[j] < n) ++count[col[j] + 1];
+    }
+    for (int y = 0; y < n; ++y) count[y + 1] += count[y];
+    gp.ptr = count;
+    gp.entry.assign(count[n], 0);
+    gp.row.assign(count[n], 0);
+    std::vector<int> fill(count.begin(), count.end() - 1);
+    for (int r : order) {
+        const int first = symm ? rowPtr[r] + 1 : rowPtr[r];
+        if (symm) {
+            gp.entry[fill[r]] = -1;
+            gp.row[fill[r]++] = r;
+        }
+        for (int j = first; j < rowPtr[r + 1]; ++j) {
+            const int c = col[j];
+            if (c < 0 || c >= n) continue;
+            gp.entry[fill[c]] = j;
+            gp.row[fill[c]++] = r;
+        }
+    }
+    return gp;
+}
+
 }  // namespace race

@@ -27,7 +27,7 @@ TWO_BLOCK, THREE_BLOCK = 0, 1
 ROW, NNZ = 0, 1
 FILL, SCATTER = 0, 1
 SPMV, SPMTV, SYMMSPMV, GS, KACZ, MPK = 0, 1, 2, 3, 4, 5
-SWEEP_AUTO, SWEEP_WAVE, SWEEP_LEAF = 0, 1, 2
+SWEEP_AUTO, SWEEP_WAVE, SWEEP_LEAF, SWEEP_GATHER = 0, 1, 2, 3
 VAL_F64, VAL_F32, VAL_BF16 = 0, 1, 2
 _VAL_TYPE = {torch.float64: VAL_F64, torch.float32: VAL_F32, torch.bfloat16: VAL_BF16}
 
@@ -300,7 +300,8 @@ class Interface:
         return lib().race_get_status(self._h)
 
     def setSweepMode(self, mode: int):
-        """SWEEP_AUTO, SWEEP_WAVE (bit-exact wave plans) or SWEEP_LEAF."""
+        """SWEEP_AUTO, SWEEP_WAVE (bit-exact wave plans), SWEEP_LEAF, or
+        SWEEP_GATHER (SpMV, SpMTV, SymmSpMV in one launch, bit-exact)."""
         self._check(lib().race_set_sweep_mode(self._h, int(mode)))
 
     def getSweepInfo(self, funcId: int, rev: bool = False) -> dict:

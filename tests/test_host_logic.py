@@ -660,3 +660,72 @@ def test_host_partition_entry_points_reject_bad_input():
     tl, av = C.c_int(), C.c_int()
     assert L.race_zone_tree_host(3, 4, 3, 0, 1, None, _lib.TRAVERSE_FN(0), _lib.RANGE_NNZ_FN(0), None, None, 0,
                                  C.byref(tl), C.byref(av)) == bad  # dist POWER has no zone tree
+
+
+def _gather_plan(kernel, mat, pp, lo, hi):
+    L = _lib.lib()
+    rp, cl = np.ascontiguousarray(mat.row_ptr, np.int32), np.ascontiguousarray(mat.col, np.int32)
+    pp, lo, hi = (np.ascontiguousarray(a, np.int32) for a in (pp, lo, hi))
+    nu = C.c_int()
+    args = [kernel, mat.n, rp.ctypes.data, cl.ctypes.data, pp.ctypes.data, lo.ctypes.data, hi.ctypes.data,
+            len(pp) - 1]
+    _lib.check(L.race_gather_plan(*args, None, None, None, 0, C.byref(nu)))
+    cap = max(nu.value, mat.n + 1)
+    ptr, entry, row = (np.zeros(cap, np.int32) for _ in range(3))
+    _lib.check(L.race_gather_plan(*args, ptr.ctypes.data, entry.ctypes.data, row.ctypes.data, cap, C.byref(nu)))
+    return ptr[: mat.n + 1], entry[: nu.value], row[: nu.value]
+
+
+def _replay_gather(mat, x, b, ptr, entry, row):
+    """The gather kernel's operations in exact arithmetic with one rounding
+    per fused multiply-add (fma(a, b, c) = round(a*b + c))."""
+    from fractions import Fraction
+
+    def fma(a, b, c):
+        return float(Fraction(a) * Fraction(b) + Fraction(c))
+
+    out = b.copy()
+    val, col, rp = mat.val, mat.col, mat.row_ptr
+    for y in range(mat.n):
+        acc = float(out[y])
+        for k in range(ptr[y], ptr[y + 1]):
+            e = int(entry[k])
+            if e >= 0:
+                acc = fma(val[e], x[row[k]], acc)
+            else:
+                s = int(rp[y])
+                acc = fma(val[s], x[y], acc)
+                t = 0.0
+                for j in range(s + 1, int(rp[y + 1])):
+                    t = fma(val[j], x[col[j]], t)
+                acc = acc + t
+        out[y] = acc
+    return out
+
+
+@pytest.mark.parametrize("m,d,t", [("lap7_16", 2, 16), ("islands_330", 2, 16), ("aniso5_120x90", 2, 48)])
+def test_gather_plans_reproduce_the_sequential_walk(golden, mats, m, d, t):
+    """RACE_SWEEP_GATHER's plans: replaying each entry of b's updates in the
+    plan's order gives RACE's sequential walk bit for bit (SpMTV on the full
+    matrix, SymmSpMV on the upper triangle; forward schedule, and the reverse
+    phase order)."""
+    A = mats[m]
+    k = key_color(m, d, t)
+    perm = golden[k + "__perm"]
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(A.n, dtype=np.int32)
+    P = A.permuted(perm, inv)
+    U = P.upper()
+    x0 = matgen.uniform_vector(A.n, 0)
+    b0 = matgen.uniform_vector(A.n, 1)  # accumulate onto a nonzero b
+    for kern, mat in ((orc.K_SPMTV, P), (orc.K_SYMMSPMV, U)):
+        for rev in (False, True):
+            pp, lo, hi = _flatten(golden[k + "__tree"], d, rev, A.n)
+            xs, bs = x0.copy(), b0.copy()
+            if rev:  # the oracle's scatter bodies take forward ranges: reversed phase order, forward leaves
+                lo, hi = np.minimum(lo, hi) + (lo > hi), np.maximum(lo, hi) + (lo > hi)
+            _run_phases(pp, lo, hi, kern, mat, xs, bs)
+            ptr, entry, row = _gather_plan(kern, mat, pp, lo, hi)
+            assert ptr[-1] == entry.size
+            got = _replay_gather(mat, x0, b0, ptr, entry, row)
+            np.testing.assert_array_equal(got, bs, err_msg=f"{kern} rev={rev}")
