@@ -4,8 +4,11 @@
 // codes follow the reference; the callback is a built-in device kernel with
 // device operands instead of a host function pointer.
 #pragma once
+#include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -197,12 +200,43 @@ class Interface {
         (void)rowPtr, (void)col, (void)val, (void)power;
     }
 
+    // tuneFunction (interface.cpp:605-647): runs the function with powers
+    // 1..p for at least 0.2 s each, keeps the power with the lowest time per
+    // power step and sets it. p is the power the function was registered
+    // with (the reference takes highestPower), so that its x, sized for p,
+    // is never overrun. The choice is kept per function.
+    int tuneFunction(int funcId, bool rev = false) {
+        auto known = tuned_.find(funcId);
+        if (known != tuned_.end()) {
+            setPower(funcId, known->second);
+            return known->second;
+        }
+        const int hp = std::max(1, getPower(funcId));
+        std::vector<double> perStep(hp, 0.0);
+        for (int p = 1; p <= hp; ++p) {
+            setPower(funcId, p);
+            const auto start = std::chrono::steady_clock::now();
+            double elapsed = 0;
+            int iter = 0;
+            do {
+                executeFunction(funcId, rev);
+                ++iter;
+                elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
+            } while (elapsed < 0.2);
+            perStep[p - 1] = elapsed / (iter * (double)p);
+        }
+        const int best = (int)(std::min_element(perStep.begin(), perStep.end()) - perStep.begin()) + 1;
+        tuned_[funcId] = best;
+        setPower(funcId, best);
+        return best;
+    }
     void setStream(void *cudaStream) { race_set_stream(e_, cudaStream); }
     race_engine *handle() { return e_; }
 
   private:
     race_engine *e_ = nullptr;
     int nrow_;
+    std::map<int, int> tuned_;
 };
 
 // Block-MPK functions of several Interfaces in one persistent launch

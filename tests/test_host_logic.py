@@ -160,8 +160,9 @@ int use(int n, int *rp, int *col, race_operands ops) {
     ce.setSerial(f);
     ce.unsetSerial(f);
     ce.numaInitMtxVec(rp, col, nullptr, nullptr, 4);
+    int best = ce.tuneFunction(f);
     return rc + f + ce.executeFunctionAsync(f) + ce.getStatus() + b.getStatus() + ce.getNumThreads() +
-           ce.getHighestPower() + (ok ? 1 : 0);
+           ce.getHighestPower() + (ok ? 1 : 0) + best;
 }
 """)
     root = pathlib.Path(__file__).resolve().parents[1]
