@@ -269,6 +269,8 @@ def main():
                     help="RACE cacheSize of each batched matrix (256 MB: fastest of 1-1000 MB on GB300)")
     ap.add_argument("--grid", type=int, default=GRID)
     ap.add_argument("--values", choices=["f64", "f32"], default="f64")
+    ap.add_argument("--c1-gather", action="store_true",
+                    help="include the gather sweep mode in the 32^3 SymmSpMV search")
     ap.add_argument("--mpk-per-call", type=int, default=0,
                     help="also time the 8 powers as 8/K chained calls of power K (K in 1, 2, 4), as "
                          "tuneFunction would choose; reported as a separate item, the headline stays one call")
@@ -453,7 +455,7 @@ def main():
     symmgs = bench_symmgs(args, ri, matgen, torch) if args.symmgs_rows > 0 else None
     batched = bench_batch(args, ri, matgen, torch) if args.batch_count > 0 else None
     tuned = bench_tuner(torch) if not args.no_tuner else None
-    c1 = bench_c1(ri, matgen, torch) if rank == 0 else None
+    c1 = bench_c1(ri, matgen, torch, gather=args.c1_gather) if rank == 0 else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
@@ -638,15 +640,15 @@ def bench_batch(args, ri, matgen, torch):
     return out
 
 
-def bench_c1(ri, matgen, torch, reps: int = 100):
+def bench_c1(ri, matgen, torch, reps: int = 100, gather: bool = False):
     """SymmSpMV with RACE distance-2 coloring on the 32^3 7-point Laplacian
     (n = 32,768, upper triangle 128,000 entries incl. the diagonal), x
     U[-1,1] seed 0, 100 calls per setting. Bytes per call: 12 nnz_u + 4(n+1)
     + 8n (x) + 16n (b read and written) = 2,453,508 B; the working set
     (2.5 MB) lives in L2, so "% of HBM" does not apply and the time is the
     latency of RACE's phases. Requested threads (RACE_THREADS, 256/1024/4096)
-    and sweep mode (wave/leaf) are searched as a user tunes them; the best is
-    reported with all settings. The CPU figure is the sequential restatement
+    and sweep mode (wave/leaf, and gather with --c1-gather) are searched as a
+    user tunes them; the best is reported with all settings. The CPU figure is the sequential restatement
     of the kernel body over all rows (one core)."""
     from oracle import oracle as orc
     A = matgen.laplace3d_7pt(32)
@@ -664,7 +666,8 @@ def bench_c1(ri, matgen, torch, reps: int = 100):
         fid = rc.registerFunction(ri.SYMMSPMV, ri.Operands(ri.DeviceCsr.from_csr(U), x, b))
         assert fid >= 0
         info = rc.getSweepInfo(fid)
-        for mode, mname in ((ri.SWEEP_WAVE, "wave"), (ri.SWEEP_LEAF, "leaf")):
+        modes = [(ri.SWEEP_WAVE, "wave"), (ri.SWEEP_LEAF, "leaf")] + ([(ri.SWEEP_GATHER, "gather")] if gather else [])
+        for mode, mname in modes:
             rc.setSweepMode(mode)
             for _ in range(5):
                 rc.executeFunctionAsync(fid)
