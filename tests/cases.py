@@ -152,6 +152,16 @@ HOPELESS_CASES = POWER_FLAT_CASES + [("band_5k", 8, 3000), ("band_5k", 8, 2500),
                                      ("plaw_3k", 4, 2e3), ("lap7_16", 4, 2e4), ("st27_24", 8, 1e5)]
 
 
+# MPK partitions with other safety factors (RACEColor's safetyFactor,
+# interface.cpp:205): (matrix, power, cacheBytes, safety)
+POWER_SAFETY_CASES = [("st27_24", 8, 2e6, 1.0), ("band_5k", 6, 3e5, 4.0), ("plaw_20k", 4, 1e6, 1.5),
+                      ("lap7_32", 4, 1e5, 8.0)]
+
+
+def key_power_safety(m, p, c, safety):
+    return f"powersafety__{m}__p{p}__c{int(c)}__s{safety:g}"
+
+
 def key_hopeless(m, p, c):
     return f"hopeless__{m}__p{p}__c{int(c)}"
 

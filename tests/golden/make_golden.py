@@ -31,7 +31,7 @@ os.environ.setdefault("ORACLE_QUIET", "1")
 os.environ.setdefault("OMP_NUM_THREADS", "8")
 
 from cases import (COLOR3_CASES, COLOR_CASES, COLOR_ENV_CASES, COLOR_INIT_CASES, COLOR_ROW_CASES,  # noqa: E402
-                   COLOR_UNSYM_CASES, EXEC_CASES, HOPELESS_CASES, MATRICES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES,  # noqa: E402
+                   COLOR_UNSYM_CASES, EXEC_CASES, POWER_SAFETY_CASES, key_power_safety, HOPELESS_CASES, MATRICES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES,  # noqa: E402
                    SIMDIFY_CASES, TRAVERSE_CASES, arr_digest, digest, key_color, key_power, key_power_flat,
                    init_perm, key_color3, key_color_env, key_color_init, key_color_row, key_color_unsym,
                    key_hopeless, key_power_tri, key_simdify, key_trav, sell_layout, triangle)
@@ -304,6 +304,20 @@ def main():
         g[k + "__leaves"] = np.array(len(tr))
         g[k + "__perm"] = perm  # after the recursion into the hopeless groups
         print(k, "groups", len(tr[0]["lp"]) - 1, "hopeless", tr[0]["hid"], "leaves", len(tr))
+
+    # other safety factors
+    for m, p, c, sf in POWER_SAFETY_CASES:
+        A = M(m)
+        k = key_power_safety(m, p, c, sf)
+        rp = refpy.RefPower(A, p, c, safety=sf)
+        perm, _ = rp.perm()
+        tr = rp.tree()
+        rp.close()
+        g[k + "__digest"] = np.array(digest(A))
+        g[k + "__perm"] = perm
+        g[k + "__lp"] = np.array(tr[0]["lp"], np.int32)
+        g[k + "__hid"] = np.array(tr[0]["hid"], np.int32)
+        print(k, "groups", len(tr[0]["lp"]) - 1, "hopeless", tr[0]["hid"])
 
     # triangular matrix power: mtxType L / U on the lower / upper triangle
     for m, tri, p, c in POWER_TRI_CASES:

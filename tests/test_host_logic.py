@@ -468,12 +468,12 @@ def test_level_recursion_on_host_matches_reference(golden, mats, m, d, t, d2type
     np.testing.assert_array_equal(perm, golden[k + "__perm"])
 
 
-def _stage_partition(lr, ln, n, nnz, power, cache, cutoff=50):
+def _stage_partition(lr, ln, n, nnz, power, cache, cutoff=50, safety=2.0):
     L = _lib.lib()
     lr = np.ascontiguousarray(lr, np.int32)
     ln = np.ascontiguousarray(ln, np.int32)
     ng, nh = C.c_int(), C.c_int()
-    args = [lr.ctypes.data, ln.ctypes.data, lr.size, n, nnz, power, float(cache), 2.0, cutoff]
+    args = [lr.ctypes.data, ln.ctypes.data, lr.size, n, nnz, power, float(cache), float(safety), cutoff]
     _lib.check(L.race_mpk_stage_partition(*args, None, None, 0, C.byref(ng), C.byref(nh)))
     cap = max(ng.value + 1, nh.value, 1)
     gp, hid = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
@@ -730,3 +730,16 @@ def test_gather_plans_reproduce_the_sequential_walk(golden, mats, m, d, t):
             assert ptr[-1] == entry.size
             got = _replay_gather(mat, x0, b0, ptr, entry, row)
             np.testing.assert_array_equal(got, bs, err_msg=f"{kern} rev={rev}")
+
+
+def test_stage_partition_with_other_safety_factors(golden, mats):
+    """RACEColor's safetyFactor (interface.cpp:205) scales every level's
+    budget: the level groups and hopeless groups follow the reference."""
+    from cases import POWER_SAFETY_CASES, key_power_safety
+    for m, p, c, sf in POWER_SAFETY_CASES:
+        A = mats[m]
+        k = key_power_safety(m, p, c, sf)
+        _, _, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+        gp, hid = _stage_partition(lr, ln, A.n, A.nnz, p, c, safety=sf)
+        np.testing.assert_array_equal(gp, golden[k + "__lp"], err_msg=k)
+        np.testing.assert_array_equal(hid, golden[k + "__hid"], err_msg=k)

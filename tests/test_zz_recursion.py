@@ -7,7 +7,7 @@ runs last among the GPU tests.)"""
 import numpy as np
 import pytest
 
-from cases import HOPELESS_CASES, digest, key_hopeless
+from cases import HOPELESS_CASES, POWER_SAFETY_CASES, digest, key_hopeless, key_power_safety
 from oracle import oracle as orc
 from race_gb300 import matgen
 
@@ -53,3 +53,16 @@ def test_deeper_recursion_is_refused(mats):
     A = mats["band_5k"]
     rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True, params={"max_recursion_stages": 2})
     assert rc.RACEColor(8, 3000) == 10  # RACE_ERR_NOT_IMPLEMENTED
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,p,c,sf", POWER_SAFETY_CASES)
+def test_partition_with_other_safety_factors(golden, mats, m, p, c, sf):
+    """RACEColor(p, cacheSize, safetyFactor): the engine's permutation and
+    level groups equal the reference's."""
+    A = mats[m]
+    k = key_power_safety(m, p, c, sf)
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, c, safetyFactor=sf) == 0
+    np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
+    np.testing.assert_array_equal(rc.getPowerGroups(), golden[k + "__lp"])
