@@ -3,9 +3,10 @@
 import numpy as np
 import pytest
 
-from cases import (EXEC_CASES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES, TRAVERSE_CASES, digest, key_color,
-                   key_power, key_power_flat, key_power_tri, key_trav, triangle)
+from cases import (COLOR_CASES, EXEC_CASES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES, TRAVERSE_CASES, digest,
+                   key_color, key_power, key_power_flat, key_power_tri, key_trav, triangle)
 from oracle import oracle as orc
+from oracle.refpy import parse_zone_tree
 from race_gb300 import matgen
 
 
@@ -212,3 +213,27 @@ def test_reference_mpk_on_recursive_partitions_equals_spmv_chain(golden, mats):
         np.testing.assert_array_equal(Y[1:], golden[k + "__out"], err_msg=k)
         checked += 1
     assert checked == 2
+
+
+@pytest.mark.parametrize("m,d,t", [c for c in COLOR_CASES if c[1] == 2])
+def test_validated_coloring_invariant(golden, mats, m, d, t):
+    """The reference's own validation of a coloring (colorSymmSpMV.cpp:
+    230-260, checkEqual in densemat.cpp:147-180): a plain SpMV, the colored
+    SpMV and the colored SymmSpMV on the upper triangle agree, here within
+    1e-12 of the largest entry (the SymmSpMV sums in another order)."""
+    A = mats[m]
+    k = key_color(m, d, t)
+    perm = golden[k + "__perm"]
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(A.n, dtype=np.int32)
+    P = A.permuted(perm, inv)
+    U = P.upper()
+    x = matgen.uniform_vector(A.n, 0)
+    plain = np.zeros(A.n)
+    orc.run_kernel(orc.K_SPMV, 0, A.n, P, x, plain)
+    nodes = parse_zone_tree(golden[k + "__tree"])
+    colored, symm = np.zeros(A.n), np.zeros(A.n)
+    orc.exec_tree(nodes, 2, golden[k + "__serial"], orc.K_SPMV, False, P, x.copy(), colored)
+    orc.exec_tree(nodes, 2, golden[k + "__serial"], orc.K_SYMMSPMV, False, U, x.copy(), symm)
+    np.testing.assert_array_equal(colored, plain)  # rows are independent: same sums
+    assert np.max(np.abs(symm - plain)) <= 1e-12 * np.max(np.abs(plain))
