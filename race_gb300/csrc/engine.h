@@ -171,6 +171,7 @@ class Engine {
 
     // power results
     int mpkStride = 2;  // issue order of the MPK wavefront (1: RACE's, 2: GPU default)
+    int mpkSplit = 0;   // powers per wavefront segment of the MPK issue order (0: all powers at once)
     bool powerReady = false;
     int highestPower = 1, highestSubPower = 1;
     std::vector<int> levelPtr, groupPtr, unlockRow, dangerRow;

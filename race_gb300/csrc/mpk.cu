@@ -459,15 +459,23 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     std::vector<int> itemChunk;
     std::vector<unsigned char> itemPow;
     itemChunk.reserve((size_t)C * power);
-    for (int st = 0; st < G + stride * (power - 1); ++st)
-        for (int k = 0; k < power; ++k) {
-            int g = st - stride * k;
-            if (g < 0 || g >= G) continue;
-            for (int t = groupFirst[g]; t < groupFirst[g + 1]; ++t) {
-                itemChunk.push_back(t);
-                itemPow.push_back((unsigned char)k);
+    // With a split of s powers, the wavefront runs over powers 1..s, then
+    // s+1..2s, ... in one launch (each segment's items follow all items of
+    // the powers before it, so the order stays a valid wavefront): fewer
+    // groups in flight at the cost of reading the matrix once per segment.
+    const int split = e.mpkSplit > 0 && e.mpkSplit < power ? e.mpkSplit : power;
+    for (int k0 = 0; k0 < power; k0 += split) {
+        const int kn = std::min(power, k0 + split) - k0;
+        for (int st = 0; st < G + stride * (kn - 1); ++st)
+            for (int k = 0; k < kn; ++k) {
+                int g = st - stride * k;
+                if (g < 0 || g >= G) continue;
+                for (int t = groupFirst[g]; t < groupFirst[g + 1]; ++t) {
+                    itemChunk.push_back(t);
+                    itemPow.push_back((unsigned char)(k0 + k));
+                }
             }
-        }
+    }
     plan->numItems = (int)itemChunk.size();
     plan->itemChunk.upload(itemChunk.data(), std::max<size_t>(itemChunk.size(), 1), s);
     plan->itemPow.upload(itemPow.data(), std::max<size_t>(itemPow.size(), 1), s);

@@ -280,6 +280,7 @@ Engine::Engine(int nrow, int nthreads, int dist_, const int *rowPtr, const int *
     dValsOut.alloc(nrow);
     dStatus.alloc(4);
     if (const char *st = getenv("RACE_GPU_MPK_STRIDE")) mpkStride = atoi(st) == 1 ? 1 : 2;
+    if (const char *sp = getenv("RACE_GPU_MPK_SPLIT")) mpkSplit = std::max(0, atoi(sp));
     if (const char *sm = getenv("RACE_GPU_SWEEP_MODE")) {
         std::string m(sm);
         sweepMode = m == "leaf" ? SWEEP_LEAF : m == "wave" ? SWEEP_WAVE : m == "gather" ? SWEEP_GATHER : SWEEP_AUTO;
