@@ -66,3 +66,22 @@ def test_partition_with_other_safety_factors(golden, mats, m, p, c, sf):
     assert rc.RACEColor(p, c, safetyFactor=sf) == 0
     np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
     np.testing.assert_array_equal(rc.getPowerGroups(), golden[k + "__lp"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("split", [4, 2, 3])
+def test_split_wavefront_order(mats, monkeypatch, split):
+    """RACE_GPU_MPK_SPLIT: the issue order in power segments inside one
+    launch still gives p sequential SpMVs bit for bit."""
+    monkeypatch.setenv("RACE_GPU_MPK_SPLIT", str(split))
+    A = mats["st27_24"]
+    p = 8
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, 2e6) == 0
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    x0 = matgen.uniform_vector(A.n, 0)
+    x = torch.zeros((p + 1) * A.n, dtype=torch.float64, device="cuda")
+    x[: A.n] = torch.tensor(x0, device="cuda")
+    fid = rc.registerFunction(ri.MPK, ri.Operands(ri.DeviceCsr.from_csr(P), x), power=p)
+    assert fid >= 0 and rc.executeFunction(fid) == 0
+    np.testing.assert_array_equal(x.cpu().numpy().reshape(p + 1, A.n), orc.mpk_plain(P, x0, p))
