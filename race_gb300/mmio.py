@@ -119,3 +119,20 @@ def make_diag_first(csr: Csr, missing_diag_value: float = 0.0, rewrite_all_diag_
     if rewrite_all_diag_with_max_row_sum:
         val_out[rp[:-1]] = max_row_sum
     return Csr(n, rp.astype(np.int32), col_out.astype(np.int32), val_out, csr.name)
+
+
+def rcm_perm(csr):
+    """A reverse Cuthill-McKee ordering to pass as the Interface's initPerm
+    (new row i = old row perm[i]) with its inverse. The reference's examples
+    take RCM from SpMP (CMakeLists.txt:294-323), a third-party library that
+    is not part of RACE; this one is SciPy's, so the ordering itself can
+    differ from SpMP's. The pattern is symmetrised first."""
+    import scipy.sparse as sp
+    from scipy.sparse.csgraph import reverse_cuthill_mckee
+
+    n = csr.n
+    S = sp.csr_matrix((np.ones(len(csr.col)), np.asarray(csr.col), np.asarray(csr.row_ptr)), shape=(n, n))
+    perm = np.asarray(reverse_cuthill_mckee((S + S.T).tocsr(), symmetric_mode=True), np.int32)
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(n, dtype=np.int32)
+    return perm, inv

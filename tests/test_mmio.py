@@ -109,3 +109,19 @@ def test_reference_example_matrix():
     np.testing.assert_array_equal(D, S.toarray())
     B = mmio.make_diag_first(A)
     assert all(B.col[B.row_ptr[r]] == r for r in range(B.n))
+
+
+def test_rcm_initial_permutation_reduces_bandwidth(mats):
+    """rcm_perm gives a permutation (and its inverse) that shrinks the
+    bandwidth of a scrambled banded matrix."""
+    pytest.importorskip("scipy")
+    A = mats["band_5k"]
+    perm, inv = mmio.rcm_perm(A)
+    assert np.array_equal(np.sort(perm), np.arange(A.n))
+    assert np.array_equal(inv[perm], np.arange(A.n))
+
+    def bandwidth(M):
+        r = np.repeat(np.arange(M.n), np.diff(M.row_ptr))
+        return int(np.max(np.abs(r - M.col)))
+
+    assert bandwidth(A.permuted(perm, inv)) < bandwidth(A) / 10
