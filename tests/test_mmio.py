@@ -2,6 +2,7 @@
 example driver: sparsemat::readFile (symmetric expansion, stable row sort,
 pattern value 0.01) and makeDiagFirst."""
 import gzip
+import os
 import pathlib
 
 import numpy as np
@@ -96,7 +97,8 @@ def test_reference_example_matrix():
     """The reference's bundled example (examples/matrices/spinSZ12.mm.gz,
     924 rows), where this container has the reference: the same entries as
     SciPy's reader, each row in file order, and every row gets a diagonal."""
-    path = pathlib.Path("/root/reference/examples/matrices/spinSZ12.mm.gz")
+    ref = pathlib.Path(os.environ.get("RACE_REFERENCE_DIR", "/root/reference"))
+    path = ref / "examples" / "matrices" / "spinSZ12.mm.gz"
     if not path.exists():
         pytest.skip("reference example matrix not present")
     scipy_io = pytest.importorskip("scipy.io")
