@@ -187,6 +187,11 @@ class Interface {
     // thread count. Kept so that callers of the reference compile; they do
     // nothing.
     void sleep() {}
+    // MPI placeholders whose bodies are empty in the reference too (all code
+    // commented out, interface.cpp:62-67 and compressColIdx after it): kept
+    // so that callers compile.
+    void passGlobalRows(int globalStartRow, int globalEndRow) { (void)globalStartRow, (void)globalEndRow; }
+    void compressColIdx() {}
     void pinThread(int threadId) { (void)threadId; }
     void setSerial(int funcId) { (void)funcId; }
     void unsetSerial(int funcId) { (void)funcId; }
