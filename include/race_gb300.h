@@ -89,6 +89,8 @@ typedef struct {
     int lvl_threads[16];
     int cache_violation_cutoff;
     int max_recursion_stages; /* -1: the reference's default; 0: MPK partition without recursion */
+    int n_cutoffs;            /* RACE_CACHE_VIOLATION_CUTOFF: cut-off of MPK recursion stage k is cutoffs[k] */
+    int cutoffs[16];          /* for k < n_cutoffs, else cache_violation_cutoff */
 } race_params;
 
 int race_params_from_env(race_params *p);
@@ -316,6 +318,21 @@ int race_mpk_stage_partition(const int *levelRow, const int *levelNnz, int total
  * hopeless as from race_mpk_stage_partition. */
 int race_mpk_recursion_permute(int n, const int *rowPtr, const int *col, int *totalPerm, int *totalInvPerm,
                                const int *groupPtr, int numGroups, const int *hopeless, int numHopeless, int power);
+
+/* Host-only: the MPK partition's recursion at any depth
+ * (mtxPowerRecursive::recursivePartition, matrixPowerRecursive.cpp:156-338):
+ * below the stage-0 groups and hopeless groups of race_mpk_stage_partition,
+ * every hopeless group is traversed with its boundaries, partitioned again
+ * (a level's size includes its boundary rows' non-zeros) with the cut-off
+ * of its stage, stageCutoff[s] (INT_MAX for s >= numStages; stageCutoff[0]
+ * is not read), and recursed into depth first. totalPerm/totalInvPerm are
+ * updated in place. treeBuf (when cap >= *treeLen) gets the leaves in the
+ * reference's order: count, then per leaf lo, hi, stage, parent, numGroups,
+ * groupPtr[numGroups+1], numHopeless, hopeless[numHopeless]. */
+int race_mpk_recursive_partition(int n, const int *rowPtr, const int *col, int *totalPerm, int *totalInvPerm,
+                                 const int *groupPtr, int numGroups, const int *hopeless, int numHopeless, int power,
+                                 long long graphNnz, double cacheSize, double safety, const int *stageCutoff,
+                                 int numStages, int *treeBuf, int cap, int *treeLen);
 
 /* Host-only: RACE's level recursion (level_recursion.cpp:149-376, the
  * zone tree of race_color) with the traversal supplied by the caller instead

@@ -14,6 +14,7 @@ LIB_PATH = PKG / "_build" / "librace_gb300.so"
 
 RACE_SUCCESS = 0
 RACE_ERR_INVALID_ARG = 1
+RACE_ERR_GRAPH_TRAVERSAL = 5
 RACE_ERR_INCOMPATIBILITY = 6
 ERRORS = {
     0: "RACE_SUCCESS", 1: "RACE_ERR_INVALID_ARG", 2: "RACE_ERR_MATRIX_SYMM", 3: "RACE_ERR_D2_COLOR",
@@ -36,6 +37,7 @@ EXPORTS = [
     "race_mlp_forward", "race_mlp_loss_grad", "race_mlp_adam_step", "race_mlp_last_error", "race_wave_plan",
     "race_simdify", "race_simdify_schedule", "race_simdify_d1", "race_get_highest_power", "race_get_device_phases",
     "race_zone_tree_host", "race_mpk_stage_partition", "race_mpk_recursion_permute", "race_gather_plan",
+    "race_mpk_recursive_partition",
 ]
 
 
@@ -48,7 +50,7 @@ class RaceError(RuntimeError):
 class race_params(C.Structure):
     _fields_ = [("n_eff", C.c_int), ("eff", C.c_double * 16), ("n_lvl_threads", C.c_int),
                 ("lvl_threads", C.c_int * 16), ("cache_violation_cutoff", C.c_int),
-                ("max_recursion_stages", C.c_int)]
+                ("max_recursion_stages", C.c_int), ("n_cutoffs", C.c_int), ("cutoffs", C.c_int * 16)]
 
 
 class race_operands(C.Structure):
@@ -107,6 +109,8 @@ def lib():
                                     ip],
             "race_mpk_stage_partition": [vp, vp, i, i, C.c_longlong, i, C.c_double, C.c_double, i, vp, vp, i, ip, ip],
             "race_mpk_recursion_permute": [i, vp, vp, vp, vp, vp, i, vp, i, i],
+            "race_mpk_recursive_partition": [i, vp, vp, vp, vp, vp, i, vp, i, i, C.c_longlong, C.c_double, C.c_double,
+                                             vp, i, vp, i, ip],
             "race_gather_plan": [i, i, vp, vp, vp, vp, vp, i, vp, vp, vp, i, ip],
             "race_simdify_schedule": [i, i, i, vp, vp, vp, vp, vp, i, i, vp, vp, i, ip],
             "race_simdify_d1": [i, i, i, vp, vp, vp, vp, vp, i, i],

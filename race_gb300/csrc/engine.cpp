@@ -93,18 +93,30 @@ void Engine::powerPrepare(int hp, double cacheSize, double safety, const std::st
     }
     if (hopeless) {
         // Hopeless regions: the reference's stage-0 groups around them
-        // (stagePartition) and, for mtxType N, its one-stage recursion, which
-        // reorders the rows of each hopeless group and of its boundary groups
-        // (recursePermutation). Every group keeps its row range, so the
-        // MPK's neighbour-group dependencies still hold.
-        if (mtxType == "N" && maxRec > 1)
-            throw Error(RACE_ERR_NOT_IMPLEMENTED,
-                        "MPK recursion deeper than one stage (RACE_MAX_RECURSION_STAGES > 1 or a list of cut-offs) is "
-                        "not built");
+        // (stagePartition) and, for mtxType N, its recursion, which reorders
+        // the rows of each hopeless group and of its boundary groups (one
+        // stage by default: recursePermutation; more: recursivePartition,
+        // whose deeper stages reorder rows inside those groups again).
+        // Every stage-0 group keeps its row range, so the MPK's
+        // neighbour-group dependencies still hold.
         const StagePartition sp = stagePartition(ld, 0, P, n, nnz, cacheSize, safety, cutoff);
         if (mtxType == "N" && !sp.hopeless.empty()) {
-            if (!recursePermutation(n, hRowPtr.data(), hCol.data(), hPerm, hInvPerm, sp.groupPtr, sp.hopeless, P))
-                throw Error(RACE_ERR_GRAPH_TRAVERSAL, "rows of a hopeless group went missing in its traversal");
+            bool ok;
+            if (maxRec > 1) {
+                // cut-off of stage s (get_cache_violation_cutoff, matrixPowerRecursive.cpp:81-100)
+                std::vector<int> stageCutoff(std::min(maxRec, 1 << 16));
+                const std::vector<int> &cv = params.cacheViolationCutoff;
+                for (int s = 0; s < (int)stageCutoff.size(); ++s)
+                    stageCutoff[s] = s < (int)cv.size() - 1 ? cv[s + 1] : cv[0];
+                std::vector<MpkLeaf> tree;
+                ok = recursivePartition(n, hRowPtr.data(), hCol.data(), hPerm, hInvPerm, sp, P, nnz, cacheSize, safety,
+                                        stageCutoff, tree);
+            } else {
+                ok = recursePermutation(n, hRowPtr.data(), hCol.data(), hPerm, hInvPerm, sp.groupPtr, sp.hopeless, P);
+            }
+            if (!ok)
+                throw Error(RACE_ERR_GRAPH_TRAVERSAL,
+                            "MPK recursion: rows of a hopeless group went missing, or its boundary groups do not exist");
             dPerm.upload(hPerm.data(), n, stream);
             dInvPerm.upload(hInvPerm.data(), n, stream);
             RACE_CUDA(cudaStreamSynchronize(stream));
@@ -244,6 +256,8 @@ race::Params toParams(const race_params *p) {
     for (size_t lvl = 1; lvl < q.lvlThreads.size() + 1 && lvl < q.effVec.size(); ++lvl) q.effVec[lvl] = 0;
     q.cacheViolationCutoffDefault = p->cache_violation_cutoff > 0 ? p->cache_violation_cutoff : 50;
     q.cacheViolationCutoff.assign(1, q.cacheViolationCutoffDefault);
+    q.cacheViolationCutoff.insert(q.cacheViolationCutoff.end(), p->cutoffs,
+                                  p->cutoffs + std::max(0, std::min(p->n_cutoffs, 16)));
     q.maxRecStages = p->max_recursion_stages >= 0 ? p->max_recursion_stages : -1;
     return q;
 }
@@ -261,6 +275,8 @@ int race_params_from_env(race_params *p) {
     for (int i = 0; i < p->n_lvl_threads; ++i) p->lvl_threads[i] = q.lvlThreads[i];
     p->cache_violation_cutoff = q.cacheViolationCutoffDefault;
     p->max_recursion_stages = q.maxRecStages;
+    p->n_cutoffs = (int)std::min<size_t>(q.cacheViolationCutoff.size() - 1, 16);
+    for (int i = 0; i < p->n_cutoffs; ++i) p->cutoffs[i] = q.cacheViolationCutoff[i + 1];
     return RACE_SUCCESS;
 }
 
@@ -559,6 +575,42 @@ int race_mpk_recursion_permute(int n, const int *rowPtr, const int *col, int *to
         std::vector<int> gp(groupPtr, groupPtr + numGroups + 1), hid(hopeless, hopeless + numHopeless);
         if (!race::recursePermutation(n, rowPtr, col, tp, ti, gp, hid, power))
             throw Error(RACE_ERR_GRAPH_TRAVERSAL, "rows of a hopeless group went missing in its traversal");
+        memcpy(totalPerm, tp.data(), sizeof(int) * n);
+        memcpy(totalInvPerm, ti.data(), sizeof(int) * n);
+    });
+}
+
+int race_mpk_recursive_partition(int n, const int *rowPtr, const int *col, int *totalPerm, int *totalInvPerm,
+                                 const int *groupPtr, int numGroups, const int *hopeless, int numHopeless, int power,
+                                 long long graphNnz, double cacheSize, double safety, const int *stageCutoff,
+                                 int numStages, int *treeBuf, int cap, int *treeLen) {
+    if (n < 1 || !rowPtr || !col || !totalPerm || !totalInvPerm || !groupPtr || numGroups < 1 || numHopeless < 0 ||
+        (numHopeless > 0 && !hopeless) || power < 1 || graphNnz < 1 || !(cacheSize > 0) || numStages < 0 ||
+        (numStages > 0 && !stageCutoff) || !treeLen || groupPtr[0] != 0 || groupPtr[numGroups] != n)
+        return RACE_ERR_INVALID_ARG;
+    for (int g = 0; g < numGroups; ++g)
+        if (groupPtr[g + 1] < groupPtr[g]) return RACE_ERR_INVALID_ARG;
+    for (int h = 0; h < numHopeless; ++h)
+        if (hopeless[h] < 0 || hopeless[h] >= numGroups) return RACE_ERR_INVALID_ARG;
+    return guard(nullptr, [&] {
+        std::vector<int> tp(totalPerm, totalPerm + n), ti(totalInvPerm, totalInvPerm + n);
+        race::StagePartition root;
+        root.groupPtr.assign(groupPtr, groupPtr + numGroups + 1);
+        root.hopeless.assign(hopeless, hopeless + numHopeless);
+        std::vector<int> cut(stageCutoff, stageCutoff + numStages);
+        std::vector<race::MpkLeaf> tree;
+        if (!race::recursivePartition(n, rowPtr, col, tp, ti, root, power, graphNnz, cacheSize, safety, cut, tree))
+            throw Error(RACE_ERR_GRAPH_TRAVERSAL,
+                        "MPK recursion: rows of a hopeless group went missing, or its boundary groups do not exist");
+        std::vector<int> buf{(int)tree.size()};
+        for (const race::MpkLeaf &l : tree) {
+            buf.insert(buf.end(), {l.lo, l.hi, l.stage, l.parent, (int)l.groupPtr.size() - 1});
+            buf.insert(buf.end(), l.groupPtr.begin(), l.groupPtr.end());
+            buf.push_back((int)l.hopeless.size());
+            buf.insert(buf.end(), l.hopeless.begin(), l.hopeless.end());
+        }
+        *treeLen = (int)buf.size();
+        if (treeBuf && cap >= *treeLen) memcpy(treeBuf, buf.data(), sizeof(int) * buf.size());
         memcpy(totalPerm, tp.data(), sizeof(int) * n);
         memcpy(totalInvPerm, ti.data(), sizeof(int) * n);
     });

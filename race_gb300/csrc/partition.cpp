@@ -119,19 +119,23 @@ std::vector<int> hopelessRegions(std::vector<int> violated, int totalLevel, int 
     return out;
 }
 
-}  // namespace
-
-StagePartition stagePartition(const LevelData &ld, int startRow, int power, int graphRows, long long graphNnz,
-                              double cacheSize, double safety, int cutoff) {
-    StagePartition sp;
-    const int L = ld.totalLevel;
-    std::vector<int> levelPtr(L + 1, startRow);
-    for (int l = 0; l < L; ++l) levelPtr[l + 1] = levelPtr[l] + ld.levelRow[l];
+// consolidatePartition (matrixPower.cpp:685-940) for one domain of L >= 1
+// levels: levelPtr (L+1 row offsets) of the stage's rows, nnzInLevel the
+// non-zeros of each level including those of the boundary regions
+// (getElemUpperLimit, :88-99), bndPtr the level offsets (L+1) of each
+// boundary region. bndGroupPtr gets each region's offsets at the
+// consolidated group starts (newBoundaryLevelPtr). False where a hopeless
+// region lacks its boundary levels (the reference stops there).
+bool consolidate(const std::vector<int> &levelPtr, const std::vector<int> &nnzInLevel, int power, int graphRows,
+                 long long graphNnz, double cacheSize, double safety, int cutoff,
+                 const std::vector<std::vector<int>> &bndPtr, StagePartition &sp,
+                 std::vector<std::vector<int>> &bndGroupPtr) {
+    const int L = (int)nnzInLevel.size();
     // getBytePerNNZ / getElemUpperLimit (matrixPower.cpp:88-99, 134-140)
     const double nnzr = graphNnz / (double)graphRows;
     const double bpn = (double)(((1 + power / nnzr) * sizeof(double) + (1 + 1 / nnzr) * sizeof(int)));
     const double cacheElem = cacheSize / bpn;
-    auto elem = [&](int l) { return safety * (power + 1) * ld.levelNnz[l]; };
+    auto elem = [&](int l) { return safety * (power + 1) * nnzInLevel[l]; };
 
     std::vector<int> violated;
     for (int l = 0; l < L; ++l) {
@@ -140,15 +144,11 @@ StagePartition stagePartition(const LevelData &ld, int startRow, int power, int 
     }
     const std::vector<int> hr = hopelessRegions(violated, L, power);
 
-    // consolidatePartition (matrixPower.cpp:685-940) for one domain
-    if (L == 0) {
-        sp.groupPtr = {startRow, startRow};
-        sp.unlockRow = {startRow};
-        sp.dangerRow = {startRow};
-        return sp;
-    }
     std::vector<int> unlock(L + 1, 0), danger(L + 1, 0);
-    sp.groupPtr.push_back(levelPtr[0]);
+    sp.groupPtr.assign(1, levelPtr[0]);
+    sp.hopeless.clear();
+    bndGroupPtr.assign(bndPtr.size(), {});
+    for (size_t b = 0; b < bndPtr.size(); ++b) bndGroupPtr[b].push_back(bndPtr[b][0]);
     unlock[0] = levelPtr[std::min(1, L)];
     const int boundary = power - 1;
     int count = 0, hs, he;
@@ -156,6 +156,7 @@ StagePartition stagePartition(const LevelData &ld, int startRow, int power, int 
     int group = 0, levelCtr = 0;
     double sumElem = 0;
     for (int level = 0; level < L; ++level) {
+        if (hs >= 0 && (hs - boundary < 0 || he + boundary > L - 1)) return false;
         const double cur = elem(level);
         sumElem += cur;
         bool hopeless = false, force = false;
@@ -175,6 +176,7 @@ StagePartition stagePartition(const LevelData &ld, int startRow, int power, int 
         if (levelCtr > 0 && !hopeless && (sumElem >= cacheElem || force)) {
             sumElem = cur;
             sp.groupPtr.push_back(levelPtr[level]);
+            for (size_t b = 0; b < bndPtr.size(); ++b) bndGroupPtr[b].push_back(bndPtr[b][level]);
             danger[group] = levelPtr[level - 1];
             if (level + 1 <= L) unlock[group + 1] = levelPtr[level + 1];
             ++group;
@@ -182,10 +184,228 @@ StagePartition stagePartition(const LevelData &ld, int startRow, int power, int 
         ++levelCtr;
     }
     sp.groupPtr.push_back(levelPtr[L]);
+    for (size_t b = 0; b < bndPtr.size(); ++b) bndGroupPtr[b].push_back(bndPtr[b][L]);
     danger[group] = levelPtr[L - 1];
     ++group;
     sp.unlockRow.assign(unlock.begin(), unlock.begin() + group);
     sp.dangerRow.assign(danger.begin(), danger.begin() + group);
+    return true;
+}
+
+struct Range {
+    int lo, hi;
+};
+
+// Per-row scratch of the leaf traversals, all -1 / 0 between leaves.
+struct Scratch {
+    std::vector<int> level;
+    std::vector<char> seen, boundary;
+    std::vector<int> frontier, next, sorted;
+    explicit Scratch(int n) : level(n, -1), seen(n, 0), boundary(n, 0) {}
+};
+
+// One recursion stage's traversal (Traverse on a range with boundaries,
+// traverse_GAP_graphSoA.cpp:31-90, 135-330, 452-575): a BFS of rows
+// [lo, hi) from lo that also walks, without counting them, the rows of the
+// boundary regions; islands of the range restart it on the same level;
+// unvisited boundary rows get the level after the last (at least one level
+// in all). The range and then every boundary region are sorted stably by
+// level and the sort is composed into totalPerm/totalInvPerm (new index ->
+// original row and back). Row lengths of the traversal graph give each
+// level's non-zeros. Returns the number of levels, or -1 if rows of the
+// range went missing. levelPtr/nnzInLevel: the range's level offsets and
+// the non-zeros of range and boundary rows per level; bndPtr: each boundary
+// region's level offsets.
+int traverseLeaf(int n, const int *rowPtr, const int *col, std::vector<int> &totalPerm,
+                 std::vector<int> &totalInvPerm, int lo, int hi, const std::vector<Range> &bnd, Scratch &s,
+                 std::vector<int> *levelPtr, std::vector<int> *nnzInLevel, std::vector<std::vector<int>> *bndPtr) {
+    for (const Range &r : bnd)
+        for (int i = r.lo; i < r.hi; ++i) s.boundary[i] = 1;
+    int counted = 0, lvl = 0, restart = lo;
+    s.frontier.clear();
+    if (lo < hi) {
+        s.frontier.push_back(lo);
+        s.seen[lo] = 1;
+        s.level[lo] = 0;
+        counted = 1;
+    }
+    bool missing = false;
+    while (!s.frontier.empty()) {
+        ++lvl;
+        s.next.clear();
+        for (int u : s.frontier) {
+            const int pu = totalPerm[u];
+            for (int idx = rowPtr[pu]; idx < rowPtr[pu + 1]; ++idx) {
+                if (col[idx] >= n) continue;
+                const int c = totalInvPerm[col[idx]];
+                if (s.seen[c]) continue;
+                const bool inside = c >= lo && c < hi;
+                if (!inside && !s.boundary[c]) continue;
+                s.seen[c] = 1;
+                s.level[c] = lvl;
+                s.next.push_back(c);
+                counted += inside;
+            }
+        }
+        s.frontier.swap(s.next);
+        if (s.frontier.empty() && counted != hi - lo) {
+            while (restart < hi && s.seen[restart]) ++restart;
+            if (restart == hi) {
+                missing = true;
+                break;
+            }
+            s.seen[restart] = 1;
+            s.level[restart] = lvl;
+            s.frontier.push_back(restart);
+            ++counted;
+        }
+    }
+    int levels = lvl;
+    bool untouched = false;
+    for (const Range &r : bnd)
+        for (int i = r.lo; i < r.hi; ++i)
+            if (!s.seen[i]) {
+                s.level[i] = lvl;
+                untouched = true;
+            }
+    levels += untouched ? 1 : 0;
+    levels = std::max(levels, 1);
+
+    std::vector<Range> regions{{lo, hi}};
+    regions.insert(regions.end(), bnd.begin(), bnd.end());
+    if (!missing) {
+        if (levelPtr) {
+            levelPtr->assign(levels + 1, lo);
+            nnzInLevel->assign(levels, 0);
+            bndPtr->assign(bnd.size(), {});
+            for (size_t k = 0; k < regions.size(); ++k) {
+                std::vector<int> rows(levels + 1, 0);
+                for (int i = regions[k].lo; i < regions[k].hi; ++i) {
+                    ++rows[s.level[i] + 1];
+                    const int pi = totalPerm[i];
+                    (*nnzInLevel)[s.level[i]] += rowPtr[pi + 1] - rowPtr[pi];
+                }
+                rows[0] = regions[k].lo;
+                for (int l = 0; l < levels; ++l) rows[l + 1] += rows[l];
+                if (k == 0)
+                    *levelPtr = rows;
+                else
+                    (*bndPtr)[k - 1] = rows;
+            }
+        }
+        // stable sort of each region by level, composed into the permutation
+        for (const Range &rg : regions) {
+            const int a = rg.lo, b = rg.hi;
+            std::vector<int> start(levels + 1, 0);
+            for (int i = a; i < b; ++i) ++start[s.level[i] + 1];
+            for (int l = 0; l < levels; ++l) start[l + 1] += start[l];
+            s.sorted.assign(b - a, 0);
+            for (int i = a; i < b; ++i) s.sorted[start[s.level[i]]++] = totalPerm[i];
+            for (int i = a; i < b; ++i) {
+                totalPerm[i] = s.sorted[i - a];
+                totalInvPerm[totalPerm[i]] = i;
+            }
+        }
+    }
+    for (const Range &rg : regions)
+        for (int i = rg.lo; i < rg.hi; ++i) {
+            s.seen[i] = 0;
+            s.boundary[i] = 0;
+            s.level[i] = -1;
+        }
+    return missing ? -1 : levels;
+}
+
+// The direct boundaries of hopeless group h of a leaf with groups groupPtr
+// (its own groups h-w..h+w but h) and, with w >= 1, the sub-ranges
+// h-w..h+w of every boundary region of the leaf by its consolidated group
+// offsets, h-1..h+1 as one range (matrixPowerRecursive.cpp:199-287). Empty
+// ranges are left out; false if a group index falls outside the leaf.
+bool childBoundaries(const std::vector<int> &groupPtr, const std::vector<std::vector<int>> &bndGroupPtr, int h,
+                     int w, std::vector<Range> &out) {
+    const int G = (int)groupPtr.size() - 1;
+    out.clear();
+    if (h - w < 0 || h + w + 1 > G) return false;
+    if (w > 0)
+        for (const std::vector<int> &bp : bndGroupPtr)
+            for (int r = -w; r <= w; ++r) {
+                Range rg;
+                if (r == -1) {
+                    rg = {bp[h - 1], bp[h + 2]};
+                    r = 1;
+                } else {
+                    rg = {bp[h + r], bp[h + r + 1]};
+                }
+                if (rg.hi > rg.lo) out.push_back(rg);
+            }
+    for (int r = -w; r <= w; ++r)
+        if (r != 0 && groupPtr[h + r + 1] > groupPtr[h + r]) out.push_back({groupPtr[h + r], groupPtr[h + r + 1]});
+    return true;
+}
+
+struct RecursionContext {
+    int n;
+    const int *rowPtr, *col;
+    std::vector<int> &totalPerm, &totalInvPerm;
+    int power;
+    long long graphNnz;
+    double cacheSize, safety;
+    const std::vector<int> &stageCutoff;
+    std::vector<MpkLeaf> &tree;
+    Scratch scratch;
+};
+
+// recursivePartition (matrixPowerRecursive.cpp:156-298) below leaf `parent`
+// whose boundary regions have consolidated offsets bndGroupPtr.
+bool recurse(RecursionContext &ctx, int parent, const std::vector<std::vector<int>> &bndGroupPtr) {
+    const int w = (ctx.power + 1) / 2 - 1;  // ceil(power/2) - 1 (workingBoundaryLength_base)
+    const std::vector<int> hid = ctx.tree[parent].hopeless;
+    const std::vector<int> gp = ctx.tree[parent].groupPtr;
+    const int stage = ctx.tree[parent].stage + 1;
+    const int cutoff = stage < (int)ctx.stageCutoff.size() ? ctx.stageCutoff[stage] : INT_MAX;
+    std::vector<Range> bnd;
+    for (int h : hid) {
+        if (h < 0 || h >= (int)gp.size() - 1 || !childBoundaries(gp, bndGroupPtr, h, w, bnd)) return false;
+        MpkLeaf leaf;
+        leaf.lo = gp[h];
+        leaf.hi = gp[h + 1];
+        leaf.stage = stage;
+        leaf.parent = parent;
+        std::vector<int> levelPtr, nnzInLevel;
+        std::vector<std::vector<int>> bndPtr, childBnd;
+        if (traverseLeaf(ctx.n, ctx.rowPtr, ctx.col, ctx.totalPerm, ctx.totalInvPerm, leaf.lo, leaf.hi, bnd,
+                         ctx.scratch, &levelPtr, &nnzInLevel, &bndPtr) < 0)
+            return false;
+        StagePartition sp;
+        if (!consolidate(levelPtr, nnzInLevel, ctx.power, ctx.n, ctx.graphNnz, ctx.cacheSize, ctx.safety, cutoff,
+                         bndPtr, sp, childBnd))
+            return false;
+        leaf.groupPtr = sp.groupPtr;
+        leaf.hopeless = sp.hopeless;
+        ctx.tree.push_back(leaf);
+        const int idx = (int)ctx.tree.size() - 1;
+        if (!sp.hopeless.empty() && !recurse(ctx, idx, childBnd)) return false;
+    }
+    return true;
+}
+
+}  // namespace
+
+StagePartition stagePartition(const LevelData &ld, int startRow, int power, int graphRows, long long graphNnz,
+                              double cacheSize, double safety, int cutoff) {
+    StagePartition sp;
+    const int L = ld.totalLevel;
+    if (L == 0) {
+        sp.groupPtr = {startRow, startRow};
+        sp.unlockRow = {startRow};
+        sp.dangerRow = {startRow};
+        return sp;
+    }
+    std::vector<int> levelPtr(L + 1, startRow);
+    for (int l = 0; l < L; ++l) levelPtr[l + 1] = levelPtr[l] + ld.levelRow[l];
+    std::vector<int> nnzInLevel(ld.levelNnz.begin(), ld.levelNnz.begin() + L);
+    std::vector<std::vector<int>> none;
+    consolidate(levelPtr, nnzInLevel, power, graphRows, graphNnz, cacheSize, safety, cutoff, {}, sp, none);
     return sp;
 }
 
@@ -194,87 +414,37 @@ bool recursePermutation(int n, const int *rowPtr, const int *col, std::vector<in
                         const std::vector<int> &hopeless, int power) {
     const int G = (int)groupPtr.size() - 1;
     const int w = (power + 1) / 2 - 1;  // ceil(power/2) - 1 (workingBoundaryLength_base)
-    std::vector<int> level(n, -1);
-    std::vector<char> seen(n, 0), boundary(n, 0);
-    std::vector<int> frontier, next, sorted;
+    Scratch s(n);
+    std::vector<Range> bnd;
     for (int h : hopeless) {
         if (h < 0 || h >= G) return false;
-        const int lo = groupPtr[h], hi = groupPtr[h + 1];
-        std::vector<std::pair<int, int>> regions{{lo, hi}};
+        bnd.clear();
         for (int r = -w; r <= w; ++r) {
             const int g = h + r;
             if (r == 0 || g < 0 || g >= G || groupPtr[g + 1] <= groupPtr[g]) continue;
-            regions.emplace_back(groupPtr[g], groupPtr[g + 1]);
-            for (int i = groupPtr[g]; i < groupPtr[g + 1]; ++i) boundary[i] = 1;
+            bnd.push_back({groupPtr[g], groupPtr[g + 1]});
         }
-        // BFS from lo (the rows are new indices; their neighbours are looked
-        // up through the running permutation)
-        int counted = 0, lvl = 0, restart = lo;
-        frontier.clear();
-        if (lo < hi) {
-            frontier.push_back(lo);
-            seen[lo] = 1;
-            level[lo] = 0;
-            counted = 1;
-        }
-        while (!frontier.empty()) {
-            ++lvl;
-            next.clear();
-            for (int u : frontier) {
-                const int pu = totalPerm[u];
-                for (int idx = rowPtr[pu]; idx < rowPtr[pu + 1]; ++idx) {
-                    if (col[idx] >= n) continue;
-                    const int c = totalInvPerm[col[idx]];
-                    if (seen[c]) continue;
-                    const bool inside = c >= lo && c < hi;
-                    if (!inside && !boundary[c]) continue;
-                    seen[c] = 1;
-                    level[c] = lvl;
-                    next.push_back(c);
-                    counted += inside;
-                }
-            }
-            frontier.swap(next);
-            if (frontier.empty() && counted != hi - lo) {
-                while (restart < hi && seen[restart]) ++restart;
-                if (restart == hi) return false;
-                seen[restart] = 1;
-                level[restart] = lvl;
-                frontier.push_back(restart);
-                ++counted;
-            }
-        }
-        int levels = lvl;
-        bool untouched = false;
-        for (size_t k = 1; k < regions.size(); ++k)
-            for (int i = regions[k].first; i < regions[k].second; ++i)
-                if (!seen[i]) {
-                    level[i] = lvl;
-                    untouched = true;
-                }
-        levels += untouched ? 1 : 0;
-        levels = std::max(levels, 1);
-        // stable sort of each region by level, composed into the permutation
-        for (const auto &rg : regions) {
-            const int a = rg.first, b = rg.second;
-            std::vector<int> start(levels + 1, 0);
-            for (int i = a; i < b; ++i) ++start[level[i] + 1];
-            for (int l = 0; l < levels; ++l) start[l + 1] += start[l];
-            sorted.assign(b - a, 0);
-            for (int i = a; i < b; ++i) sorted[start[level[i]]++] = totalPerm[i];
-            for (int i = a; i < b; ++i) {
-                totalPerm[i] = sorted[i - a];
-                totalInvPerm[totalPerm[i]] = i;
-            }
-        }
-        for (const auto &rg : regions)
-            for (int i = rg.first; i < rg.second; ++i) {
-                seen[i] = 0;
-                boundary[i] = 0;
-                level[i] = -1;
-            }
+        if (traverseLeaf(n, rowPtr, col, totalPerm, totalInvPerm, groupPtr[h], groupPtr[h + 1], bnd, s, nullptr,
+                         nullptr, nullptr) < 0)
+            return false;
     }
     return true;
+}
+
+bool recursivePartition(int n, const int *rowPtr, const int *col, std::vector<int> &totalPerm,
+                        std::vector<int> &totalInvPerm, const StagePartition &root, int power, long long graphNnz,
+                        double cacheSize, double safety, const std::vector<int> &stageCutoff,
+                        std::vector<MpkLeaf> &tree) {
+    tree.clear();
+    MpkLeaf r;
+    r.lo = 0;
+    r.hi = n;
+    r.groupPtr = root.groupPtr;
+    r.hopeless = root.hopeless;
+    tree.push_back(r);
+    RecursionContext ctx{n, rowPtr, col, totalPerm, totalInvPerm, power, graphNnz, cacheSize, safety, stageCutoff,
+                         tree, Scratch(n)};
+    return recurse(ctx, 0, {});
 }
 
 }  // namespace race

@@ -39,4 +39,33 @@ bool recursePermutation(int n, const int *rowPtr, const int *col, std::vector<in
                         std::vector<int> &totalInvPerm, const std::vector<int> &groupPtr,
                         const std::vector<int> &hopeless, int power);
 
+// One leaf of the MPK recursion tree (MPLeaf, include/matrixPowerRecursive.h):
+// its rows, stage, parent leaf, consolidated level groups and hopeless groups.
+struct MpkLeaf {
+    int lo = 0, hi = 0, stage = 0, parent = -1;
+    std::vector<int> groupPtr;  // MPLeaf::lp
+    std::vector<int> hopeless;  // MPLeaf::hid
+};
+
+// The whole MPK recursion below a stage-0 partition `root` of rows [0, n)
+// (mtxPowerRecursive::recursivePartition, matrixPowerRecursive.cpp:156-338),
+// at any depth. Depth first, for each hopeless group h of a leaf in turn, a
+// child leaf takes the group's rows and as boundaries (:199-287) the leaf's
+// own groups h-w..h+w other than h and, of every boundary region of the
+// leaf, its consolidated level groups h-w..h+w (h-1..h+1 as one region),
+// w = ceil(power/2)-1, empty ranges left out. The child's BFS (as in
+// recursePermutation) permutes its rows and boundary rows; its levels are
+// then partitioned like stage 0 (mtxPower::findPartition, matrixPower.cpp:
+// 505-605) except that a level's size includes the boundary rows' non-zeros
+// of that level (getElemUpperLimit, :88-99), with the cut-off of its stage,
+// stageCutoff[stage] (INT_MAX from stageCutoff.size() on); a child with
+// hopeless groups recurses before its next sibling is built. Every stage's
+// permutation is composed into totalPerm/totalInvPerm; `tree` gets the root
+// and every leaf in the reference's order. Returns false if rows of a group
+// went missing or a hopeless group lacks its boundary groups.
+bool recursivePartition(int n, const int *rowPtr, const int *col, std::vector<int> &totalPerm,
+                        std::vector<int> &totalInvPerm, const StagePartition &root, int power, long long graphNnz,
+                        double cacheSize, double safety, const std::vector<int> &stageCutoff,
+                        std::vector<MpkLeaf> &tree);
+
 }  // namespace race

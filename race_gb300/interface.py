@@ -117,7 +117,12 @@ class Interface:
     """RACE::Interface(nrow, nthreads, dist, rowPtr, col, symm_hint, SMT,
     pinMethod, initPerm, initInvPerm, d2Type, lbTarget) (interface.h:124).
     SMT and pinMethod are accepted for signature parity; thread pinning has no
-    meaning on the GPU."""
+    meaning on the GPU. ``params`` overrides the reference's environment
+    knobs (read from the environment otherwise): ``efficiency`` and
+    ``lvl_threads`` (RACE_EFFICIENCY, RACE_THREADS), ``cache_violation_cutoff``
+    (RACE_CACHE_VIOLATION_CUTOFF_DEFAULT), ``cache_violation_cutoffs`` (the
+    list RACE_CACHE_VIOLATION_CUTOFF: entry k is the cut-off of MPK
+    recursion stage k) and ``max_recursion_stages`` (RACE_MAX_RECURSION_STAGES)."""
 
     def __init__(self, nrow: int, nthreads: int, dist: int, rowPtr, col, symm_hint: bool = False, SMT: int = 1,
                  pinMethod: int = SCATTER, initPerm=None, initInvPerm=None, d2Type: int = TWO_BLOCK,
@@ -147,6 +152,11 @@ class Interface:
                 cparams.cache_violation_cutoff = int(params["cache_violation_cutoff"])
             if "max_recursion_stages" in params:
                 cparams.max_recursion_stages = int(params["max_recursion_stages"])
+            if "cache_violation_cutoffs" in params:
+                cuts = [int(v) for v in params["cache_violation_cutoffs"]][:16]
+                cparams.n_cutoffs = len(cuts)
+                for i, v in enumerate(cuts):
+                    cparams.cutoffs[i] = v
         h = C.c_void_p()
         check(lib().race_create(C.byref(h), self.nrow, int(nthreads), int(dist), rp.ctypes.data, cl.ctypes.data,
                                 int(bool(symm_hint)), None if ip is None else ip.ctypes.data,

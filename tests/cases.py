@@ -166,6 +166,31 @@ def key_hopeless(m, p, c):
     return f"hopeless__{m}__p{p}__c{int(c)}"
 
 
+# MPK partitions that recurse deeper than one stage: (matrix, power,
+# cacheBytes, RACE_MAX_RECURSION_STAGES (-1: unset), RACE_CACHE_VIOLATION_CUTOFF
+# list). The reference's whole leaf tree and permutation are stored. Powers
+# 2, 3-4, 5-6 and 8 give boundary widths ceil(p/2)-1 = 0, 1, 2 and 3.
+DEEP_CASES = [("band_5k", 8, 3000, 2, ()), ("band_5k", 8, 3000, -1, (50, 1)), ("band_5k", 8, 3000, 3, (50, 1, 1)),
+              ("plaw_3k", 3, 2000, 3, (50, 2, 1)), ("st27_24", 2, 2000, 3, (50, 2, 1)),
+              ("st27_24", 5, 20000, 3, (50, 2, 1)), ("lap7_32", 4, 10000, 2, ()),
+              ("aniso5_120x90", 6, 2000, 3, (50, 2, 1)), ("plaw_20k", 4, 10000, 2, ())]
+# deep cases whose reference MPK outputs are stored
+DEEP_EXEC_CASES = {("band_5k", 8, 3000, -1, (50, 1)), ("plaw_3k", 3, 2000, 3, (50, 2, 1))}
+
+
+def key_deep(m, p, c, stages, cuts):
+    return f"deep__{m}__p{p}__c{int(c)}__s{stages}__k{'-'.join(str(v) for v in cuts)}"
+
+
+def deep_stage_cutoffs(stages, cuts, default=50):
+    """The cut-off of each recursion stage s < the maximal depth
+    (get_cache_violation_cutoff, matrixPowerRecursive.cpp:81-100); deeper
+    stages have none (INT_MAX)."""
+    cv = [default] + list(cuts)
+    depth = stages if stages >= 0 else len(cv)
+    return [cv[s + 1] if s < len(cv) - 1 else cv[0] for s in range(depth)]
+
+
 # (matrix, triangle, power, cacheBytes): the lower ("L") or upper ("U")
 # triangle of the matrix, partitioned with mtxType L / U (one row per level,
 # traverse_GAP_graphSoA.cpp:316-335)

@@ -9,8 +9,9 @@ threads/efficiency/stage depth, MPK level groups and the reference's sweep
 and MPK outputs for a few small cases; coloring variants (THREE_BLOCK, an
 initial permutation, row balancing, environment knobs, unsymmetric
 patterns); MPK partitions with hopeless regions (level groups, hopeless
-groups, the permutation after the recursion), without recursion, and of
-triangular matrices; the load balancer on level histograms; simdify /
+groups, the permutation after the recursion), without recursion, with
+recursion deeper than one stage (the whole leaf tree), and of triangular
+matrices; the load balancer on level histograms; simdify /
 simdifyD1 outputs. The reference's executor runs on
 OpenMP threads; its outputs are deterministic for valid colorings.
 Full-size configurations are stored as digests only.
@@ -34,7 +35,8 @@ from cases import (COLOR3_CASES, COLOR_CASES, COLOR_ENV_CASES, COLOR_INIT_CASES,
                    COLOR_UNSYM_CASES, EXEC_CASES, POWER_SAFETY_CASES, key_power_safety, HOPELESS_CASES, MATRICES, POWER_CASES, POWER_FLAT_CASES, POWER_TRI_CASES,  # noqa: E402
                    SIMDIFY_CASES, TRAVERSE_CASES, arr_digest, digest, key_color, key_power, key_power_flat,
                    init_perm, key_color3, key_color_env, key_color_init, key_color_row, key_color_unsym,
-                   key_hopeless, key_power_tri, key_simdify, key_trav, sell_layout, triangle)
+                   key_hopeless, key_power_tri, key_simdify, key_trav, sell_layout, triangle,
+                   DEEP_CASES, DEEP_EXEC_CASES, key_deep)
 from oracle import refpy  # noqa: E402
 from oracle.refpy import RefInterface  # noqa: E402
 from race_gb300 import matgen  # noqa: E402
@@ -333,6 +335,37 @@ def main():
         g[k + "__lp"] = np.array(tr[0]["lp"], np.int32)
         g[k + "__leaves"] = np.array(len(tr))
         print(k, "groups", len(tr[0]["lp"]) - 1)
+
+    # recursion deeper than one stage: the whole leaf tree (count, then per
+    # leaf lo, hi, stage, parent, groups, lp, hopeless count, hid) and the
+    # permutation
+    for m, p, c, stages, cuts in DEEP_CASES:
+        A = M(m)
+        k = key_deep(m, p, c, stages, cuts)
+        env = {"RACE_MAX_RECURSION_STAGES": str(stages) if stages >= 0 else None,
+               "RACE_CACHE_VIOLATION_CUTOFF": ",".join(str(v) for v in cuts) or None}
+        for var, val in env.items():
+            if val is not None:
+                os.environ[var] = val
+        try:
+            rp = refpy.RefPower(A, p, c)
+            perm, ip = rp.perm()
+            tr = rp.tree()
+            assert (rp.coverage() == 1).all()
+            if (m, p, c, stages, cuts) in DEEP_EXEC_CASES:
+                g[k + "__out"] = rp.execute(A.permuted(perm, ip), matgen.uniform_vector(A.n, 0))[1:]
+            rp.close()
+        finally:
+            for var in env:
+                os.environ.pop(var, None)
+        flat = [len(tr)]
+        for leaf in tr:
+            flat += [leaf["lo"], leaf["hi"], leaf["stage"], leaf["parent"], len(leaf["lp"]) - 1] + leaf["lp"]
+            flat += [len(leaf["hid"])] + leaf["hid"]
+        g[k + "__digest"] = np.array(digest(A))
+        g[k + "__tree"] = np.array(flat, np.int32)
+        g[k + "__perm"] = perm
+        print(k, "leaves", len(tr), "deepest stage", max(leaf["stage"] for leaf in tr))
 
     # full-size MPK configuration: digests only
     A = matgen.stencil3d_27pt(128)

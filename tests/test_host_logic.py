@@ -289,6 +289,13 @@ def test_params_from_env_reads_recursion_stages(monkeypatch):
     monkeypatch.setenv("RACE_MAX_RECURSION_STAGES", "0")
     _lib.check(L.race_params_from_env(C.byref(p)))
     assert p.max_recursion_stages == 0
+    # the per-stage list RACE_CACHE_VIOLATION_CUTOFF after the default
+    # (matrixPowerRecursive.cpp:39-48)
+    assert p.n_cutoffs == 0
+    monkeypatch.setenv("RACE_CACHE_VIOLATION_CUTOFF_DEFAULT", "30")
+    monkeypatch.setenv("RACE_CACHE_VIOLATION_CUTOFF", "50,2,1")
+    _lib.check(L.race_params_from_env(C.byref(p)))
+    assert p.cache_violation_cutoff == 30 and p.n_cutoffs == 3 and list(p.cutoffs[:3]) == [50, 2, 1]
 
 
 def _conflicts(P, pp, lo, hi, dist):
@@ -531,6 +538,97 @@ def test_mpk_recursion_matches_reference(golden, mats):
                                                 gp.ctypes.data, gp.size - 1, hid.ctypes.data, hid.size, p))
         np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
         np.testing.assert_array_equal(ti[tp], np.arange(A.n))
+
+
+def _recursive_partition(A, p, c, stage_cutoffs, safety=2.0):
+    """Stage 0 from the oracle's BFS (race_mpk_stage_partition), then the
+    engine's recursion below it (race_mpk_recursive_partition): the flat
+    leaf tree and the permutation."""
+    L = _lib.lib()
+    tp, ti, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+    c0 = stage_cutoffs[0] if stage_cutoffs else 2**31 - 1
+    gp, hid = _stage_partition(lr, ln, A.n, A.nnz, p, c, c0, safety)
+    gp, hid = np.ascontiguousarray(gp, np.int32), np.ascontiguousarray(hid, np.int32)
+    rp, cl = np.ascontiguousarray(A.row_ptr, np.int32), np.ascontiguousarray(A.col, np.int32)
+    tp, ti = np.ascontiguousarray(tp, np.int32), np.ascontiguousarray(ti, np.int32)
+    sc = np.ascontiguousarray(list(stage_cutoffs) or [0], np.int32)
+    tl = C.c_int()
+    tree = np.zeros(1 << 16, np.int32)
+    _lib.check(L.race_mpk_recursive_partition(A.n, rp.ctypes.data, cl.ctypes.data, tp.ctypes.data, ti.ctypes.data,
+                                              gp.ctypes.data, gp.size - 1, hid.ctypes.data, hid.size, p, A.nnz,
+                                              float(c), float(safety), sc.ctypes.data, len(stage_cutoffs),
+                                              tree.ctypes.data, tree.size, C.byref(tl)))
+    assert 0 < tl.value <= tree.size
+    return tree[: tl.value], tp, ti
+
+
+def test_mpk_deep_recursion_matches_reference(golden, mats):
+    """The MPK partition's recursion deeper than one stage
+    (RACE_MAX_RECURSION_STAGES > 1, a list of cut-offs per stage;
+    mtxPowerRecursive::recursivePartition, matrixPowerRecursive.cpp:156-338)
+    computed by the engine on the host gives the reference's whole leaf tree
+    (each leaf's rows, stage, parent, level groups and hopeless groups) and
+    its permutation, for boundary widths 0 to 3 and up to three stages."""
+    from cases import DEEP_CASES, deep_stage_cutoffs, key_deep
+    deepest = 0
+    for m, p, c, stages, cuts in DEEP_CASES:
+        A = mats[m]
+        k = key_deep(m, p, c, stages, cuts)
+        assert str(golden[k + "__digest"]) == digest(A)
+        tree, tp, ti = _recursive_partition(A, p, c, deep_stage_cutoffs(stages, cuts))
+        np.testing.assert_array_equal(tree, golden[k + "__tree"], err_msg=k)
+        np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
+        np.testing.assert_array_equal(ti[tp], np.arange(A.n))
+        deepest = max(deepest, max(int(v) for v in _leaf_stages(tree)))
+    assert deepest == 3
+
+
+def _leaf_stages(tree):
+    k, out = 1, []
+    for _ in range(int(tree[0])):
+        out.append(tree[k + 2])
+        k += 5 + int(tree[k + 4]) + 1
+        k += 1 + int(tree[k])
+    return out
+
+
+def test_mpk_one_stage_recursion_is_the_general_one(golden, mats):
+    """At the default depth (one stage past the cut-off list: stage 1 has no
+    cut-off) the general recursion gives the one-stage permutation of the
+    reference's default partitions, and one leaf per hopeless group."""
+    from cases import HOPELESS_CASES, key_hopeless
+    for m, p, c in HOPELESS_CASES:
+        A = mats[m]
+        k = key_hopeless(m, p, c)
+        tree, tp, _ = _recursive_partition(A, p, c, [50])
+        np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
+        assert int(tree[0]) == int(golden[k + "__leaves"]) == 1 + len(golden[k + "__hid"])
+
+
+def test_mpk_recursive_partition_rejects_invalid_input():
+    """Group offsets that do not cover the rows, hopeless indices outside
+    the groups and missing arrays are refused before any work."""
+    L = _lib.lib()
+    A = matgen.laplace3d_7pt(4)
+    rp, cl = np.ascontiguousarray(A.row_ptr, np.int32), np.ascontiguousarray(A.col, np.int32)
+    tp = np.arange(A.n, dtype=np.int32)
+    ti = tp.copy()
+    sc = np.array([50, 50], np.int32)
+    tl = C.c_int()
+
+    def call(gp, hid, n=A.n, stages=2):
+        gp, hid = np.ascontiguousarray(gp, np.int32), np.ascontiguousarray(hid, np.int32)
+        return L.race_mpk_recursive_partition(n, rp.ctypes.data, cl.ctypes.data, tp.ctypes.data, ti.ctypes.data,
+                                              gp.ctypes.data, gp.size - 1, hid.ctypes.data, hid.size, 4, A.nnz, 1e4,
+                                              2.0, sc.ctypes.data, stages, None, 0, C.byref(tl))
+    assert call([0, 10, A.n], []) == _lib.RACE_SUCCESS and int(tl.value) == 1 + 5 + 3 + 1  # the root alone
+    assert call([0, 10, A.n - 1], []) == _lib.RACE_ERR_INVALID_ARG
+    assert call([0, 10, 5, A.n], []) == _lib.RACE_ERR_INVALID_ARG
+    assert call([0, 10, A.n], [2]) == _lib.RACE_ERR_INVALID_ARG
+    assert call([0, 10, A.n], [], stages=-1) == _lib.RACE_ERR_INVALID_ARG
+    # a hopeless group without p-1 groups on either side has no boundaries to take
+    assert call([0, 10, A.n], [0]) == _lib.RACE_ERR_GRAPH_TRAVERSAL
+    np.testing.assert_array_equal(tp, np.arange(A.n))  # untouched on errors
 
 
 def test_level_recursion_from_an_initial_permutation(golden, mats):

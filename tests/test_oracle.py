@@ -215,6 +215,21 @@ def test_reference_mpk_on_recursive_partitions_equals_spmv_chain(golden, mats):
     assert checked == 2
 
 
+def test_reference_mpk_on_deep_partitions_equals_spmv_chain(golden, mats):
+    """With recursion deeper than one stage too, the reference's MPK executor
+    (recursivePowerCallSerial over the whole leaf tree) gives p sequential
+    SpMVs of the permuted matrix bit for bit."""
+    from cases import DEEP_EXEC_CASES, key_deep
+    for m, p, c, stages, cuts in sorted(DEEP_EXEC_CASES):
+        k = key_deep(m, p, c, stages, cuts)
+        A = mats[m]
+        perm = golden[k + "__perm"]
+        inv = np.empty_like(perm)
+        inv[perm] = np.arange(A.n, dtype=np.int32)
+        Y = orc.mpk_plain(A.permuted(perm, inv), matgen.uniform_vector(A.n, 0), p)
+        np.testing.assert_array_equal(Y[1:], golden[k + "__out"], err_msg=k)
+
+
 @pytest.mark.parametrize("m,d,t", [c for c in COLOR_CASES if c[1] == 2])
 def test_validated_coloring_invariant(golden, mats, m, d, t):
     """The reference's own validation of a coloring (colorSymmSpMV.cpp:

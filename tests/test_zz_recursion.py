@@ -1,13 +1,14 @@
-"""MPK partitions with hopeless regions at the default settings, on the GPU:
-the engine's RACEColor(p, cacheSize) gives the reference's level groups and,
-after its one-stage recursion into the hopeless groups, the reference's
-permutation; the MPK on that partition equals p sequential SpMVs bit for
-bit. (The host parts are checked on the CPU in test_host_logic.py; this file
-runs last among the GPU tests.)"""
+"""MPK partitions with hopeless regions on the GPU: the engine's
+RACEColor(p, cacheSize) gives the reference's level groups and, after its
+recursion into the hopeless groups (one stage by default, deeper with
+max_recursion_stages or a list of cut-offs), the reference's permutation;
+the MPK on that partition equals p sequential SpMVs bit for bit. (The host
+parts are checked on the CPU in test_host_logic.py; this file runs last
+among the GPU tests.)"""
 import numpy as np
 import pytest
 
-from cases import HOPELESS_CASES, POWER_SAFETY_CASES, digest, key_hopeless, key_power_safety
+from cases import DEEP_CASES, HOPELESS_CASES, POWER_SAFETY_CASES, digest, key_deep, key_hopeless, key_power_safety
 from oracle import oracle as orc
 from race_gb300 import matgen
 
@@ -27,8 +28,15 @@ def test_default_partition_with_hopeless_regions(golden, mats, m, p, c):
     rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
     assert rc.RACEColor(p, c) == 0
     np.testing.assert_array_equal(rc.getPowerGroups(), golden[k + "__lp"])
+    _check_mpk(rc, A, p, golden[k + "__perm"])
+
+
+def _check_mpk(rc, A, p, want_perm):
+    """The engine's permutation is want_perm and its MPK on the permuted
+    matrix gives the oracle's p sequential SpMVs (bit for bit without hub
+    rows, which a warp sums in another order)."""
     perm, inv = rc.getPerm(), rc.getInvPerm()
-    np.testing.assert_array_equal(perm, golden[k + "__perm"])
+    np.testing.assert_array_equal(perm, want_perm)
     np.testing.assert_array_equal(inv[perm], np.arange(A.n))
     P = A.permuted(perm, inv)
     x0 = matgen.uniform_vector(A.n, 0)
@@ -48,11 +56,22 @@ def test_default_partition_with_hopeless_regions(golden, mats, m, p, c):
 
 
 @pytest.mark.gpu
-def test_deeper_recursion_is_refused(mats):
-    """More than one recursion stage is not built."""
-    A = mats["band_5k"]
-    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True, params={"max_recursion_stages": 2})
-    assert rc.RACEColor(8, 3000) == 10  # RACE_ERR_NOT_IMPLEMENTED
+@pytest.mark.parametrize("m,p,c,stages,cuts", DEEP_CASES)
+def test_deep_recursion(golden, mats, m, p, c, stages, cuts):
+    """Recursion deeper than one stage (RACE_MAX_RECURSION_STAGES and the
+    per-stage RACE_CACHE_VIOLATION_CUTOFF list, given as params): the
+    reference's stage-0 groups and its permutation after every stage."""
+    A = mats[m]
+    k = key_deep(m, p, c, stages, cuts)
+    params = {"cache_violation_cutoffs": list(cuts)}
+    if stages >= 0:
+        params["max_recursion_stages"] = stages
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True, params=params)
+    assert rc.RACEColor(p, c) == 0
+    tree = golden[k + "__tree"]
+    ng = int(tree[5])  # the root leaf: lo, hi, stage, parent, groups, lp
+    np.testing.assert_array_equal(rc.getPowerGroups(), tree[6:7 + ng])
+    _check_mpk(rc, A, p, golden[k + "__perm"])
 
 
 @pytest.mark.gpu
