@@ -62,6 +62,9 @@ def lib():
         L.orc_mpk_groups.restype = C.c_int
         L.orc_mpk_groups.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_double, C.c_double, C.c_int, C.c_int,
                                      IP, IP, IP, IP, IP]
+        L.orc_mpk_partition.restype = C.c_int
+        L.orc_mpk_partition.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_double, C.c_double, C.c_int, C.c_int,
+                                        IP, IP, C.c_int, IP, IP, IP, C.POINTER(C.c_int), IP]
         L.orc_mpk_unlock_ctr.argtypes = [C.c_int, IP, IP, C.c_int, IP]
         L.orc_mpk_wavefront.argtypes = [C.c_int, C.c_int, C.c_int, IP, IP, IP, C.c_int, IP, IP, DP, DP]
         _lib = L
@@ -101,13 +104,15 @@ def traverse(csr, dist: int, lo: int, hi: int, total_perm=None, total_inv=None):
     return tp, ti, lr[:L], ln[:L], d
 
 
-def traverse_boundary(csr, lo: int, hi: int, regions, total_perm, total_inv):
+def traverse_boundary(csr, lo: int, hi: int, regions, total_perm, total_inv, region_levels: bool = False):
     """One traversal of a recursion stage of the MPK partition: rows [lo,hi)
     with boundary regions [(lo_k, hi_k), ...] (orc_bfs_boundary), then the
     range and every boundary region each stably sorted by level and composed
     into the running permutation (permuteGraph, traverse_GAP_graphSoA.cpp:
-    506-575). Returns the new (total_perm, total_inv, levels of [lo,hi),
-    number of levels)."""
+    506-575). Returns the new (total_perm, total_inv, level rows and level
+    non-zeros of [lo,hi), number of levels), and with region_levels also the
+    (level rows, level non-zeros) of every boundary region
+    (createLevelData, :449-504)."""
     n = csr.n
     tp = _i32(total_perm).copy()
     ti = _i32(total_inv).copy()
@@ -120,9 +125,113 @@ def traverse_boundary(csr, lo: int, hi: int, regions, total_perm, total_inv):
     lr = np.zeros(L, np.int32)
     ln = np.zeros(L, np.int32)
     lib().orc_level_data(_i32(csr.row_ptr), tp, d, lo, hi, L, lr, ln)
+    per_region = []
+    for a, b in regions:
+        rr, rn = np.zeros(L, np.int32), np.zeros(L, np.int32)
+        lib().orc_level_data(_i32(csr.row_ptr), tp, d, a, b, L, rr, rn)
+        per_region.append((rr, rn))
     for a, b in [(lo, hi)] + list(regions):
         lib().orc_level_permute(n, d, a, b, L, tp, ti)
+    if region_levels:
+        return tp, ti, lr, ln, L, per_region
     return tp, ti, lr, ln, L
+
+
+INT_MAX = 2**31 - 1
+
+
+def mpk_partition(p: int, nrow: int, nnz: int, cache_bytes: float, safety: float, cutoff: int, level_ptr, level_nnz,
+                  bnd_ptrs=()):
+    """One stage of the MPK partition with hopeless regions
+    (orc_mpk_partition): (group row offsets, hopeless group indices, each
+    boundary region's offsets at the group starts), or None."""
+    L = len(level_nnz)
+    nb = len(bnd_ptrs)
+    gp = np.zeros(L + 1, np.int32)
+    hid = np.zeros(max(L, 1), np.int32)
+    nh = C.c_int()
+    bp = np.ascontiguousarray(np.concatenate([_i32(b) for b in bnd_ptrs]) if nb else np.zeros(1, np.int32), np.int32)
+    bgp = np.zeros(max(nb * (L + 1), 1), np.int32)
+    ng = lib().orc_mpk_partition(p, nrow, nnz, float(cache_bytes), float(safety), int(cutoff), L, _i32(level_ptr),
+                                 _i32(level_nnz), nb, bp, gp, hid, C.byref(nh), bgp)
+    if ng < 0:
+        return None
+    bgps = [bgp[k * (L + 1): k * (L + 1) + ng + 1].copy() for k in range(nb)]
+    return gp[: ng + 1].copy(), hid[: nh.value].copy(), bgps
+
+
+def mpk_recursive(csr, p: int, cache_bytes: float, safety: float, stage_cutoffs):
+    """RACE's MPK partition with its recursion into hopeless groups
+    (mtxPowerRecursive::findPartition / recursivePartition,
+    matrixPowerRecursive.cpp:156-436), composed from the oracle's traversals
+    and orc_mpk_partition. stage_cutoffs[s] is the cut-off of stage s
+    (INT_MAX beyond the list). Depth first, each hopeless group h of a leaf
+    becomes a leaf whose boundaries are the leaf's groups h-w..h+w but h and,
+    of each of the leaf's boundary regions, its groups h-w..h+w with h-1..h+1
+    as one range (w = ceil(p/2)-1, empty ranges left out); the leaf is
+    traversed with them, partitioned (boundary non-zeros counted per level)
+    and recursed into before its next sibling. Returns (tree, total_perm,
+    total_inv): tree is a list of dicts lo, hi, stage, parent, lp, hid in the
+    reference's order; None if a partition fails."""
+    n = csr.n
+    nnz = int(csr.row_ptr[-1])
+    cut = list(stage_cutoffs)
+    tp, ti, lr, ln, L = traverse(csr, 3, 0, n)
+    lp0 = np.concatenate([[0], np.cumsum(lr)]).astype(np.int32)
+    part = mpk_partition(p, n, nnz, cache_bytes, safety, cut[0] if cut else INT_MAX, lp0, ln)
+    if part is None:
+        return None
+    tree = [dict(lo=0, hi=n, stage=0, parent=-1, lp=[int(v) for v in part[0]], hid=[int(v) for v in part[1]])]
+    w = (p + 1) // 2 - 1
+    state = {"tp": tp, "ti": ti}
+
+    def recurse(parent, bgps):
+        leaf = tree[parent]
+        gp, stage = leaf["lp"], leaf["stage"] + 1
+        cutoff = cut[stage] if stage < len(cut) else INT_MAX
+        for h in list(leaf["hid"]):
+            regions = []
+            if w > 0:
+                for bp in bgps:
+                    r = -w
+                    while r <= w:
+                        if r == -1:
+                            a, b = bp[h - 1], bp[h + 2]
+                            r = 1
+                        else:
+                            a, b = bp[h + r], bp[h + r + 1]
+                        if b > a:
+                            regions.append((int(a), int(b)))
+                        r += 1
+            regions += [(gp[h + r], gp[h + r + 1]) for r in range(-w, w + 1) if r != 0 and gp[h + r + 1] > gp[h + r]]
+            lo, hi = gp[h], gp[h + 1]
+            state["tp"], state["ti"], clr, cln, CL, reg = traverse_boundary(csr, lo, hi, regions, state["tp"],
+                                                                            state["ti"], region_levels=True)
+            lvl_ptr = np.concatenate([[lo], lo + np.cumsum(clr)]).astype(np.int32)
+            lvl_nnz = cln.astype(np.int64) + sum((rn.astype(np.int64) for _, rn in reg), np.zeros(CL, np.int64))
+            bnd = [np.concatenate([[a], a + np.cumsum(rr)]).astype(np.int32) for (a, _), (rr, _) in zip(regions, reg)]
+            part = mpk_partition(p, n, nnz, cache_bytes, safety, cutoff, lvl_ptr, lvl_nnz.astype(np.int32), bnd)
+            if part is None:
+                return False
+            tree.append(dict(lo=int(lo), hi=int(hi), stage=stage, parent=parent, lp=[int(v) for v in part[0]],
+                             hid=[int(v) for v in part[1]]))
+            if part[1].size and not recurse(len(tree) - 1, part[2]):
+                return False
+        return True
+
+    if not recurse(0, []):
+        return None
+    return tree, state["tp"], state["ti"]
+
+
+def flat_power_tree(tree):
+    """A tree of mpk_recursive flattened like the golden fixtures: count,
+    then per leaf lo, hi, stage, parent, groups, lp, hopeless count, hid."""
+    flat = [len(tree)]
+    for leaf in tree:
+        flat += [leaf["lo"], leaf["hi"], leaf["stage"], leaf["parent"], len(leaf["lp"]) - 1] + list(leaf["lp"])
+        flat += [len(leaf["hid"])] + list(leaf["hid"])
+    return np.array(flat, np.int32)
 
 
 def run_kernel(kernel: int, start: int, end: int, csr, x, b):

@@ -17,8 +17,8 @@
  *   - A sequential walk of a RACE zone tree in the executor's order
  *     (src/functionManager.cpp:201-265, 1453-1501).
  *   - The matrix-power partition of a single stage (levels grouped to fit a
- *     cache budget, unlock/danger rows, per-level unlock counters;
- *     src/matrixPower.cpp:88-140, 505-605, 685-940, 958-1044) and the level
+ *     cache budget, hopeless regions, unlock/danger rows, per-level unlock
+ *     counters; src/matrixPower.cpp:88-140, 147-605, 685-940, 958-1044) and the level
  *     wavefront executor that runs it on OpenMP threads
  *     (src/functionManager.cpp:560-823). This is the CPU baseline for the
  *     matrix-power kernel.
@@ -497,6 +497,103 @@ int orc_mpk_groups(int p, int nrow, long long nnz, double cacheSize, double safe
     dangerRow[ng] = levelPtr[totalLevel - 1];
     ng += 1;
     return ng;
+}
+
+/* Level groups of one stage of the MPK partition with hopeless regions
+ * (mtxPower::findPartition for one shared-cache domain, matrixPower.cpp:
+ * 505-605: identifyHopelessRegions :147-503 and consolidatePartition
+ * :685-940), stated from what they compute:
+ *   - a level is violated when its budget b(l) = safety*(p+1)*levelNnz[l]
+ *     exceeds the cache by more than `cutoff` (ceil(b/cacheElem) > cutoff);
+ *   - every run of two or more consecutive violated levels is a hopeless
+ *     region; regions with fewer than p-1 levels between them merge;
+ *   - the first region starts no earlier than level p-1 and the last ends
+ *     no later than level L-p (a region left empty is dropped);
+ *   - grouping walks the levels once, opening a group at a level (not the
+ *     first) when the running budget reaches the cache or the level is
+ *     forced: the p-1 levels before a region and its first level, the p-1
+ *     levels after it and the one after those; the levels inside a region
+ *     after its first never open a group, so a region is one group, whose
+ *     index is reported (MPLeaf::hid). Opening a group restarts the
+ *     running budget at the level's own.
+ * levelNnz includes the non-zeros of boundary rows of each level
+ * (getElemUpperLimit, :88-99). levelPtr holds L+1 row offsets; bndPtr holds
+ * nb regions' L+1 offsets each. Writes groupPtr (ng+1), hid (*numHid) and
+ * each region's offsets at the group starts into bndGroupPtr (nb*(ng+1),
+ * region-major with stride L+1). Returns ng, or -1 when L < 1 or a region
+ * lacks p-1 levels on either side. */
+int orc_mpk_partition(int p, int nrow, long long nnz, double cacheSize, double safety, int cutoff, int L,
+                      const int *levelPtr, const int *levelNnz, int nb, const int *bndPtr, int *groupPtr, int *hid,
+                      int *numHid, int *bndGroupPtr) {
+    if (L < 1) return -1;
+    double cacheElem = cacheSize / orc_byte_per_nnz(p, nrow, nnz);
+    int *viol = (int *)calloc((size_t)L, sizeof(int));
+    int *rs = (int *)malloc(sizeof(int) * (size_t)L), *re = (int *)malloc(sizeof(int) * (size_t)L);
+    int nr = 0;
+    for (int l = 0; l < L; ++l) {
+        double b = safety * (p + 1) * levelNnz[l];
+        viol[l] = b > cacheElem && (int)ceil(b / cacheElem) > cutoff;
+    }
+    for (int l = 0; l + 1 < L; ++l) /* runs of length >= 2 */
+        if (viol[l] && viol[l + 1] && (l == 0 || !viol[l - 1])) {
+            int e = l + 1;
+            while (e + 1 < L && viol[e + 1]) ++e;
+            if (nr > 0 && l - re[nr - 1] - 1 < p - 1) {
+                re[nr - 1] = e; /* merge with the previous region */
+            } else {
+                rs[nr] = l;
+                re[nr] = e;
+                ++nr;
+            }
+        }
+    int first = 0, last = nr - 1;
+    if (nr > 0 && rs[0] < p) { /* keep p-1 levels before the first region */
+        if (re[0] < p - 1) first = 1;
+        else rs[0] = p - 1;
+    }
+    if (nr > 0 && re[nr - 1] > L - 1 - p) { /* and after the last */
+        if (rs[nr - 1] > L - p) last = nr - 2;
+        else re[nr - 1] = L - p;
+    }
+    /* classify the levels: 1 forced, 2 inside a region after its first level, 3 first level of a region */
+    int *kind = (int *)calloc((size_t)L + 1, sizeof(int));
+    int ok = 1;
+    for (int r = first; r <= last; ++r) {
+        int a = rs[r], z = re[r], b = p - 1;
+        if (a - b < 0 || z + b > L - 1) ok = 0;
+        for (int l = a - b; l <= z + b + 1 && ok; ++l) {
+            if (l < 0 || l >= L) continue;
+            if (l == a) kind[l] = 3;
+            else if (l > a && l <= z) kind[l] = 2;
+            else if (kind[l] == 0) kind[l] = 1;
+        }
+    }
+    int ng = 0, nh = 0;
+    if (ok) {
+        groupPtr[0] = levelPtr[0];
+        for (int k = 0; k < nb; ++k) bndGroupPtr[(size_t)k * (L + 1)] = bndPtr[(size_t)k * (L + 1)];
+        double sum = 0;
+        for (int l = 0; l < L; ++l) {
+            double b = safety * (p + 1) * levelNnz[l];
+            sum += b;
+            if (kind[l] == 3) hid[nh++] = ng + 1;
+            if (l > 0 && kind[l] != 2 && (sum >= cacheElem || kind[l] != 0)) {
+                sum = b;
+                ++ng;
+                groupPtr[ng] = levelPtr[l];
+                for (int k = 0; k < nb; ++k) bndGroupPtr[(size_t)k * (L + 1) + ng] = bndPtr[(size_t)k * (L + 1) + l];
+            }
+        }
+        ++ng;
+        groupPtr[ng] = levelPtr[L];
+        for (int k = 0; k < nb; ++k) bndGroupPtr[(size_t)k * (L + 1) + ng] = bndPtr[(size_t)k * (L + 1) + L];
+    }
+    *numHid = nh;
+    free(viol);
+    free(rs);
+    free(re);
+    free(kind);
+    return ok ? ng : -1;
 }
 
 /* Per-group unlock counters for `nthreads` threads (findUnlockCtr,

@@ -215,6 +215,52 @@ def test_reference_mpk_on_recursive_partitions_equals_spmv_chain(golden, mats):
     assert checked == 2
 
 
+def test_oracle_stage_partition_matches_reference(golden, mats):
+    """The oracle's own stage-0 MPK partition with hopeless regions
+    (orc_mpk_partition, restated from what identifyHopelessRegions and
+    consolidatePartition compute) gives the reference's level groups and
+    hopeless groups: partitions without hopeless regions, with them, without
+    recursion (cut-off disabled) and with other safety factors."""
+    from cases import HOPELESS_CASES, POWER_SAFETY_CASES, key_hopeless, key_power_safety
+    cases = [((m, p, c, 2.0), key_power(m, p, c), 50, golden[key_power(m, p, c) + "__hid"][:-1])
+             for m, p, c in POWER_CASES]  # -1 ends the stored list
+    cases += [((m, p, c, 2.0), key_hopeless(m, p, c), 50, golden[key_hopeless(m, p, c) + "__hid"])
+              for m, p, c in HOPELESS_CASES]
+    cases += [((m, p, c, 2.0), key_power_flat(m, p, c), orc.INT_MAX, np.zeros(0, np.int32))
+              for m, p, c in POWER_FLAT_CASES]
+    cases += [((m, p, c, sf), key_power_safety(m, p, c, sf), 50, golden[key_power_safety(m, p, c, sf) + "__hid"])
+              for m, p, c, sf in POWER_SAFETY_CASES]
+    with_hopeless = 0
+    for (m, p, c, sf), k, cutoff, want_hid in cases:
+        A = mats[m]
+        _, _, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+        lp = np.concatenate([[0], np.cumsum(lr)]).astype(np.int32)
+        gp, hid, _ = orc.mpk_partition(p, A.n, A.nnz, c, sf, cutoff, lp, ln)
+        np.testing.assert_array_equal(gp, golden[k + "__lp"], err_msg=k)
+        np.testing.assert_array_equal(hid, want_hid, err_msg=k)
+        with_hopeless += hid.size > 0
+    assert with_hopeless >= 6
+
+
+def test_oracle_mpk_recursion_matches_reference(golden, mats):
+    """The oracle's MPK recursion (mpk_recursive: its traversals with
+    boundaries and orc_mpk_partition, depth first) gives the reference's
+    whole leaf tree and permutation, for the default single stage and for
+    recursion up to three stages deep."""
+    from cases import DEEP_CASES, HOPELESS_CASES, deep_stage_cutoffs, key_deep, key_hopeless
+    for m, p, c, stages, cuts in DEEP_CASES:
+        k = key_deep(m, p, c, stages, cuts)
+        tree, tp, _ = orc.mpk_recursive(mats[m], p, c, 2.0, deep_stage_cutoffs(stages, cuts))
+        np.testing.assert_array_equal(orc.flat_power_tree(tree), golden[k + "__tree"], err_msg=k)
+        np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
+    for m, p, c in HOPELESS_CASES:
+        k = key_hopeless(m, p, c)
+        tree, tp, _ = orc.mpk_recursive(mats[m], p, c, 2.0, [50])
+        assert len(tree) == int(golden[k + "__leaves"])
+        np.testing.assert_array_equal(tree[0]["lp"], golden[k + "__lp"])
+        np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
+
+
 def test_reference_mpk_on_deep_partitions_equals_spmv_chain(golden, mats):
     """With recursion deeper than one stage too, the reference's MPK executor
     (recursivePowerCallSerial over the whole leaf tree) gives p sequential
