@@ -171,6 +171,13 @@ int race_get_sweep_info(race_engine *e, int func_id, int rev, int *numWaves, int
 /* Interface::setPower / getPower (interface.cpp:574-590) */
 int race_set_power(race_engine *e, int func_id, int power);
 int race_get_power(race_engine *e, int func_id, int *out);
+/* Interface::setSubPower / getSubPower (interface.cpp:579-592) for a
+ * built-in function. The built-in kernels have no sub-steps, so only 1 is
+ * accepted (RACE_ERR_INCOMPATIBILITY otherwise) and getSubPower gives 1.
+ * The caller's own power functions with sub-powers are device functors
+ * (DevicePowerFunction::setSubPower in race_gb300_device.cuh). */
+int race_set_sub_power(race_engine *e, int func_id, int subPower);
+int race_get_sub_power(race_engine *e, int func_id, int *out);
 
 /* Plain FP64 CRS SpMV b = A x (no schedule; the traditional baseline the
  * reference compares MPK against, kernels.cpp:90-105). */

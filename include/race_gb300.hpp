@@ -143,6 +143,14 @@ class Interface {
         race_get_power(e_, funcId, &v);
         return v;
     }
+    // built-in functions have sub-power 1 (race_set_sub_power); device
+    // power functors carry their own (DevicePowerFunction::setSubPower)
+    void setSubPower(int funcId, int subPow) { race_set_sub_power(e_, funcId, subPow); }
+    int getSubPower(int funcId) {
+        int v = 0;
+        race_get_sub_power(e_, funcId, &v);
+        return v;
+    }
     int getHighestPower() {
         int v = 0;
         race_get_highest_power(e_, &v);

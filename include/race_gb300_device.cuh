@@ -154,24 +154,8 @@ template <class F>
 class DevicePowerFunction {
   public:
     DevicePowerFunction(race_engine *e, const F &f, int power, int rowsPerCall = 32, int subPower = 1)
-        : f_(f), power_(power), subPower_(subPower) {
-        if (power < 1 || subPower < 1 || rowsPerCall < 1) {
-            rc_ = RACE_ERR_INVALID_ARG;
-            return;
-        }
-        int len = 0;
-        rc_ = race_get_power_groups(e, nullptr, 0, &len);
-        if (rc_ != RACE_SUCCESS) return;
-        std::vector<int> gp(len);
-        rc_ = race_get_power_groups(e, gp.data(), len, &len);
-        if (rc_ != RACE_SUCCESS) return;
-        std::vector<int4> calls;
-        detail::powerCalls(gp, power * subPower, rowsPerCall, calls, stepPtr_);
-        if (!calls.empty()) {
-            if (cudaMalloc(&calls_, sizeof(int4) * calls.size()) != cudaSuccess ||
-                cudaMemcpy(calls_, calls.data(), sizeof(int4) * calls.size(), cudaMemcpyHostToDevice) != cudaSuccess)
-                rc_ = RACE_ERR_CUDA;
-        }
+        : e_(e), f_(f), power_(power), subPower_(subPower), rowsPerCall_(rowsPerCall) {
+        rc_ = build();
     }
     ~DevicePowerFunction() {
         if (calls_) cudaFree(calls_);
@@ -181,6 +165,17 @@ class DevicePowerFunction {
     int status() const { return rc_; }
     int getPower() const { return power_; }
     int getSubPower() const { return subPower_; }
+    // Interface::setPower / setSubPower (interface.cpp:574-582): the next
+    // execute runs power * subPower steps; the call table is rebuilt.
+    // Returns the new status.
+    int setPower(int power) {
+        power_ = power;
+        return rc_ = build();
+    }
+    int setSubPower(int subPower) {
+        subPower_ = subPower;
+        return rc_ = build();
+    }
     int execute(cudaStream_t stream = 0) const {
         if (rc_ != RACE_SUCCESS) return rc_;
         for (size_t st = 0; st + 1 < stepPtr_.size(); ++st) {
@@ -193,12 +188,86 @@ class DevicePowerFunction {
     }
 
   private:
+    // The call table of power_ * subPower_ steps over the engine's groups.
+    int build() {
+        if (calls_) cudaFree(calls_);
+        calls_ = nullptr;
+        stepPtr_.clear();
+        if (power_ < 1 || subPower_ < 1 || rowsPerCall_ < 1) return RACE_ERR_INVALID_ARG;
+        int len = 0;
+        int rc = race_get_power_groups(e_, nullptr, 0, &len);
+        if (rc != RACE_SUCCESS) return rc;
+        std::vector<int> gp(len);
+        rc = race_get_power_groups(e_, gp.data(), len, &len);
+        if (rc != RACE_SUCCESS) return rc;
+        std::vector<int4> calls;
+        detail::powerCalls(gp, power_ * subPower_, rowsPerCall_, calls, stepPtr_);
+        if (!calls.empty() && (cudaMalloc(&calls_, sizeof(int4) * calls.size()) != cudaSuccess ||
+                               cudaMemcpy(calls_, calls.data(), sizeof(int4) * calls.size(),
+                                          cudaMemcpyHostToDevice) != cudaSuccess))
+            return RACE_ERR_CUDA;
+        return RACE_SUCCESS;
+    }
+
+    race_engine *e_;
     F f_;
-    int power_, subPower_;
+    int power_, subPower_, rowsPerCall_;
     std::vector<int> stepPtr_;
     int4 *calls_ = nullptr;
     int rc_ = RACE_SUCCESS;
 };
+
+namespace detail {
+
+// MAT_NUM_VEC_ACCESSES (interface.cpp:1060-1080): each row counts its
+// visits; a visit that leaves the count other than pow is an error.
+struct CoverageCount {
+    double *x;
+    int *errors;
+    __device__ void operator()(int start, int end, int pow) const {
+        for (int row = start; row < end; ++row) {
+            x[row] += 1;
+            if (x[row] != (double)pow) atomicAdd(errors, 1);
+        }
+    }
+};
+
+}  // namespace detail
+
+// Interface::checkPowerCoverage (interface.cpp:1082-1095): a counting
+// function of the engine's highest power runs over its level groups
+// (after race_power_prepare); *errors gets the number of row visits out of
+// turn (missing or repeated computations), 0 for a sound schedule. The
+// reference prints each such visit instead. Synchronises the device.
+inline int checkPowerCoverage(race_engine *e, int *errors) {
+    if (!errors) return RACE_ERR_INVALID_ARG;
+    *errors = -1;
+    int hp = 0, len = 0;
+    int rc = race_get_highest_power(e, &hp);
+    if (rc == RACE_SUCCESS) rc = race_get_power_groups(e, nullptr, 0, &len);
+    if (rc != RACE_SUCCESS) return rc;
+    std::vector<int> gp(len);
+    rc = race_get_power_groups(e, gp.data(), len, &len);
+    if (rc != RACE_SUCCESS) return rc;
+    const int n = gp.empty() ? 0 : gp.back();
+    double *x = nullptr;
+    int *err = nullptr;
+    if (cudaMalloc(&x, sizeof(double) * (size_t)std::max(n, 1)) != cudaSuccess ||
+        cudaMalloc(&err, sizeof(int)) != cudaSuccess || cudaMemset(x, 0, sizeof(double) * (size_t)n) != cudaSuccess ||
+        cudaMemset(err, 0, sizeof(int)) != cudaSuccess) {
+        rc = RACE_ERR_CUDA;
+    } else {
+        DevicePowerFunction<detail::CoverageCount> f(e, detail::CoverageCount{x, err}, hp);
+        rc = f.status();
+        if (rc == RACE_SUCCESS) rc = f.execute(0);
+        if (rc == RACE_SUCCESS && (cudaDeviceSynchronize() != cudaSuccess ||
+                                   cudaMemcpy(errors, err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess))
+            rc = RACE_ERR_CUDA;
+    }
+    if (x) cudaFree(x);
+    if (err) cudaFree(err);
+    return rc;
+}
 
 }  // namespace gb300
 }  // namespace RACE

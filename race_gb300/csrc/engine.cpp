@@ -450,6 +450,17 @@ int race_get_power(race_engine *e, int func_id, int *out) {
     return RACE_SUCCESS;
 }
 
+int race_set_sub_power(race_engine *e, int func_id, int subPower) {
+    if (!e || func_id < 0 || func_id >= (int)e->eng->funcs.size() || subPower < 1) return RACE_ERR_INVALID_ARG;
+    return subPower == 1 ? RACE_SUCCESS : RACE_ERR_INCOMPATIBILITY;
+}
+
+int race_get_sub_power(race_engine *e, int func_id, int *out) {
+    if (!e || !out || func_id < 0 || func_id >= (int)e->eng->funcs.size()) return RACE_ERR_INVALID_ARG;
+    *out = 1;
+    return RACE_SUCCESS;
+}
+
 int race_symmgs_ir(race_engine *e, int inner_func_id, int n, const int *rowPtr, const int *col, const double *val,
                    const double *b, double *x, double tol, int maxIter, int sweeps, int *iters, double *relres) {
     if (!e || !rowPtr || !col || !val || !b || !x || !iters || !relres || sweeps < 1 || maxIter < 0)

@@ -332,6 +332,16 @@ class Interface:
         self._check(lib().race_get_power(self._h, int(funcId), C.byref(v)))
         return v.value
 
+    def setSubPower(self, funcId: int, subPow: int):
+        """Interface::setSubPower: built-in kernels have no sub-steps, so
+        only 1 is accepted (RACE_ERR_INCOMPATIBILITY otherwise)."""
+        self._check(lib().race_set_sub_power(self._h, int(funcId), int(subPow)))
+
+    def getSubPower(self, funcId: int) -> int:
+        v = C.c_int()
+        self._check(lib().race_get_sub_power(self._h, int(funcId), C.byref(v)))
+        return v.value
+
     def tuneFunction(self, funcId: int, rev: bool = False, highestPower: Optional[int] = None) -> int:
         """Interface::tuneFunction (interface.cpp:605-647): time powers
         1..highestPower for >= 0.2 s each, keep the fastest time per power."""

@@ -62,4 +62,6 @@ def fnlib(tmp_path_factory):
     L.fn_gs.argtypes = [vp, vp, vp, vp, vp, vp, C.c_int]
     L.fn_mpk.argtypes = [vp, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]
     L.fn_count_subpower.argtypes = [vp, vp, C.c_int, C.c_int, vp]
+    L.fn_count_after_set.argtypes = [vp, vp, C.c_int, C.c_int, vp]
+    L.fn_check_coverage.argtypes = [vp, C.POINTER(C.c_int)]
     return L

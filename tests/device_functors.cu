@@ -81,3 +81,15 @@ extern "C" int fn_count_subpower(race_engine *e, double *x, int power, int subPo
     if (f.status() != RACE_SUCCESS) return f.status();
     return finish(f.execute(0));
 }
+
+// The same count after setPower / setSubPower on a function registered
+// with power 1 and sub-power 1 (Interface::setPower / setSubPower).
+extern "C" int fn_count_after_set(race_engine *e, double *x, int power, int subPower, int *errors) {
+    RACE::gb300::DevicePowerFunction<CountFn> f(e, CountFn{x, subPower, errors}, 1, 32, 1);
+    if (f.status() != RACE_SUCCESS) return f.status();
+    if (f.setPower(power) != RACE_SUCCESS || f.getPower() != power) return RACE_ERR_INVALID_ARG;
+    if (f.setSubPower(subPower) != RACE_SUCCESS || f.getSubPower() != subPower) return RACE_ERR_INVALID_ARG;
+    return finish(f.execute(0));
+}
+
+extern "C" int fn_check_coverage(race_engine *e, int *errors) { return RACE::gb300::checkPowerCoverage(e, errors); }

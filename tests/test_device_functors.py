@@ -5,6 +5,7 @@ sequential walk of the engine's phases bit for bit, and the MPK body as a
 power functor must equal p sequential SpMVs bit for bit. The functors live
 in tests/device_functors.cu, compiled with nvcc for sm_103a (the fnlib
 fixture of conftest.py)."""
+import ctypes as C
 import pathlib
 import subprocess
 
@@ -41,6 +42,9 @@ def test_device_functions_link_and_reject_a_null_engine(fnlib):
     assert fnlib.fn_mpk(None, None, None, None, None, 10, 2, 32) == bad
     assert fnlib.fn_mpk(None, None, None, None, None, 10, 0, 32) == bad  # power below 1
     assert fnlib.fn_count_subpower(None, None, 2, 2, None) == bad
+    assert fnlib.fn_count_after_set(None, None, 2, 2, None) == bad
+    errors = C.c_int(7)
+    assert fnlib.fn_check_coverage(None, C.byref(errors)) == bad and errors.value == -1
 
 
 @pytest.mark.gpu

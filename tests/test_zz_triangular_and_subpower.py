@@ -52,3 +52,51 @@ def test_subpower_functor_visits_every_row_in_order(mats, fnlib, m, p, sub, c):
     assert fnlib.fn_count_subpower(rc._h, x.data_ptr(), p, sub, err.data_ptr()) == 0
     assert int(err.item()) == 0
     assert bool((x == p * sub).all())
+
+
+@pytest.mark.gpu
+def test_set_power_and_subpower_rebuild_the_schedule(mats, fnlib):
+    """Interface::setPower / setSubPower on a device power function: after
+    both, every row is called once per (pow, subPow), in order."""
+    A = mats["st27_24"]
+    p, sub = 4, 2
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, 2e6, highestSubPower=sub) == 0
+    x = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert fnlib.fn_count_after_set(rc._h, x.data_ptr(), p, sub, err.data_ptr()) == 0
+    assert int(err.item()) == 0
+    assert bool((x == p * sub).all())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,p,c", [("st27_24", 8, 2e6), ("plaw_3k", 4, 2e3), ("band_5k", 8, 3000)])
+def test_check_power_coverage(mats, fnlib, m, p, c):
+    """Interface::checkPowerCoverage: the reference's counting kernel over
+    the engine's level groups (also with hopeless regions) finds every row
+    computed once per power, in order."""
+    import ctypes as C
+    A = mats[m]
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, c) == 0
+    errors = C.c_int(-2)
+    assert fnlib.fn_check_coverage(rc._h, C.byref(errors)) == 0
+    assert errors.value == 0
+
+
+@pytest.mark.gpu
+def test_builtin_functions_have_subpower_one(mats):
+    """Interface::setSubPower / getSubPower on a built-in function: sub-power
+    1 only (the built-in kernels have no sub-steps)."""
+    A = mats["lap7_16"]
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(2, 1e6) == 0
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    x = torch.zeros(3 * A.n, dtype=torch.float64, device="cuda")
+    fid = rc.registerFunction(ri.MPK, ri.Operands(ri.DeviceCsr.from_csr(P), x), power=2)
+    assert fid >= 0
+    assert rc.getSubPower(fid) == 1
+    rc.setSubPower(fid, 1)
+    with pytest.raises(RuntimeError):
+        rc.setSubPower(fid, 2)
+    assert rc.executeFunction(fid) == 0
