@@ -52,6 +52,11 @@ struct MpkPlan {
     DevBuf<int> done;           // power * numChunks completion flags
     DevBuf<int> ticket;         // 1: next work item
     DevBuf<int> status;         // 1: device status word
+    // Triangular partitions (mtxType L/U): a row may read any earlier group,
+    // so the items run as one launch per wavefront step, without waits;
+    // items stepPtr[s] .. stepPtr[s+1]) form step s.
+    bool stepped = false;
+    std::vector<int> stepPtr;
 };
 
 // Device tables of one persistent block-MPK launch over one or more members

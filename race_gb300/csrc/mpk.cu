@@ -238,6 +238,18 @@ __global__ void __launch_bounds__(kWarpThreads) kSpmvSell(SellView m, int numChu
         chunkRow<VT, HUBS>(m, c, k, n, x, xf);
 }
 
+// One wavefront step of a triangular partition: one warp per (chunk,
+// power) item of the step. Every item's inputs were written by earlier
+// launches, so nothing waits.
+template <typename VT, bool HUBS>
+__global__ void __launch_bounds__(kWarpThreads) kMpkStep(SellView m, const int *__restrict__ itemChunk,
+                                                         const unsigned char *__restrict__ itemPow, int count, int n,
+                                                         double *x, float *xf) {
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < count; i += nw)
+        chunkRow<VT, HUBS>(m, itemChunk[i], itemPow[i], n, x, xf);
+}
+
 // x0 -> FP32 copy (rounding to nearest) for the reduced-precision path.
 __global__ void kToFloat(const double *__restrict__ x, float *__restrict__ xf, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -298,10 +310,12 @@ __global__ void kToSell(const int *__restrict__ rowPtr, const int *__restrict__ 
 // For every chunk, the range of chunks its columns fall in, separately for
 // the previous, the own and the next level group. Columns outside those
 // three groups mark the plan invalid (*bad = 1): BFS levels only couple
-// neighbouring levels, so a RACE-permuted matrix never has them.
+// neighbouring levels, so a RACE-permuted matrix never has them. With
+// earlierOk (triangular partitions, run step by step) columns in any
+// earlier group are allowed and left out of the ranges.
 __global__ void kChunkRanges(const int *__restrict__ rowPtr, const int *__restrict__ col,
                              const int *__restrict__ chunkRowP, const int *__restrict__ chunkGroup, int numChunks,
-                             int *__restrict__ range, int *__restrict__ bad) {
+                             int *__restrict__ range, int *__restrict__ bad, int earlierOk) {
     const int t = blockIdx.x;
     if (t >= numChunks) return;
     __shared__ int lo[3], hi[3];
@@ -319,6 +333,7 @@ __global__ void kChunkRanges(const int *__restrict__ rowPtr, const int *__restri
             if (chunkRowP[mid] <= c) a = mid; else b = mid - 1;
         }
         const int d = chunkGroup[a] - g + 1;
+        if (d < 0 && earlierOk) continue;
         if (d < 0 || d > 2) {
             atomicExch(bad, 1);
             continue;
@@ -452,7 +467,10 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     // sits in an earlier step, so the items in flight are independent; each
     // group stays in use for 2p-1 steps instead of p. Both orders compute the
     // same rows at the same powers; results are bit-identical.
-    const int stride = e.mpkStride == 1 ? 1 : 2;
+    // A triangular partition (mtxType L/U) runs step by step: stride 2 puts
+    // every earlier group's previous power in an earlier step.
+    plan->stepped = e.powerLevelsType == "L" || e.powerLevelsType == "U";
+    const int stride = e.mpkStride == 1 && !plan->stepped ? 1 : 2;
     std::vector<int> groupFirst(G + 1, C);
     for (int t = C - 1; t >= 0; --t) groupFirst[chunkGroup[t]] = t;
     for (int g = G - 1; g >= 0; --g) groupFirst[g] = std::min(groupFirst[g], groupFirst[g + 1]);
@@ -463,10 +481,11 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     // s+1..2s, ... in one launch (each segment's items follow all items of
     // the powers before it, so the order stays a valid wavefront): fewer
     // groups in flight at the cost of reading the matrix once per segment.
-    const int split = e.mpkSplit > 0 && e.mpkSplit < power ? e.mpkSplit : power;
+    const int split = e.mpkSplit > 0 && e.mpkSplit < power && !plan->stepped ? e.mpkSplit : power;
+    plan->stepPtr.assign(1, 0);
     for (int k0 = 0; k0 < power; k0 += split) {
         const int kn = std::min(power, k0 + split) - k0;
-        for (int st = 0; st < G + stride * (kn - 1); ++st)
+        for (int st = 0; st < G + stride * (kn - 1); ++st) {
             for (int k = 0; k < kn; ++k) {
                 int g = st - stride * k;
                 if (g < 0 || g >= G) continue;
@@ -475,6 +494,8 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
                     itemPow.push_back((unsigned char)(k0 + k));
                 }
             }
+            plan->stepPtr.push_back((int)itemChunk.size());
+        }
     }
     plan->numItems = (int)itemChunk.size();
     plan->itemChunk.upload(itemChunk.data(), std::max<size_t>(itemChunk.size(), 1), s);
@@ -488,15 +509,16 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     RACE_CUDA(cudaMemsetAsync(dBad.p, 0, sizeof(int), s));
     if (C > 0)
         kChunkRanges<<<C, 128, 0, s>>>(ops.rowPtr, ops.col, plan->chunkRow.p, dChunkGroup.p, C, plan->depRange.p,
-                                       dBad.p);
+                                       dBad.p, plan->stepped ? 1 : 0);
     RACE_CUDA(cudaGetLastError());
     int bad = 0;
     RACE_CUDA(cudaMemcpyAsync(&bad, dBad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     RACE_CUDA(cudaStreamSynchronize(s));
     // Every dependency must come earlier in the wavefront order: the columns
-    // of group g lie in groups g-1..g+1 (BFS levels couple neighbours only).
-    // A matrix not permuted with this engine's MPK permutation breaks that
-    // and is rejected here instead of stalling the kernel.
+    // of group g lie in groups g-1..g+1 (BFS levels couple neighbours only;
+    // for a triangular partition in any group up to g+1). A matrix not
+    // permuted with this engine's MPK permutation breaks that and is
+    // rejected here instead of stalling the kernel.
     if (bad)
         throw Error(RACE_ERR_INVALID_ARG,
                     "MPK operand is not in the engine's level order (permute it with getPerm/getInvPerm)");
@@ -515,7 +537,7 @@ bool chunkDependencyRanges(const int *rowPtr, const int *col, const std::vector<
     dRow.upload(chunkRow.data(), chunkRow.size(), s);
     dGroup.upload(chunkGroup.data(), chunkGroup.size(), s);
     RACE_CUDA(cudaMemsetAsync(dBad.p, 0, sizeof(int), s));
-    kChunkRanges<<<C, 128, 0, s>>>(rowPtr, col, dRow.p, dGroup.p, C, dRange.p, dBad.p);
+    kChunkRanges<<<C, 128, 0, s>>>(rowPtr, col, dRow.p, dGroup.p, C, dRange.p, dBad.p, 0);
     RACE_CUDA(cudaGetLastError());
     int bad = 0;
     RACE_CUDA(cudaMemcpyAsync(range.data(), dRange.p, sizeof(int) * range.size(), cudaMemcpyDeviceToHost, s));
@@ -542,6 +564,22 @@ void launchMpk(const MpkArgs &a, bool hubs, cudaStream_t s) {
 }
 
 template <typename VT>
+void launchMpkSteps(const MpkPlan &p, int n, double *x, cudaStream_t s) {
+    const SellView v = viewOf(p);
+    for (size_t st = 0; st + 1 < p.stepPtr.size(); ++st) {
+        const int first = p.stepPtr[st], count = p.stepPtr[st + 1] - first;
+        if (count == 0) continue;
+        const int blocks = std::min(ceilDiv(count, kWarpThreads / 32), devSms() * 16);
+        if (p.numHubs > 0)
+            kMpkStep<VT, true><<<blocks, kWarpThreads, 0, s>>>(v, p.itemChunk.p + first, p.itemPow.p + first, count,
+                                                                n, x, p.xf.p);
+        else
+            kMpkStep<VT, false><<<blocks, kWarpThreads, 0, s>>>(v, p.itemChunk.p + first, p.itemPow.p + first, count,
+                                                                 n, x, p.xf.p);
+    }
+}
+
+template <typename VT>
 void launchSpmvSell(const SellView &v, int numChunks, int n, int k, double *x, float *xf, bool hubs,
                     cudaStream_t s) {
     if (hubs) {
@@ -561,6 +599,16 @@ void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
     RACE_CUDA(cudaMemsetAsync(plan.ticket.p, 0, sizeof(int), s));
     RACE_CUDA(cudaMemsetAsync(plan.status.p, 0, sizeof(int), s));
     if (plan.valType != RACE_VAL_F64) kToFloat<<<ceilDiv(ops.n, 256), 256, 0, s>>>((const double *)ops.x, plan.xf.p, ops.n);
+    if (plan.stepped) {
+        switch (plan.valType) {
+        case RACE_VAL_F64: launchMpkSteps<double>(plan, ops.n, (double *)ops.x, s); break;
+        case RACE_VAL_F32: launchMpkSteps<float>(plan, ops.n, (double *)ops.x, s); break;
+        case RACE_VAL_BF16: launchMpkSteps<__nv_bfloat16>(plan, ops.n, (double *)ops.x, s); break;
+        default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
+        }
+        RACE_CUDA(cudaGetLastError());
+        return;
+    }
     MpkArgs a{viewOf(plan), (double *)ops.x, plan.xf.p, ops.n, plan.depRange.p, plan.itemChunk.p, plan.itemPow.p,
               plan.numItems, plan.numChunks, plan.done.p, plan.ticket.p, plan.status.p};
     switch (plan.valType) {

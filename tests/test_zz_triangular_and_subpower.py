@@ -1,7 +1,7 @@
-"""Matrix-power cases run through device functors on the GPU (after the
-other GPU tests): triangular partitions (mtxType L / U) and their MPK, and
-sub-powers. Their host parts are checked on the CPU (test_oracle.py,
-test_device_functors.py)."""
+"""Matrix-power cases on the GPU (after the other GPU tests): triangular
+partitions (mtxType L / U) and their MPK through device functors and the
+built-in kernel, and sub-powers. Their host parts are checked on the CPU
+(test_oracle.py, test_device_functors.py)."""
 import numpy as np
 import pytest
 
@@ -12,6 +12,8 @@ from race_gb300 import matgen
 torch = pytest.importorskip("torch")
 
 from race_gb300 import interface as ri  # noqa: E402
+
+HUB_ROW_LEN = 256  # rows longer than this are summed by a warp (mpk.cu kHubRowLen)
 
 
 @pytest.mark.gpu
@@ -36,6 +38,30 @@ def test_triangular_partition_and_functor_mpk(golden, mats, fnlib, m, tri, p, c)
     assert fnlib.fn_mpk(rc._h, dm.row_ptr.data_ptr(), dm.col.data_ptr(), dm.val.data_ptr(), x.data_ptr(), T.n,
                         p, 32) == 0
     np.testing.assert_array_equal(x.cpu().numpy().reshape(p + 1, T.n), Y)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,tri,p,c", POWER_TRI_CASES)
+def test_triangular_builtin_mpk(golden, mats, m, tri, p, c):
+    """The built-in MPK on a triangular partition (run one launch per
+    wavefront step, since a row may read any earlier group) equals p
+    sequential SpMVs bit for bit."""
+    T = triangle(mats[m], tri)
+    rc = ri.Interface(T.n, 1, ri.POWER, T.row_ptr, T.col, symm_hint=True)
+    assert rc.RACEColor(p, c, mtxType=tri) == 0
+    np.testing.assert_array_equal(rc.getPerm(), golden[key_power_tri(m, tri, p, c) + "__perm"])
+    P = T.permuted(rc.getPerm(), rc.getInvPerm())
+    x0 = matgen.uniform_vector(T.n, 0)
+    x = torch.zeros((p + 1) * T.n, dtype=torch.float64, device="cuda")
+    x[: T.n] = torch.tensor(x0, device="cuda")
+    fid = rc.registerFunction(ri.MPK, ri.Operands(ri.DeviceCsr.from_csr(P), x), power=p)
+    assert fid >= 0 and rc.executeFunction(fid) == 0
+    got, Y = x.cpu().numpy().reshape(p + 1, T.n), orc.mpk_plain(P, x0, p)
+    if np.diff(P.row_ptr).max() <= HUB_ROW_LEN:
+        np.testing.assert_array_equal(got, Y)
+    else:  # hub rows are summed by a warp, in another order
+        for kk in range(1, p + 1):
+            assert np.max(np.abs(got[kk] - Y[kk])) <= 1e-12 * np.max(np.abs(Y[kk]))
 
 
 @pytest.mark.gpu
