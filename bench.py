@@ -172,6 +172,8 @@ def cpu_partition(A, x0, threads):
         times[c] = statistics.median(ts)
         if best is None or times[c] < times[best[1]]:
             best = (groups, c)
+    if best is None:
+        raise RuntimeError("no cache budget gives a partition without hopeless regions for the CPU wavefront")
     return P, best[0], best[1], times
 
 

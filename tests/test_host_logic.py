@@ -31,6 +31,23 @@ def test_library_exports_every_declared_symbol():
     assert sorted(_lib.EXPORTS) == declared
 
 
+def test_every_handle_entry_point_rejects_a_null_handle():
+    """Every entry point taking an engine, batch or MLP handle returns
+    RACE_ERR_INVALID_ARG for NULL (no GPU needed, nothing dereferenced);
+    the destroy calls accept NULL as a no-op, like free."""
+    L = _lib.lib()
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "race_gb300.h").read_text(), flags=re.S)
+    names = sorted(set(re.findall(
+        r"int\s+(race_[a-z_0-9]+)\s*\(\s*(?:const\s+)?race_(?:engine|batch|mlp)\s*\*\s*\w+\s*[,)]", text)))
+    assert len(names) >= 40
+    for name in names:
+        f = getattr(L, name)
+        args = [0 if t in (C.c_int, C.c_longlong) else 0.0 if t in (C.c_double, C.c_float) else None
+                for t in f.argtypes]
+        want = _lib.RACE_SUCCESS if name.endswith("destroy") else _lib.RACE_ERR_INVALID_ARG
+        assert f(*args) == want, name
+
+
 def _lb(levelRow, levelNnz, nt, eff, dist, tgt, base=7, d2type=0):
     L = _lib.lib()
     lr = np.ascontiguousarray(levelRow, np.int32)
