@@ -91,6 +91,17 @@ def key_color_row(m, d, t):
     return f"colorrow__{m}__d{d}__t{t}"
 
 
+# colorings at the edges of the thread count: one thread, odd and prime
+# counts, far more threads than the matrix can use: (matrix, dist, nthreads)
+COLOR_EDGE_CASES = [("lap7_16", 2, 1), ("lap7_16", 1, 1), ("band_5k", 1, 3), ("aniso5_120x90", 2, 7),
+                    ("plaw_3k", 2, 1000), ("islands_330", 1, 2), ("arrow_64", 2, 5), ("st27_16", 2, 13),
+                    ("aniso9_100x80", 2, 4096), ("tiny_1", 2, 1)]
+
+
+def key_color_edge(m, d, t):
+    return f"coloredge__{m}__d{d}__t{t}"
+
+
 # colorings of matrices whose pattern is not symmetric (a triangle), with
 # symm_hint false, so that RACE first adds the missing transposed entries
 # (makeSymmetricGraph, graph.cpp:47-142): (matrix, triangle, dist, nthreads)

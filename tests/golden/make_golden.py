@@ -36,7 +36,7 @@ from cases import (COLOR3_CASES, COLOR_CASES, COLOR_ENV_CASES, COLOR_INIT_CASES,
                    SIMDIFY_CASES, TRAVERSE_CASES, arr_digest, digest, key_color, key_power, key_power_flat,
                    init_perm, key_color3, key_color_env, key_color_init, key_color_row, key_color_unsym,
                    key_hopeless, key_power_tri, key_simdify, key_trav, sell_layout, triangle,
-                   DEEP_CASES, DEEP_EXEC_CASES, key_deep)
+                   DEEP_CASES, DEEP_EXEC_CASES, key_deep, COLOR_EDGE_CASES, key_color_edge)
 from oracle import refpy  # noqa: E402
 from oracle.refpy import RefInterface  # noqa: E402
 from race_gb300 import matgen  # noqa: E402
@@ -160,6 +160,20 @@ def main():
         g[k + "__perm"] = p
         g[k + "__tree"] = rc.tree_flat()
         g[k + "__threads"] = np.array(rc.threads())
+        rc.close()
+        print(k, "threads", int(g[k + "__threads"]))
+
+    # colorings at the edges of the thread count
+    for m, d, t in COLOR_EDGE_CASES:
+        A = M(m)
+        rc = refpy.RefColor(A, d, t)
+        k = key_color_edge(m, d, t)
+        p, ip = rc.perm()
+        g[k + "__digest"] = np.array(digest(A))
+        g[k + "__perm"] = p
+        g[k + "__tree"] = rc.tree_flat()
+        g[k + "__threads"] = np.array(rc.threads())
+        g[k + "__eff"] = np.array(rc.efficiency())
         rc.close()
         print(k, "threads", int(g[k + "__threads"]))
 

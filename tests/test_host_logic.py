@@ -725,6 +725,24 @@ def test_level_recursion_balancing_rows(golden, mats, monkeypatch):
         np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)
 
 
+def test_level_recursion_at_thread_count_edges(golden, mats, monkeypatch):
+    """The engine's level recursion at the edges of the thread count (one
+    thread, odd and prime counts, far more threads than the matrix can
+    use) gives the reference's zone tree, threads and permutation."""
+    from cases import COLOR_EDGE_CASES, key_color_edge
+    for var in ("RACE_EFFICIENCY", "RACE_THREADS"):
+        monkeypatch.delenv(var, raising=False)
+    for m, d, t in COLOR_EDGE_CASES:
+        A = mats[m]
+        k = key_color_edge(m, d, t)
+        assert str(golden[k + "__digest"]) == digest(A)
+        gold = golden[k + "__tree"]
+        tree, avail, perm = _zone_tree_host(A, d, t, 0, 2 * gold.size + 1024)
+        np.testing.assert_array_equal(tree, gold, err_msg=k)
+        assert avail == int(golden[k + "__threads"]), k
+        np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)
+
+
 def test_level_recursion_on_unsymmetric_patterns(golden, mats, monkeypatch):
     """Matrices whose pattern is not symmetric, colored with symm_hint
     false: with RACE's symmetrisation (the missing transposed entries added,

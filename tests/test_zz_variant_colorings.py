@@ -7,8 +7,8 @@ test_host_logic.py; this file runs after the other GPU tests.)"""
 import numpy as np
 import pytest
 
-from cases import (COLOR3_CASES, COLOR_INIT_CASES, COLOR_ROW_CASES, COLOR_UNSYM_CASES, digest, key_color3,
-                   key_color_init, key_color_row, key_color_unsym, triangle)
+from cases import (COLOR3_CASES, COLOR_EDGE_CASES, COLOR_INIT_CASES, COLOR_ROW_CASES, COLOR_UNSYM_CASES, digest,
+                   key_color3, key_color_edge, key_color_init, key_color_row, key_color_unsym, triangle)
 from race_gb300 import matgen
 
 torch = pytest.importorskip("torch")
@@ -97,3 +97,20 @@ def test_coloring_balancing_rows(golden, mats, m, d, t):
     assert rc.RACEColor() == 0
     np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
     np.testing.assert_array_equal(rc.getZoneTreeFlat(), golden[k + "__tree"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,d,t", COLOR_EDGE_CASES)
+def test_coloring_at_thread_count_edges(golden, mats, m, d, t):
+    """One thread, odd and prime thread counts, and far more threads than
+    the matrix can use: the reference's permutation, zone tree, thread
+    count and efficiency."""
+    A = mats[m]
+    k = key_color_edge(m, d, t)
+    assert str(golden[k + "__digest"]) == digest(A)
+    rc = ri.Interface(A.n, t, d, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor() == 0
+    np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
+    np.testing.assert_array_equal(rc.getZoneTreeFlat(), golden[k + "__tree"])
+    assert rc.getNumThreads() == int(golden[k + "__threads"])
+    assert rc.getEfficiency() == float(golden[k + "__eff"])
