@@ -189,6 +189,19 @@ DEEP_CASES = [("band_5k", 8, 3000, 2, ()), ("band_5k", 8, 3000, -1, (50, 1)), ("
 DEEP_EXEC_CASES = {("band_5k", 8, 3000, -1, (50, 1)), ("plaw_3k", 3, 2000, 3, (50, 2, 1))}
 
 
+# MPK partitions at edge parameters (default recursion): power 1 and high
+# powers, a budget that holds the whole matrix in one group, tiny budgets
+# (hopeless regions, also with power 1), a one-row matrix, islands:
+# (matrix, power, cacheBytes). The whole leaf tree and permutation are stored.
+POWER_EDGE_CASES = [("lap7_16", 1, 1e4), ("band_5k", 16, 1e5), ("st27_16", 8, 1e9), ("lap7_32", 3, 1e3),
+                    ("islands_330", 5, 1e3), ("tiny_1", 4, 1e2), ("aniso9_100x80", 12, 2e4), ("plaw_20k", 2, 1e3),
+                    ("arrow_64", 3, 50), ("st27_24", 1, 1e3)]
+
+
+def key_power_edge(m, p, c):
+    return f"poweredge__{m}__p{p}__c{int(c)}"
+
+
 def key_deep(m, p, c, stages, cuts):
     return f"deep__{m}__p{p}__c{int(c)}__s{stages}__k{'-'.join(str(v) for v in cuts)}"
 

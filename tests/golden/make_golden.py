@@ -36,7 +36,8 @@ from cases import (COLOR3_CASES, COLOR_CASES, COLOR_ENV_CASES, COLOR_INIT_CASES,
                    SIMDIFY_CASES, TRAVERSE_CASES, arr_digest, digest, key_color, key_power, key_power_flat,
                    init_perm, key_color3, key_color_env, key_color_init, key_color_row, key_color_unsym,
                    key_hopeless, key_power_tri, key_simdify, key_trav, sell_layout, triangle,
-                   DEEP_CASES, DEEP_EXEC_CASES, key_deep, COLOR_EDGE_CASES, key_color_edge)
+                   DEEP_CASES, DEEP_EXEC_CASES, key_deep, COLOR_EDGE_CASES, key_color_edge, POWER_EDGE_CASES,
+                   key_power_edge)
 from oracle import refpy  # noqa: E402
 from oracle.refpy import RefInterface  # noqa: E402
 from race_gb300 import matgen  # noqa: E402
@@ -45,6 +46,16 @@ OUT = pathlib.Path(__file__).resolve().parent / "golden.npz"
 
 # full-size MPK configuration: 128^3 27-point stencil, p=8, 100 MB cache budget
 FULL_POWER = ("st27_128", 8, 100e6)
+
+
+def flat_power_tree(tr):
+    """An MPK leaf tree flattened: count, then per leaf lo, hi, stage,
+    parent, groups, lp, hopeless count, hid."""
+    flat = [len(tr)]
+    for leaf in tr:
+        flat += [leaf["lo"], leaf["hi"], leaf["stage"], leaf["parent"], len(leaf["lp"]) - 1] + leaf["lp"]
+        flat += [len(leaf["hid"])] + leaf["hid"]
+    return np.array(flat, np.int32)
 
 
 def main():
@@ -372,14 +383,24 @@ def main():
         finally:
             for var in env:
                 os.environ.pop(var, None)
-        flat = [len(tr)]
-        for leaf in tr:
-            flat += [leaf["lo"], leaf["hi"], leaf["stage"], leaf["parent"], len(leaf["lp"]) - 1] + leaf["lp"]
-            flat += [len(leaf["hid"])] + leaf["hid"]
         g[k + "__digest"] = np.array(digest(A))
-        g[k + "__tree"] = np.array(flat, np.int32)
+        g[k + "__tree"] = flat_power_tree(tr)
         g[k + "__perm"] = perm
         print(k, "leaves", len(tr), "deepest stage", max(leaf["stage"] for leaf in tr))
+
+    # MPK partitions at edge parameters, default recursion
+    for m, p, c in POWER_EDGE_CASES:
+        A = M(m)
+        k = key_power_edge(m, p, c)
+        rp = refpy.RefPower(A, p, c)
+        perm, ip = rp.perm()
+        tr = rp.tree()
+        assert (rp.coverage() == 1).all()
+        rp.close()
+        g[k + "__digest"] = np.array(digest(A))
+        g[k + "__tree"] = flat_power_tree(tr)
+        g[k + "__perm"] = perm
+        print(k, "leaves", len(tr), "groups", len(tr[0]["lp"]) - 1, "hopeless", tr[0]["hid"])
 
     # full-size MPK configuration: digests only
     A = matgen.stencil3d_27pt(128)

@@ -609,6 +609,24 @@ def _leaf_stages(tree):
     return out
 
 
+def test_mpk_partition_at_edge_parameters(golden, mats):
+    """Power 1 and high powers, a budget that holds the whole matrix, tiny
+    budgets (hopeless regions, also with power 1), a one-row matrix: the
+    engine's host partition and recursion give the reference's whole leaf
+    tree and permutation."""
+    from cases import POWER_EDGE_CASES, key_power_edge
+    with_hopeless = 0
+    for m, p, c in POWER_EDGE_CASES:
+        A = mats[m]
+        k = key_power_edge(m, p, c)
+        assert str(golden[k + "__digest"]) == digest(A)
+        tree, tp, _ = _recursive_partition(A, p, c, [50])
+        np.testing.assert_array_equal(tree, golden[k + "__tree"], err_msg=k)
+        np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
+        with_hopeless += int(tree[0]) > 1
+    assert with_hopeless == 3
+
+
 def test_mpk_one_stage_recursion_is_the_general_one(golden, mats):
     """At the default depth (one stage past the cut-off list: stage 1 has no
     cut-off) the general recursion gives the one-stage permutation of the

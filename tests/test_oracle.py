@@ -245,12 +245,18 @@ def test_oracle_stage_partition_matches_reference(golden, mats):
 def test_oracle_mpk_recursion_matches_reference(golden, mats):
     """The oracle's MPK recursion (mpk_recursive: its traversals with
     boundaries and orc_mpk_partition, depth first) gives the reference's
-    whole leaf tree and permutation, for the default single stage and for
-    recursion up to three stages deep."""
+    whole leaf tree and permutation, for the default single stage (also at
+    edge parameters) and for recursion up to three stages deep."""
     from cases import DEEP_CASES, HOPELESS_CASES, deep_stage_cutoffs, key_deep, key_hopeless
     for m, p, c, stages, cuts in DEEP_CASES:
         k = key_deep(m, p, c, stages, cuts)
         tree, tp, _ = orc.mpk_recursive(mats[m], p, c, 2.0, deep_stage_cutoffs(stages, cuts))
+        np.testing.assert_array_equal(orc.flat_power_tree(tree), golden[k + "__tree"], err_msg=k)
+        np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
+    from cases import POWER_EDGE_CASES, key_power_edge
+    for m, p, c in POWER_EDGE_CASES:
+        k = key_power_edge(m, p, c)
+        tree, tp, _ = orc.mpk_recursive(mats[m], p, c, 2.0, [50])
         np.testing.assert_array_equal(orc.flat_power_tree(tree), golden[k + "__tree"], err_msg=k)
         np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
     for m, p, c in HOPELESS_CASES:

@@ -8,7 +8,8 @@ among the GPU tests.)"""
 import numpy as np
 import pytest
 
-from cases import DEEP_CASES, HOPELESS_CASES, POWER_SAFETY_CASES, digest, key_deep, key_hopeless, key_power_safety
+from cases import (DEEP_CASES, HOPELESS_CASES, POWER_EDGE_CASES, POWER_SAFETY_CASES, digest, key_deep, key_hopeless,
+                   key_power_edge, key_power_safety)
 from oracle import oracle as orc
 from race_gb300 import matgen
 
@@ -71,6 +72,22 @@ def test_deep_recursion(golden, mats, m, p, c, stages, cuts):
     tree = golden[k + "__tree"]
     ng = int(tree[5])  # the root leaf: lo, hi, stage, parent, groups, lp
     np.testing.assert_array_equal(rc.getPowerGroups(), tree[6:7 + ng])
+    _check_mpk(rc, A, p, golden[k + "__perm"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("m,p,c", POWER_EDGE_CASES)
+def test_partition_at_edge_parameters(golden, mats, m, p, c):
+    """Power 1 and high powers, a budget that holds the whole matrix, tiny
+    budgets, a one-row matrix: the reference's groups and permutation, and
+    the MPK on them."""
+    A = mats[m]
+    k = key_power_edge(m, p, c)
+    assert str(golden[k + "__digest"]) == digest(A)
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, c) == 0
+    tree = golden[k + "__tree"]
+    np.testing.assert_array_equal(rc.getPowerGroups(), tree[6:7 + int(tree[5])])
     _check_mpk(rc, A, p, golden[k + "__perm"])
 
 
