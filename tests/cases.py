@@ -98,6 +98,11 @@ COLOR_EDGE_CASES = [("lap7_16", 2, 1), ("lap7_16", 1, 1), ("band_5k", 1, 3), ("a
                     ("aniso9_100x80", 2, 4096), ("tiny_1", 2, 1)]
 
 
+# edge colorings whose reference sweep outputs are stored
+COLOR_EDGE_EXEC = {("aniso5_120x90", 2, 7), ("plaw_3k", 2, 1000), ("st27_16", 2, 13), ("arrow_64", 2, 5),
+                   ("band_5k", 1, 3)}
+
+
 def key_color_edge(m, d, t):
     return f"coloredge__{m}__d{d}__t{t}"
 

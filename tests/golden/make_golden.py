@@ -36,8 +36,8 @@ from cases import (COLOR3_CASES, COLOR_CASES, COLOR_ENV_CASES, COLOR_INIT_CASES,
                    SIMDIFY_CASES, TRAVERSE_CASES, arr_digest, digest, key_color, key_power, key_power_flat,
                    init_perm, key_color3, key_color_env, key_color_init, key_color_row, key_color_unsym,
                    key_hopeless, key_power_tri, key_simdify, key_trav, sell_layout, triangle,
-                   DEEP_CASES, DEEP_EXEC_CASES, key_deep, COLOR_EDGE_CASES, key_color_edge, POWER_EDGE_CASES,
-                   key_power_edge)
+                   DEEP_CASES, DEEP_EXEC_CASES, key_deep, COLOR_EDGE_CASES, COLOR_EDGE_EXEC, key_color_edge,
+                   POWER_EDGE_CASES, key_power_edge)
 from oracle import refpy  # noqa: E402
 from oracle.refpy import RefInterface  # noqa: E402
 from race_gb300 import matgen  # noqa: E402
@@ -56,6 +56,25 @@ def flat_power_tree(tr):
         flat += [leaf["lo"], leaf["hi"], leaf["stage"], leaf["parent"], len(leaf["lp"]) - 1] + leaf["lp"]
         flat += [len(leaf["hid"])] + leaf["hid"]
     return np.array(flat, np.int32)
+
+
+def exec_outputs(rc, A, d, p, ip):
+    """The reference executor's outputs of the example kernels on its own
+    coloring (SymmSpMV and KACZ need distance 2)."""
+    P = A.permuted(p, ip)
+    U = P.upper()
+    x0 = matgen.uniform_vector(A.n, 0)
+    b0 = matgen.uniform_vector(A.n, 1)
+    out = {}
+    for kern, name, mat, rev in [(2, "symmspmv", U, False), (3, "gs", P, False), (3, "gsrev", P, True),
+                                 (4, "kacz", P, False), (0, "spmv", P, False)]:
+        if kern in (2, 4) and d != 2:
+            continue
+        x = x0.copy()
+        b = np.zeros(A.n) if kern in (0, 2) else b0.copy()
+        rc.execute(kern, rev, mat, x, b)
+        out[name] = b if kern in (0, 2) else x
+    return out
 
 
 def main():
@@ -110,18 +129,8 @@ def main():
         g[k + "__stage"] = np.array(rc.max_stage())
         g[k + "__serial"] = rc.serial_part()
         if (m, d, t) in EXEC_CASES:
-            P = A.permuted(p, ip)
-            U = P.upper()
-            x0 = matgen.uniform_vector(A.n, 0)
-            b0 = matgen.uniform_vector(A.n, 1)
-            for kern, name, mat, rev in [(2, "symmspmv", U, False), (3, "gs", P, False), (3, "gsrev", P, True),
-                                         (4, "kacz", P, False), (0, "spmv", P, False)]:
-                if kern in (2, 4) and d != 2:
-                    continue
-                x = x0.copy()
-                b = np.zeros(A.n) if kern in (0, 2) else b0.copy()
-                rc.execute(kern, rev, mat, x, b)
-                g[k + f"__out_{name}"] = b if kern in (0, 2) else x
+            for name, out in exec_outputs(rc, A, d, p, ip).items():
+                g[k + f"__out_{name}"] = out
         rc.close()
         print(k, "threads", int(g[k + "__threads"]), "eff %.3f" % float(g[k + "__eff"]))
 
@@ -185,6 +194,10 @@ def main():
         g[k + "__tree"] = rc.tree_flat()
         g[k + "__threads"] = np.array(rc.threads())
         g[k + "__eff"] = np.array(rc.efficiency())
+        if (m, d, t) in COLOR_EDGE_EXEC:
+            g[k + "__serial"] = rc.serial_part()
+            for name, out in exec_outputs(rc, A, d, p, ip).items():
+                g[k + f"__out_{name}"] = out
         rc.close()
         print(k, "threads", int(g[k + "__threads"]))
 

@@ -27,12 +27,19 @@ def _tree(golden, k):
     return parse_zone_tree(golden[k + "__tree"])
 
 
-@pytest.mark.parametrize("m,d,t", sorted(EXEC_CASES))
-def test_executor_walk_matches_reference(golden, mats, m, d, t):
+def _edge_exec_cases():
+    from cases import COLOR_EDGE_EXEC, key_color_edge
+    return [(m, d, t, key_color_edge(m, d, t)) for m, d, t in sorted(COLOR_EDGE_EXEC)]
+
+
+@pytest.mark.parametrize("m,d,t,k", [(m, d, t, key_color(m, d, t)) for m, d, t in sorted(EXEC_CASES)]
+                         + _edge_exec_cases())
+def test_executor_walk_matches_reference(golden, mats, m, d, t, k):
     """The sequential zone-tree walk reproduces the reference's threaded
-    executor bit for bit on its own schedule."""
+    executor bit for bit on its own schedule (also at the thread-count
+    edges: 3, 5, 7, 13 and 1000 requested threads)."""
     A = mats[m]
-    k = key_color(m, d, t)
+    checked = 0
     perm = golden[k + "__perm"]
     inv = np.empty_like(perm); inv[perm] = np.arange(A.n, dtype=np.int32)
     P = A.permuted(perm, inv)
@@ -51,6 +58,8 @@ def test_executor_walk_matches_reference(golden, mats, m, d, t):
         orc.exec_tree(nodes, 2, golden[k + "__serial"], kern, rev, mat, x, b)
         out = b if kern in (orc.K_SPMV, orc.K_SYMMSPMV) else x
         np.testing.assert_array_equal(out, golden[key], err_msg=name)
+        checked += 1
+    assert checked == (5 if d == 2 else 3)
 
 
 @pytest.mark.parametrize("m,p,c", POWER_CASES)

@@ -104,7 +104,8 @@ def test_coloring_balancing_rows(golden, mats, m, d, t):
 def test_coloring_at_thread_count_edges(golden, mats, m, d, t):
     """One thread, odd and prime thread counts, and far more threads than
     the matrix can use: the reference's permutation, zone tree, thread
-    count and efficiency."""
+    count and efficiency, and (where stored) the reference executor's sweep
+    outputs from the engine's wave mode."""
     A = mats[m]
     k = key_color_edge(m, d, t)
     assert str(golden[k + "__digest"]) == digest(A)
@@ -114,3 +115,29 @@ def test_coloring_at_thread_count_edges(golden, mats, m, d, t):
     np.testing.assert_array_equal(rc.getZoneTreeFlat(), golden[k + "__tree"])
     assert rc.getNumThreads() == int(golden[k + "__threads"])
     assert rc.getEfficiency() == float(golden[k + "__eff"])
+    if k + "__out_gs" not in golden:
+        return
+    rc.setSweepMode(ri.SWEEP_WAVE)
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    U = P.upper()
+    x0 = matgen.uniform_vector(A.n, 0)
+    b0 = matgen.uniform_vector(A.n, 1)
+    for kern, name, mat, rev in [(ri.SYMMSPMV, "symmspmv", U, False), (ri.GS, "gs", P, False),
+                                 (ri.GS, "gsrev", P, True), (ri.KACZ, "kacz", P, False),
+                                 (ri.SPMV, "spmv", P, False)]:
+        if k + f"__out_{name}" not in golden:
+            continue
+        zero_b = kern in (ri.SYMMSPMV, ri.SPMV)
+        dm = ri.DeviceCsr.from_csr(mat, "cuda", torch.float64)
+        x = torch.tensor(x0, device="cuda")
+        b = torch.zeros(A.n, dtype=torch.float64, device="cuda") if zero_b else torch.tensor(b0, device="cuda")
+        fid = rc.registerFunction(kern, ri.Operands(dm, x, b))
+        assert fid >= 0
+        assert rc.executeFunction(fid, rev) == 0
+        torch.cuda.synchronize()
+        out = (b if zero_b else x).cpu().numpy()
+        ref = golden[k + f"__out_{name}"]
+        if np.diff(mat.row_ptr).max() <= 512:
+            np.testing.assert_array_equal(out, ref, err_msg=name)
+        else:  # rows above 512 entries run with a warp reduction
+            assert np.max(np.abs(out - ref)) <= 1e-12 * np.max(np.abs(ref)), name
