@@ -61,3 +61,25 @@ def test_regret_and_best_fixed_config():
                        np.array(["x"] * 3), np.ones((3, 2), np.int64), "symmgs")
     # config 2 has the lowest mean regret (0.5+0.2+0)/3
     assert tuner.best_fixed_config(ds) == 2
+
+
+def test_tuning_matrices_have_no_hopeless_regions():
+    """The recursion depth (RACE_MAX_RECURSION_STAGES) changes a partition
+    only where two consecutive levels exceed the budget by more than the
+    cut-off (50). On the seeded tuning matrices none does at any searched
+    power and budget, so the depth is not a tuning knob there (the first
+    matrices up to at least 8 and all four families; the oracle's BFS
+    levels)."""
+    from oracle import oracle as orc
+    families = set()
+    idx = 0
+    while idx < 8 or len(families) < 4:
+        fam, A = tuner.dataset_matrix(idx)
+        idx += 1
+        families.add(fam)
+        _, _, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
+        lp = np.concatenate([[0], np.cumsum(lr)]).astype(np.int32)
+        for p, c in tuner.CONFIGS:
+            part = orc.mpk_partition(p, A.n, A.nnz, c * 1e6, 2.0, 50, lp, ln)
+            assert part is not None and part[1].size == 0, (idx - 1, fam, p, c)
+    assert families == {"lap7", "st27", "band", "plaw"}
