@@ -297,6 +297,12 @@ def arr_digest(a) -> str:
     return hashlib.sha256(np.ascontiguousarray(a, np.int32).tobytes()).hexdigest()[:16]
 
 
+def f64_digest(a) -> str:
+    """A checksum of the exact bits of a float64 array (outputs stored as
+    digests where the arrays themselves would be large)."""
+    return hashlib.sha256(np.ascontiguousarray(a, np.float64).tobytes()).hexdigest()[:16]
+
+
 def key_color(m, d, t):
     return f"color__{m}__d{d}__t{t}"
 

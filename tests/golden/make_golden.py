@@ -37,7 +37,7 @@ from cases import (COLOR3_CASES, COLOR_CASES, COLOR_ENV_CASES, COLOR_INIT_CASES,
                    init_perm, key_color3, key_color_env, key_color_init, key_color_row, key_color_unsym,
                    key_hopeless, key_power_tri, key_simdify, key_trav, sell_layout, triangle,
                    DEEP_CASES, DEEP_EXEC_CASES, key_deep, COLOR_EDGE_CASES, COLOR_EDGE_EXEC, key_color_edge,
-                   POWER_EDGE_CASES, key_power_edge)
+                   POWER_EDGE_CASES, key_power_edge, f64_digest)
 from oracle import refpy  # noqa: E402
 from oracle.refpy import RefInterface  # noqa: E402
 from race_gb300 import matgen  # noqa: E402
@@ -409,10 +409,12 @@ def main():
         perm, ip = rp.perm()
         tr = rp.tree()
         assert (rp.coverage() == 1).all()
+        out = rp.execute(A.permuted(perm, ip), matgen.uniform_vector(A.n, 0))[1:]
         rp.close()
         g[k + "__digest"] = np.array(digest(A))
         g[k + "__tree"] = flat_power_tree(tr)
         g[k + "__perm"] = perm
+        g[k + "__out_digest"] = np.array(f64_digest(out))  # the reference MPK executor's outputs
         print(k, "leaves", len(tr), "groups", len(tr[0]["lp"]) - 1, "hopeless", tr[0]["hid"])
 
     # full-size MPK configuration: digests only

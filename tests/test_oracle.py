@@ -276,6 +276,22 @@ def test_oracle_mpk_recursion_matches_reference(golden, mats):
         np.testing.assert_array_equal(tp, golden[k + "__perm"], err_msg=k)
 
 
+def test_reference_mpk_at_edge_parameters_equals_spmv_chain(golden, mats):
+    """The reference's MPK executor at edge parameters (power 1 and 16, one
+    group for the whole matrix, tiny budgets with hopeless regions, a
+    one-row matrix) gives p sequential SpMVs of the permuted matrix bit for
+    bit (its outputs are stored as a checksum of their exact bits)."""
+    from cases import POWER_EDGE_CASES, f64_digest, key_power_edge
+    for m, p, c in POWER_EDGE_CASES:
+        k = key_power_edge(m, p, c)
+        A = mats[m]
+        perm = golden[k + "__perm"]
+        inv = np.empty_like(perm)
+        inv[perm] = np.arange(A.n, dtype=np.int32)
+        Y = orc.mpk_plain(A.permuted(perm, inv), matgen.uniform_vector(A.n, 0), p)
+        assert f64_digest(Y[1:]) == str(golden[k + "__out_digest"]), k
+
+
 def test_reference_mpk_on_deep_partitions_equals_spmv_chain(golden, mats):
     """With recursion deeper than one stage too, the reference's MPK executor
     (recursivePowerCallSerial over the whole leaf tree) gives p sequential
