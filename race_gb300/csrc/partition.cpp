@@ -124,12 +124,14 @@ std::vector<int> hopelessRegions(std::vector<int> violated, int totalLevel, int 
 // non-zeros of each level including those of the boundary regions
 // (getElemUpperLimit, :88-99), bndPtr the level offsets (L+1) of each
 // boundary region. bndGroupPtr gets each region's offsets at the
-// consolidated group starts (newBoundaryLevelPtr). False where a hopeless
-// region lacks its boundary levels (the reference stops there).
+// consolidated group starts (newBoundaryLevelPtr). With checkBoundaries,
+// false where a hopeless region lacks its boundary levels (the reference
+// stops there); the trimming of the regions rules that out, so stage 0
+// groups without the check, as before.
 bool consolidate(const std::vector<int> &levelPtr, const std::vector<int> &nnzInLevel, int power, int graphRows,
                  long long graphNnz, double cacheSize, double safety, int cutoff,
                  const std::vector<std::vector<int>> &bndPtr, StagePartition &sp,
-                 std::vector<std::vector<int>> &bndGroupPtr) {
+                 std::vector<std::vector<int>> &bndGroupPtr, bool checkBoundaries) {
     const int L = (int)nnzInLevel.size();
     // getBytePerNNZ / getElemUpperLimit (matrixPower.cpp:88-99, 134-140)
     const double nnzr = graphNnz / (double)graphRows;
@@ -156,7 +158,7 @@ bool consolidate(const std::vector<int> &levelPtr, const std::vector<int> &nnzIn
     int group = 0, levelCtr = 0;
     double sumElem = 0;
     for (int level = 0; level < L; ++level) {
-        if (hs >= 0 && (hs - boundary < 0 || he + boundary > L - 1)) return false;
+        if (checkBoundaries && hs >= 0 && (hs - boundary < 0 || he + boundary > L - 1)) return false;
         const double cur = elem(level);
         sumElem += cur;
         bool hopeless = false, force = false;
@@ -378,7 +380,7 @@ bool recurse(RecursionContext &ctx, int parent, const std::vector<std::vector<in
             return false;
         StagePartition sp;
         if (!consolidate(levelPtr, nnzInLevel, ctx.power, ctx.n, ctx.graphNnz, ctx.cacheSize, ctx.safety, cutoff,
-                         bndPtr, sp, childBnd))
+                         bndPtr, sp, childBnd, true))
             return false;
         leaf.groupPtr = sp.groupPtr;
         leaf.hopeless = sp.hopeless;
@@ -405,7 +407,7 @@ StagePartition stagePartition(const LevelData &ld, int startRow, int power, int 
     for (int l = 0; l < L; ++l) levelPtr[l + 1] = levelPtr[l] + ld.levelRow[l];
     std::vector<int> nnzInLevel(ld.levelNnz.begin(), ld.levelNnz.begin() + L);
     std::vector<std::vector<int>> none;
-    consolidate(levelPtr, nnzInLevel, power, graphRows, graphNnz, cacheSize, safety, cutoff, {}, sp, none);
+    consolidate(levelPtr, nnzInLevel, power, graphRows, graphNnz, cacheSize, safety, cutoff, {}, sp, none, false);
     return sp;
 }
 
