@@ -341,6 +341,17 @@ int race_mpk_recursive_partition(int n, const int *rowPtr, const int *col, int *
                                  long long graphNnz, double cacheSize, double safety, const int *stageCutoff,
                                  int numStages, int *treeBuf, int cap, int *treeLen);
 
+/* Host-only: one traversal of rows [lo,hi) of the current permuted space
+ * with RACE's distance-1 or distance-2 rules (dist 1 or 2;
+ * traverse_GAP_graphSoA.cpp:135-641): the engine's own traversal, which it
+ * runs on the host for ranges shorter than RACE_GPU_HOST_TRAVERSE_BELOW.
+ * rowPtr/col: the traversal graph (original rows); totalPerm/totalInvPerm
+ * (n each) are updated in place and levelRow/levelNnz written when
+ * cap >= *totalLevel (otherwise nothing changes and *totalLevel says how
+ * much room is needed). */
+int race_traverse_host(int n, const int *rowPtr, const int *col, int *totalPerm, int *totalInvPerm, int lo, int hi,
+                       int dist, int *levelRow, int *levelNnz, int cap, int *totalLevel);
+
 /* Host-only: RACE's level recursion (level_recursion.cpp:149-376, the
  * zone tree of race_color) with the traversal supplied by the caller instead
  * of the engine's GPU BFS. `trav` runs one traversal of rows [lo,hi) of the

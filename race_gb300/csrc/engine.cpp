@@ -34,6 +34,7 @@ void Engine::color() {
         n, requested, dist, d2, lbTarget, params, [this](int lo, int hi) { return traverse(lo, hi, dist); },
         [this](int lo, int hi) { return rangeNnz(lo, hi); });
     lr.levelBalancing();
+    syncDevicePerm();
     availableThreads = lr.availableThreads;
     tree = std::make_unique<ZoneTree>(lr.tree);
     for (int dir = 0; dir < 2; ++dir) {
@@ -622,6 +623,26 @@ int race_mpk_recursive_partition(int n, const int *rowPtr, const int *col, int *
         }
         *treeLen = (int)buf.size();
         if (treeBuf && cap >= *treeLen) memcpy(treeBuf, buf.data(), sizeof(int) * buf.size());
+        memcpy(totalPerm, tp.data(), sizeof(int) * n);
+        memcpy(totalInvPerm, ti.data(), sizeof(int) * n);
+    });
+}
+
+int race_traverse_host(int n, const int *rowPtr, const int *col, int *totalPerm, int *totalInvPerm, int lo, int hi,
+                       int dist, int *levelRow, int *levelNnz, int cap, int *totalLevel) {
+    if (n < 1 || !rowPtr || !col || !totalPerm || !totalInvPerm || lo < 0 || hi > n || lo > hi ||
+        (dist != race::DIST_ONE && dist != race::DIST_TWO) || !totalLevel || (cap > 0 && (!levelRow || !levelNnz)))
+        return RACE_ERR_INVALID_ARG;
+    return guard(nullptr, [&] {
+        std::vector<int> tp(totalPerm, totalPerm + n), ti(totalInvPerm, totalInvPerm + n);
+        race::HostTraverseScratch sc;
+        race::LevelData ld;
+        if (!race::traverseRangeHost(n, rowPtr, col, tp, ti, lo, hi, dist, sc, ld))
+            throw Error(RACE_ERR_GRAPH_TRAVERSAL, "some rows went missing in BFS");
+        *totalLevel = ld.totalLevel;
+        if (cap < ld.totalLevel) return;
+        std::copy(ld.levelRow.begin(), ld.levelRow.end(), levelRow);
+        std::copy(ld.levelNnz.begin(), ld.levelNnz.end(), levelNnz);
         memcpy(totalPerm, tp.data(), sizeof(int) * n);
         memcpy(totalInvPerm, ti.data(), sizeof(int) * n);
     });

@@ -7,6 +7,7 @@
 #include "coloring.h"
 #include "common.cuh"
 #include "lb.h"
+#include "traverse_host.h"
 #include "waves.h"
 
 namespace race {
@@ -177,6 +178,13 @@ class Engine {
     // power results
     int mpkStride = 2;  // issue order of the MPK wavefront (1: RACE's, 2: GPU default)
     int mpkSplit = 0;   // powers per wavefront segment of the MPK issue order (0: all powers at once)
+    // Ranges shorter than this are traversed on the host (RACE_GPU_HOST_TRAVERSE_BELOW,
+    // 0: never); the device permutation is then refreshed before the next
+    // GPU traversal and at the end of the coloring.
+    int hostTraverseBelow = 0;
+    bool devPermStale = false;
+    HostTraverseScratch hostScratch;
+    void syncDevicePerm();
     bool powerReady = false;
     int highestPower = 1, highestSubPower = 1;
     std::vector<int> levelPtr, groupPtr, unlockRow, dangerRow;

@@ -281,6 +281,7 @@ Engine::Engine(int nrow, int nthreads, int dist_, const int *rowPtr, const int *
     dStatus.alloc(4);
     if (const char *st = getenv("RACE_GPU_MPK_STRIDE")) mpkStride = atoi(st) == 1 ? 1 : 2;
     if (const char *sp = getenv("RACE_GPU_MPK_SPLIT")) mpkSplit = std::max(0, atoi(sp));
+    if (const char *ht = getenv("RACE_GPU_HOST_TRAVERSE_BELOW")) hostTraverseBelow = std::max(0, atoi(ht));
     if (const char *sm = getenv("RACE_GPU_SWEEP_MODE")) {
         std::string m(sm);
         sweepMode = m == "leaf" ? SWEEP_LEAF : m == "wave" ? SWEEP_WAVE : m == "gather" ? SWEEP_GATHER : SWEEP_AUTO;
@@ -299,11 +300,28 @@ long long Engine::rangeNnz(int lo, int hi) const {
     return s;
 }
 
+void Engine::syncDevicePerm() {
+    if (!devPermStale) return;
+    dPerm.upload(hPerm.data(), n, stream);
+    dInvPerm.upload(hInvPerm.data(), n, stream);
+    RACE_CUDA(cudaStreamSynchronize(stream));
+    devPermStale = false;
+}
+
 LevelData Engine::traverse(int lo, int hi, int mode, const std::string &mtxType) {
     LevelData ld;
     if (hi <= lo) return ld;
     const int len = hi - lo;
     cudaStream_t s = stream;
+    // A short coloring range costs the GPU a few launches and host round
+    // trips per level for little work: traverse it on the host instead.
+    if (mtxType == "N" && (mode == DIST_ONE || mode == DIST_TWO) && len < hostTraverseBelow) {
+        if (!traverseRangeHost(n, hRowPtr.data(), hCol.data(), hPerm, hInvPerm, lo, hi, mode, hostScratch, ld))
+            throw Error(RACE_ERR_GRAPH_TRAVERSAL, "some rows went missing in BFS");
+        devPermStale = true;
+        return ld;
+    }
+    syncDevicePerm();
     int totalLevel = 0;
     if (mtxType == "N") {
         ++stamp;

@@ -434,10 +434,30 @@ def test_three_block_phases_reproduce_reference(golden, mats, m, t):
 
 
 
-def _zone_tree_host(A, d, t, d2type, cap, init=None, params=None, lb_target=1):
+def _host_traverse(A, d, lo, hi, tp, ti):
+    """The engine's host traversal (race_traverse_host) in the oracle's
+    calling convention: (totalPerm, totalInvPerm, levelRow, levelNnz)."""
+    L = _lib.lib()
+    rp, cl = np.ascontiguousarray(A.row_ptr, np.int32), np.ascontiguousarray(A.col, np.int32)
+    tp, ti = np.array(tp, np.int32), np.array(ti, np.int32)
+    total = C.c_int()
+    args = [A.n, rp.ctypes.data, cl.ctypes.data, tp.ctypes.data, ti.ctypes.data, lo, hi, d]
+    # the first call only sizes the level arrays (distance 2 can count more
+    # levels than the range has rows); the second traverses
+    before = tp.copy()
+    _lib.check(L.race_traverse_host(*args, None, None, 0, C.byref(total)))
+    np.testing.assert_array_equal(tp, before)  # nothing written without room
+    lr = np.zeros(max(total.value, 1), np.int32)
+    ln = np.zeros_like(lr)
+    _lib.check(L.race_traverse_host(*args, lr.ctypes.data, ln.ctypes.data, lr.size, C.byref(total)))
+    return tp, ti, lr[: total.value], ln[: total.value]
+
+
+def _zone_tree_host(A, d, t, d2type, cap, init=None, params=None, lb_target=1, host_traverse=False):
     """The engine's level recursion (race_zone_tree_host) driven by the
-    oracle's traversal, which keeps the running permutation here (starting
-    from `init`, the identity by default)."""
+    oracle's traversal (or, with host_traverse, the engine's own host
+    traversal), which keeps the running permutation here (starting from
+    `init`, the identity by default)."""
     L = _lib.lib()
     lens = np.diff(A.row_ptr).astype(np.int64)
     tp0 = np.arange(A.n, dtype=np.int32) if init is None else np.ascontiguousarray(init, np.int32)
@@ -448,7 +468,10 @@ def _zone_tree_host(A, d, t, d2type, cap, init=None, params=None, lb_target=1):
     @_lib.TRAVERSE_FN
     def trav(user, lo, hi, lr_ptr, ln_ptr, lcap, total):
         try:
-            tp, ti, lr, ln, _ = orc.traverse(A, d, lo, hi, state["tp"], state["ti"])
+            if host_traverse:
+                tp, ti, lr, ln = _host_traverse(A, d, lo, hi, state["tp"], state["ti"])
+            else:
+                tp, ti, lr, ln, _ = orc.traverse(A, d, lo, hi, state["tp"], state["ti"])
             state["tp"], state["ti"] = tp, ti
             if len(lr) > lcap:
                 return 1
@@ -738,6 +761,41 @@ def test_level_recursion_balancing_rows(golden, mats, monkeypatch):
         k = key_color_row(m, d, t)
         gold = golden[k + "__tree"]
         tree, avail, perm = _zone_tree_host(A, d, t, 0, 2 * gold.size + 1024, lb_target=0)
+        np.testing.assert_array_equal(tree, gold, err_msg=k)
+        assert avail == int(golden[k + "__threads"]), k
+        np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)
+
+
+@pytest.mark.parametrize("m,d", [c for c in __import__("cases").TRAVERSE_CASES if c[1] in (1, 2)])
+def test_host_traversal_matches_reference(golden, mats, m, d):
+    """The engine's host traversal (run for short coloring ranges with
+    RACE_GPU_HOST_TRAVERSE_BELOW) of the whole matrix gives the reference's
+    permutation and level histogram."""
+    from cases import key_trav
+    A = mats[m]
+    k = key_trav(m, d)
+    ident = np.arange(A.n, dtype=np.int32)
+    tp, ti, lr, ln = _host_traverse(A, d, 0, A.n, ident, ident)
+    np.testing.assert_array_equal(tp, golden[k + "__perm"])
+    np.testing.assert_array_equal(lr, golden[k + "__levelRow"])
+    np.testing.assert_array_equal(ln, golden[k + "__levelNnz"])
+    np.testing.assert_array_equal(ti[tp], np.arange(A.n))
+
+
+def test_level_recursion_with_host_traversal_matches_reference(golden, mats, monkeypatch):
+    """The engine's level recursion driven by the engine's own host
+    traversal on every sub-range (what RACE_GPU_HOST_TRAVERSE_BELOW does for
+    short ranges) gives the reference's zone trees, thread counts and
+    permutations: all coloring cases and the thread-count edges."""
+    from cases import COLOR_EDGE_CASES, key_color_edge
+    for var in ("RACE_EFFICIENCY", "RACE_THREADS"):
+        monkeypatch.delenv(var, raising=False)
+    cases = [(m, d, t, key_color(m, d, t)) for m, d, t in COLOR_CASES]
+    cases += [(m, d, t, key_color_edge(m, d, t)) for m, d, t in COLOR_EDGE_CASES]
+    for m, d, t, k in cases:
+        A = mats[m]
+        gold = golden[k + "__tree"]
+        tree, avail, perm = _zone_tree_host(A, d, t, 0, 2 * gold.size + 1024, host_traverse=True)
         np.testing.assert_array_equal(tree, gold, err_msg=k)
         assert avail == int(golden[k + "__threads"]), k
         np.testing.assert_array_equal(perm, golden[k + "__perm"], err_msg=k)

@@ -141,3 +141,21 @@ def test_coloring_at_thread_count_edges(golden, mats, m, d, t):
             np.testing.assert_array_equal(out, ref, err_msg=name)
         else:  # rows above 512 entries run with a warp reduction
             assert np.max(np.abs(out - ref)) <= 1e-12 * np.max(np.abs(ref)), name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("below", [1000, 1 << 30])
+@pytest.mark.parametrize("m,d,t", [("plaw_3k", 2, 1000), ("lap7_32", 2, 64), ("aniso9_100x80", 1, 16)])
+def test_host_traversal_of_short_ranges(golden, mats, monkeypatch, below, m, d, t):
+    """RACE_GPU_HOST_TRAVERSE_BELOW: ranges shorter than the threshold are
+    traversed on the host (all of them with a huge threshold); the coloring
+    is the reference's all the same."""
+    from cases import COLOR_EDGE_CASES
+    monkeypatch.setenv("RACE_GPU_HOST_TRAVERSE_BELOW", str(below))
+    A = mats[m]
+    k = key_color_edge(m, d, t) if (m, d, t) in COLOR_EDGE_CASES else f"color__{m}__d{d}__t{t}"
+    rc = ri.Interface(A.n, t, d, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor() == 0
+    np.testing.assert_array_equal(rc.getPerm(), golden[k + "__perm"])
+    np.testing.assert_array_equal(rc.getZoneTreeFlat(), golden[k + "__tree"])
+    assert rc.getNumThreads() == int(golden[k + "__threads"])
