@@ -120,13 +120,16 @@ void example(RACE::gb300::Interface &ce, int *d_rowPtr, int *d_col, double *d_va
 @pytest.mark.parametrize("key,power,sub,rows", [("power__st27_24__p8__c2000000", 8, 1, 32),
                                                 ("power__band_5k__p8__c3300", 2, 3, 7),
                                                 ("power__tiny_1__p2__c10000", 2, 2, 32),
-                                                ("power__islands_330__p3__c20000", 3, 2, 5)])
+                                                ("power__islands_330__p3__c20000", 3, 2, 5),
+                                                ("powertri__lap7_16__L__p4__c20000", 4, 1, 32),
+                                                ("powertri__plaw_3k__U__p8__c50000", 8, 1, 16)])
 def test_power_call_schedule(golden, tmp_path, key, power, sub, rows):
     """The matrix-power call table on the reference's level groups: every
     row gets every (power, sub-power) exactly once, in order; the call of
     group g at flat step q runs in wavefront step g + 2(q-1), so everything it
-    reads (flat step q-1 of groups g-1..g+1) ran in an earlier step; and a
-    four-argument functor sees (pow, subPow) = ((q-1)/sub+1, (q-1)%sub+1)."""
+    reads (flat step q-1 of groups up to g+1, any earlier group included, as
+    triangular partitions need) ran in an earlier step; and a four-argument
+    functor sees (pow, subPow) = ((q-1)/sub+1, (q-1)%sub+1)."""
     exe = tmp_path / "pc"
     r = subprocess.run([_nvcc(), *NVCC, str(ROOT / "tests" / "power_calls_check.cu"), "-o", str(exe)],
                        capture_output=True, text=True)
