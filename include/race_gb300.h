@@ -139,6 +139,13 @@ int race_get_device_phases(race_engine *e, int rev, const int **leafLo, const in
 /* MPK level groups (consolidated levelPtr of the reference's MPLeaf::lp,
  * matrixPowerRecursive.h:27-62), *len = groups+1. */
 int race_get_power_groups(race_engine *e, int *buf, int cap, int *len);
+/* The MPK partition's leaf tree (mtxPowerRecursive's MPLeaf tree,
+ * matrixPowerRecursive.h:27-62; the reference prints it with printTree):
+ * count, then per leaf lo, hi, stage, parent, numGroups,
+ * groupPtr[numGroups+1], numHopeless, hopeless[numHopeless]; the root alone
+ * without hopeless regions. *len receives the length; data is written when
+ * cap is large enough. */
+int race_get_power_tree(race_engine *e, int *buf, int cap, int *len);
 
 /* Interface::registerFunction (interface.h:149-157, interface.cpp:391-485)
  * with a built-in device kernel in place of a host callback; `power`

@@ -38,6 +38,7 @@ EXPORTS = [
     "race_simdify", "race_simdify_schedule", "race_simdify_d1", "race_get_highest_power", "race_get_device_phases",
     "race_zone_tree_host", "race_mpk_stage_partition", "race_mpk_recursion_permute", "race_gather_plan",
     "race_mpk_recursive_partition", "race_set_sub_power", "race_get_sub_power", "race_traverse_host",
+    "race_get_power_tree",
 ]
 
 
@@ -88,6 +89,7 @@ def lib():
             "race_get_status": [vp], "race_set_power": [vp, i, i], "race_get_power": [vp, i, ip],
             "race_set_sub_power": [vp, i, i], "race_get_sub_power": [vp, i, ip],
             "race_traverse_host": [i, vp, vp, vp, vp, i, i, i, vp, vp, i, ip],
+            "race_get_power_tree": [vp, vp, i, ip],
             "race_set_sweep_mode": [vp, i], "race_get_sweep_info": [vp, i, i, ip, ip, ip, ip, ip],
             "race_spmv_plain": [vp, i, vp, vp, vp, vp, vp], "race_spmv_power_layout": [vp, i, i],
             "race_mpk_noalloc": [i, vp, vp, vp, vp, vp, i, i, vp, vp],

@@ -95,26 +95,22 @@ void Engine::powerPrepare(int hp, double cacheSize, double safety, const std::st
     if (hopeless) {
         // Hopeless regions: the reference's stage-0 groups around them
         // (stagePartition) and, for mtxType N, its recursion, which reorders
-        // the rows of each hopeless group and of its boundary groups (one
-        // stage by default: recursePermutation; more: recursivePartition,
-        // whose deeper stages reorder rows inside those groups again).
+        // the rows of each hopeless group and of its boundary groups
+        // (recursivePartition: one stage by default, deeper stages reorder
+        // rows inside those groups again) and gives the leaf tree.
         // Every stage-0 group keeps its row range, so the MPK's
         // neighbour-group dependencies still hold.
         const StagePartition sp = stagePartition(ld, 0, P, n, nnz, cacheSize, safety, cutoff);
+        powerTree.assign(1, MpkLeaf{0, n, 0, -1, sp.groupPtr, sp.hopeless});
         if (mtxType == "N" && !sp.hopeless.empty()) {
-            bool ok;
-            if (maxRec > 1) {
-                // cut-off of stage s (get_cache_violation_cutoff, matrixPowerRecursive.cpp:81-100)
-                std::vector<int> stageCutoff(std::min(maxRec, 1 << 16));
-                const std::vector<int> &cv = params.cacheViolationCutoff;
-                for (int s = 0; s < (int)stageCutoff.size(); ++s)
-                    stageCutoff[s] = s < (int)cv.size() - 1 ? cv[s + 1] : cv[0];
-                std::vector<MpkLeaf> tree;
-                ok = recursivePartition(n, hRowPtr.data(), hCol.data(), hPerm, hInvPerm, sp, P, nnz, cacheSize, safety,
-                                        stageCutoff, tree);
-            } else {
-                ok = recursePermutation(n, hRowPtr.data(), hCol.data(), hPerm, hInvPerm, sp.groupPtr, sp.hopeless, P);
-            }
+            // cut-off of stage s (get_cache_violation_cutoff, matrixPowerRecursive.cpp:81-100);
+            // stages from maxRec on have none
+            std::vector<int> stageCutoff(std::min(std::max(maxRec, 1), 1 << 16));
+            const std::vector<int> &cv = params.cacheViolationCutoff;
+            for (int s = 0; s < (int)stageCutoff.size(); ++s)
+                stageCutoff[s] = s < (int)cv.size() - 1 ? cv[s + 1] : cv[0];
+            const bool ok = recursivePartition(n, hRowPtr.data(), hCol.data(), hPerm, hInvPerm, sp, P, nnz, cacheSize,
+                                               safety, stageCutoff, powerTree);
             if (!ok)
                 throw Error(RACE_ERR_GRAPH_TRAVERSAL,
                             "MPK recursion: rows of a hopeless group went missing, or its boundary groups do not exist");
@@ -146,6 +142,7 @@ void Engine::powerPrepare(int hp, double cacheSize, double safety, const std::st
     }
     groupPtr.push_back(levelPtr[L]);
     dangerRow.push_back(levelPtr[L > 0 ? L - 1 : 0]);
+    powerTree.assign(1, MpkLeaf{0, n, 0, -1, groupPtr, {}});
     powerReady = true;
 }
 
@@ -377,6 +374,20 @@ int race_get_device_phases(race_engine *e, int rev, const int **leafLo, const in
     *leafLo = d.leafLo.p;
     *leafHi = d.leafHi.p;
     *numLeaves = d.numLeaves;
+    return RACE_SUCCESS;
+}
+
+int race_get_power_tree(race_engine *e, int *buf, int cap, int *len) {
+    if (!e || !len || !e->eng->powerReady) return RACE_ERR_INVALID_ARG;
+    std::vector<int> flat{(int)e->eng->powerTree.size()};
+    for (const race::MpkLeaf &l : e->eng->powerTree) {
+        flat.insert(flat.end(), {l.lo, l.hi, l.stage, l.parent, (int)l.groupPtr.size() - 1});
+        flat.insert(flat.end(), l.groupPtr.begin(), l.groupPtr.end());
+        flat.push_back((int)l.hopeless.size());
+        flat.insert(flat.end(), l.hopeless.begin(), l.hopeless.end());
+    }
+    *len = (int)flat.size();
+    if (buf && cap >= *len) memcpy(buf, flat.data(), sizeof(int) * flat.size());
     return RACE_SUCCESS;
 }
 

@@ -7,6 +7,7 @@
 #include "coloring.h"
 #include "common.cuh"
 #include "lb.h"
+#include "partition.h"
 #include "traverse_host.h"
 #include "waves.h"
 
@@ -181,6 +182,8 @@ class Engine {
     // Ranges shorter than this are traversed on the host (RACE_GPU_HOST_TRAVERSE_BELOW,
     // 0: never); the device permutation is then refreshed before the next
     // GPU traversal and at the end of the coloring.
+    // the MPK partition's leaf tree (the root alone without hopeless regions)
+    std::vector<MpkLeaf> powerTree;
     int hostTraverseBelow = 0;
     bool devPermStale = false;
     HostTraverseScratch hostScratch;

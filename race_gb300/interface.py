@@ -265,6 +265,14 @@ class Interface:
                                           C.byref(npz), C.byref(nl)))
         return pp[: npz.value + 1], lo[: nl.value], hi[: nl.value]
 
+    def getPowerTree(self) -> np.ndarray:
+        """The MPK partition's leaf tree, flat (race_get_power_tree)."""
+        n = C.c_int()
+        self._check(lib().race_get_power_tree(self._h, None, 0, C.byref(n)))
+        buf = np.zeros(n.value, np.int32)
+        self._check(lib().race_get_power_tree(self._h, buf.ctypes.data, n.value, C.byref(n)))
+        return buf
+
     def getPowerGroups(self) -> np.ndarray:
         n = C.c_int()
         self._check(lib().race_get_power_groups(self._h, None, 0, C.byref(n)))

@@ -29,6 +29,10 @@ def test_default_partition_with_hopeless_regions(golden, mats, m, p, c):
     rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
     assert rc.RACEColor(p, c) == 0
     np.testing.assert_array_equal(rc.getPowerGroups(), golden[k + "__lp"])
+    tree = rc.getPowerTree()
+    assert int(tree[0]) == int(golden[k + "__leaves"])  # the root and one leaf per hopeless group
+    ng = int(tree[5])
+    np.testing.assert_array_equal(tree[7 + ng:8 + ng + int(tree[7 + ng])][1:], golden[k + "__hid"])
     _check_mpk(rc, A, p, golden[k + "__perm"])
 
 
@@ -72,6 +76,7 @@ def test_deep_recursion(golden, mats, m, p, c, stages, cuts):
     tree = golden[k + "__tree"]
     ng = int(tree[5])  # the root leaf: lo, hi, stage, parent, groups, lp
     np.testing.assert_array_equal(rc.getPowerGroups(), tree[6:7 + ng])
+    np.testing.assert_array_equal(rc.getPowerTree(), tree)  # every leaf of every stage
     _check_mpk(rc, A, p, golden[k + "__perm"])
 
 
@@ -88,6 +93,7 @@ def test_partition_at_edge_parameters(golden, mats, m, p, c):
     assert rc.RACEColor(p, c) == 0
     tree = golden[k + "__tree"]
     np.testing.assert_array_equal(rc.getPowerGroups(), tree[6:7 + int(tree[5])])
+    np.testing.assert_array_equal(rc.getPowerTree(), tree)
     _check_mpk(rc, A, p, golden[k + "__perm"])
 
 
