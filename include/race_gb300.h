@@ -392,6 +392,34 @@ int race_gather_plan(int kernel, int n, const int *rowPtr, const int *col, const
 int race_wave_plan(int kernel, int n, const int *rowPtr, const int *col, const int *phasePtr, const int *leafLo,
                    const int *leafHi, int numPhases, int *wavePtr, int *rows, int cap, int *numWaves, int *numRows);
 
+/* Host-only: the issue order of the persistent matrix-power kernel for
+ * numChunks chunks whose dependency intervals are depRange (6 ints per
+ * chunk: the chunk intervals [lo,hi] its columns fall in within the
+ * previous, own and next level group; hi < lo when empty). order 0: the
+ * chunk-level wavefront in runs of up to runLen chunks (1..32) per ticket,
+ * powers in segments of segLen (0: one segment), each item at least `lag`
+ * chunks of issue time after its inputs; chunkDie (NULL: one die) gives the
+ * L2 die (0 or 1) whose SMs run each chunk, and the runs are grouped into one
+ * queue per die. order 1: RACE's level-group order
+ * (functionManager.cpp:618-823) with stride `stride`, one chunk per run,
+ * chunkGroup giving each chunk's level group. Writes, when
+ * cap >= *numRuns, per run head[4] (first chunk, end chunk, power, flags),
+ * dep[8] (four chunk intervals that must be complete at the previous
+ * power) and rank (its position in the global order; may be NULL), and
+ * dieStart[3] (die d's queue is runs dieStart[d] .. dieStart[d+1]-1). No
+ * counterpart in the reference; exposed for tests. */
+int race_mpk_issue_order(const int *depRange, const int *chunkGroup, const int *chunkDie, int numChunks, int power,
+                         int order, int stride, int segLen, int runLen, int lag, int *head, int *dep, int *rank,
+                         int *dieStart, int cap, int *numRuns);
+
+/* The L2 die map of the current device as the engine measured it (once per
+ * process and device, at the first matrix-power registration or at this
+ * call): *numDies (1 or 2), *numSms and, when cap >= *numSms, smDie[sm] for
+ * every SM index. GB300's two dies each cache what their own SMs read; the
+ * matrix-power kernel keeps each chunk's work on one die. Synchronises the
+ * device on the first call. No counterpart in the reference. */
+int race_device_dies(int *numDies, int *smDie, int cap, int *numSms);
+
 /* RACE::Interface::getHighestPower (interface.cpp:1055-1058): the highest
  * power given to race_power_prepare (1 before it). */
 int race_get_highest_power(race_engine *e, int *power);

@@ -38,7 +38,7 @@ EXPORTS = [
     "race_simdify", "race_simdify_schedule", "race_simdify_d1", "race_get_highest_power", "race_get_device_phases",
     "race_zone_tree_host", "race_mpk_stage_partition", "race_mpk_recursion_permute", "race_gather_plan",
     "race_mpk_recursive_partition", "race_set_sub_power", "race_get_sub_power", "race_traverse_host",
-    "race_get_power_tree",
+    "race_get_power_tree", "race_mpk_issue_order", "race_device_dies",
 ]
 
 
@@ -118,6 +118,8 @@ def lib():
             "race_gather_plan": [i, i, vp, vp, vp, vp, vp, i, vp, vp, vp, i, ip],
             "race_simdify_schedule": [i, i, i, vp, vp, vp, vp, vp, i, i, vp, vp, i, ip],
             "race_simdify_d1": [i, i, i, vp, vp, vp, vp, vp, i, i],
+            "race_mpk_issue_order": [vp, vp, vp, i, i, i, i, i, i, i, vp, vp, vp, vp, i, ip],
+            "race_device_dies": [ip, vp, i, ip],
         }
         for name, args in sig.items():
             fn = getattr(L, name)

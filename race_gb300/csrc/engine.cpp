@@ -6,7 +6,9 @@
 #include <cstring>
 #include <numeric>
 
+#include "dies.h"
 #include "engine.h"
+#include "mpk_order.h"
 #include "partition.h"
 #include "simdify.h"
 
@@ -722,6 +724,52 @@ int race_gather_plan(int kernel, int n, const int *rowPtr, const int *col, const
                 memcpy(row, gp.row.data(), sizeof(int) * gp.row.size());
             }
         }
+    });
+}
+
+int race_mpk_issue_order(const int *depRange, const int *chunkGroup, const int *chunkDie, int numChunks, int power,
+                         int order, int stride, int segLen, int runLen, int lag, int *head, int *dep, int *rank,
+                         int *dieStart, int cap, int *numRuns) {
+    if (numChunks < 0 || (numChunks > 0 && !depRange) || power < 1 || power > 255 || !numRuns || lag < 0 ||
+        (order == 1 && numChunks > 0 && !chunkGroup) || (order != 0 && order != 1) || runLen < 1 ||
+        runLen > race::kMpkMaxRunLen)
+        return RACE_ERR_INVALID_ARG;
+    int numGroups = 0;
+    for (int c = 0; c < numChunks; ++c) {
+        for (int d = 0; d < 3; ++d) {
+            const int lo = depRange[6 * c + 2 * d], hi = depRange[6 * c + 2 * d + 1];
+            if (hi >= lo && (lo < 0 || hi >= numChunks)) return RACE_ERR_INVALID_ARG;
+        }
+        if (order == 1) {
+            if (chunkGroup[c] < 0 || (c > 0 && chunkGroup[c] < chunkGroup[c - 1])) return RACE_ERR_INVALID_ARG;
+            numGroups = chunkGroup[c] + 1;
+        }
+        if (chunkDie && chunkDie[c] != 0 && chunkDie[c] != 1) return RACE_ERR_INVALID_ARG;
+    }
+    return guard(nullptr, [&] {
+        const std::vector<int> dr(depRange, depRange + 6 * (size_t)numChunks);
+        const std::vector<int> cd = chunkDie ? std::vector<int>(chunkDie, chunkDie + numChunks) : std::vector<int>();
+        const race::MpkOrder o =
+            order == 1 ? race::mpkGroupOrder(dr, std::vector<int>(chunkGroup, chunkGroup + numChunks), numGroups,
+                                             power, stride == 1 ? 1 : 2, segLen)
+                       : race::mpkRunOrder(dr, numChunks, power, segLen, runLen, lag, cd);
+        *numRuns = o.numRuns();
+        if (head && dep && cap >= o.numRuns()) {
+            memcpy(head, o.head.data(), sizeof(int) * o.head.size());
+            memcpy(dep, o.dep.data(), sizeof(int) * o.dep.size());
+            if (rank) memcpy(rank, o.rank.data(), sizeof(int) * o.rank.size());
+        }
+        if (dieStart) memcpy(dieStart, o.dieStart.data(), sizeof(int) * 3);
+    });
+}
+
+int race_device_dies(int *numDies, int *smDie, int cap, int *numSms) {
+    if (!numDies || !numSms) return RACE_ERR_INVALID_ARG;
+    return guard(nullptr, [&] {
+        const race::DieMap &m = race::dieMap();
+        *numDies = m.numDies;
+        *numSms = (int)m.smDie.size();
+        if (smDie && cap >= (int)m.smDie.size()) memcpy(smDie, m.smDie.data(), sizeof(int) * m.smDie.size());
     });
 }
 

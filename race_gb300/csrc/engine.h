@@ -49,15 +49,27 @@ struct MpkPlan {
     DevBuf<int> sellCol;        // sellSlots column indices
     DevBuf<float> xf;           // (power+1)*n FP32 powers (reduced-precision storage)
     DevBuf<int> depRange;       // numChunks*6: chunks read in the previous/own/next group
-    DevBuf<int> itemChunk;      // numItems: chunk of each work item, wavefront order
-    DevBuf<unsigned char> itemPow;  // numItems: power (0-based) of each work item
+    int numRuns = 0;            // runs of the persistent kernel (mpk_order.h)
+    DevBuf<int4> runHead;       // numRuns: first chunk, end chunk, power, flags
+    DevBuf<int4> runDep;        // 2 per run: four chunk intervals read at the previous power
+    DevBuf<longlong2> runSpan;  // numRuns: SELL slots [lo, hi) of the run's chunks
+    int numDies = 1;            // run queues, one per L2 die (dies.h): die d's are dieStart[d] .. dieStart[d+1]-1
+    int dieStart[3] = {0, 0, 0};
+    const int *smDie = nullptr; // device table: die of every SM
+    int hints = 1;              // L2 eviction hints on the matrix loads
+    int prefetch = 0;           // runs ahead whose matrix block kMpk prefetches into L2 (0: off)
+    int unroll = 4;             // row-loop unroll of kMpk (4 or 8)
+    int loads = 1;              // kMpk matrix loads: 0 plain, 1 with an L2 policy, 2 non-coherent without L1
+    int ctasPerSm = 0;          // kMpk blocks per SM (0: as many as fit)
     DevBuf<int> done;           // power * numChunks completion flags
-    DevBuf<int> ticket;         // 1: next work item
+    DevBuf<int> ticket;         // next run of each die queue
     DevBuf<int> status;         // 1: device status word
     // Triangular partitions (mtxType L/U): a row may read any earlier group,
     // so the items run as one launch per wavefront step, without waits;
     // items stepPtr[s] .. stepPtr[s+1]) form step s.
     bool stepped = false;
+    DevBuf<int> itemChunk;      // numItems: chunk of each work item, step order
+    DevBuf<unsigned char> itemPow;  // numItems: power (0-based) of each work item
     std::vector<int> stepPtr;
 };
 
@@ -177,8 +189,23 @@ class Engine {
     DevPhases dPhases[2];
 
     // power results
-    int mpkStride = 2;  // issue order of the MPK wavefront (1: RACE's, 2: GPU default)
-    int mpkSplit = 0;   // powers per wavefront segment of the MPK issue order (0: all powers at once)
+    // MPK issue order and kernel (mpk_order.h, mpk.cu): order 0 the
+    // chunk-level wavefront, 1 the level-group order with stride mpkStride
+    // (1: RACE's, 2); powers per segment (0: all powers in one sweep);
+    // chunks per run; lag in chunks; one queue per L2 die; L2 prefetch
+    // distance in runs; eviction hints; row unroll; matrix load flavour;
+    // blocks per SM (0: as many as fit)
+    int mpkOrder = 0;
+    int mpkStride = 2;
+    int mpkSplit = 0;
+    int mpkRun = 2;
+    int mpkLag = 0;
+    bool mpkDieQueues = true;
+    int mpkPrefetch = 0;
+    int mpkHints = 1;
+    int mpkUnroll = 4;
+    int mpkLoads = 1;
+    int mpkCtasPerSm = 0;
     // Ranges shorter than this are traversed on the host (RACE_GPU_HOST_TRAVERSE_BELOW,
     // 0: never); the device permutation is then refreshed before the next
     // GPU traversal and at the end of the coloring.

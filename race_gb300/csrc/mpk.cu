@@ -41,7 +41,9 @@
 
 #include <cuda_bf16.h>
 
+#include "dies.h"
 #include "engine.h"
+#include "mpk_order.h"
 
 namespace race {
 
@@ -55,6 +57,94 @@ __device__ __forceinline__ int ldAcquire(const int *p) {
     int v;
     asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
+}
+__device__ __forceinline__ int ldRelaxed(const int *p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned smIndex() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+    return r;
+}
+
+// L2 eviction priorities (createpolicy): kind 1 evict_last, 2 evict_first,
+// otherwise evict_normal.
+__device__ __forceinline__ unsigned long long l2Policy(int kind) {
+    unsigned long long p;
+    if (kind == 1)
+        asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    else if (kind == 2)
+        asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    else
+        asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// Matrix loads of the wavefront kernel with an L2 policy. LD 1: through L1
+// as plain loads are; LD 2: the matrix is read-only while a kernel runs and
+// each entry is read once per item, so the loads take the non-coherent path
+// without allocating in L1 (which keeps the gathered x).
+template <int LD>
+__device__ __forceinline__ double ldMat(const double *a, unsigned long long pol) {
+    double v;
+    if constexpr (LD == 2)
+        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+    else
+        asm("ld.global.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+    return v;
+}
+template <int LD>
+__device__ __forceinline__ float ldMat(const float *a, unsigned long long pol) {
+    float v;
+    if constexpr (LD == 2)
+        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+    else
+        asm("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+    return v;
+}
+template <int LD>
+__device__ __forceinline__ __nv_bfloat16 ldMat(const __nv_bfloat16 *a, unsigned long long pol) {
+    unsigned short v;
+    if constexpr (LD == 2)
+        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(a), "l"(pol));
+    else
+        asm("ld.global.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(a), "l"(pol));
+    return __ushort_as_bfloat16(v);
+}
+template <int LD>
+__device__ __forceinline__ int ldMat(const int *a, unsigned long long pol) {
+    int v;
+    if constexpr (LD == 2)
+        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    else
+        asm("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
+}
+
+// Matrix entry loads: LD 0 plain loads, 1 and 2 with an L2 policy (ldMat).
+template <int LD, typename T>
+__device__ __forceinline__ T ldEntry(const T *a, unsigned long long pol) {
+    if constexpr (LD > 0)
+        return ldMat<LD>(a, pol);
+    else
+        return *a;
+}
+
+// Asynchronous copy of [p, p+bytes) from HBM into L2 (bulk prefetch; p and
+// bytes multiples of 16). Piece index j in 0..15 takes the 32 KB piece j
+// (blocks above 512 KB are prefetched in part).
+__device__ __forceinline__ void prefetchBlockL2(const unsigned char *p, long long bytes, int piece,
+                                                unsigned long long pol) {
+    constexpr long long kPiece = 32 * 1024;
+    const long long o = (long long)piece * kPiece;
+    if (piece >= 0 && piece < 16 && o < bytes) {
+        const unsigned b = (unsigned)(bytes - o < kPiece ? bytes - o : kPiece);
+        asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;" ::"l"(p + o), "r"(b), "l"(pol)
+                     : "memory");
+    }
 }
 
 template <typename VT>
@@ -97,21 +187,66 @@ struct SellView {
     const int *hubCol;
 };
 
-// One row of a SELL-32 chunk, FP64 storage: lane-owned fma chain.
+// One row of a SELL-32 chunk, FP64 storage: lane-owned fma chain. U = 8
+// issues the row in batches: eight column and value loads, then the eight
+// gathers of x, then the eight fused multiply-adds in entry order (the same
+// sequential chain, more loads in flight per warp).
+template <int U, int LD>
 __device__ __forceinline__ double sellRowD(const double *__restrict__ val, const int *__restrict__ col, long long off,
-                                           int len, const double *x) {
+                                           int len, const double *x, unsigned long long pol) {
     double t = 0.0;
+    if constexpr (U == 8) {
+        for (int j = 0; j < len; j += 8) {
+            int cc[8];
+            double vv[8], xx[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (j + i < len) {
+                    cc[i] = ldEntry<LD>(col + off + 32LL * (j + i), pol);
+                    vv[i] = ldEntry<LD>(val + off + 32LL * (j + i), pol);
+                }
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (j + i < len) xx[i] = x[cc[i]];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (j + i < len) t = fma(vv[i], xx[i], t);
+        }
+    } else {
 #pragma unroll 4
-    for (int j = 0; j < len; ++j) t = fma(val[off + 32LL * j], x[col[off + 32LL * j]], t);
+        for (int j = 0; j < len; ++j)
+            t = fma(ldEntry<LD>(val + off + 32LL * j, pol), x[ldEntry<LD>(col + off + 32LL * j, pol)], t);
+    }
     return t;
 }
 // FP32/BF16 storage with an FP32 vector.
-template <typename VT>
+template <typename VT, int U, int LD>
 __device__ __forceinline__ float sellRowF(const VT *__restrict__ val, const int *__restrict__ col, long long off,
-                                          int len, const float *x) {
+                                          int len, const float *x, unsigned long long pol) {
     float t = 0.0f;
+    if constexpr (U == 8) {
+        for (int j = 0; j < len; j += 8) {
+            int cc[8];
+            float vv[8], xx[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (j + i < len) {
+                    cc[i] = ldEntry<LD>(col + off + 32LL * (j + i), pol);
+                    vv[i] = toF<VT>(ldEntry<LD>(val + off + 32LL * (j + i), pol));
+                }
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (j + i < len) xx[i] = x[cc[i]];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (j + i < len) t = fmaf(vv[i], xx[i], t);
+        }
+    } else {
 #pragma unroll 4
-    for (int j = 0; j < len; ++j) t = fmaf(toF<VT>(val[off + 32LL * j]), x[col[off + 32LL * j]], t);
+        for (int j = 0; j < len; ++j)
+            t = fmaf(toF<VT>(ldEntry<LD>(val + off + 32LL * j, pol)), x[ldEntry<LD>(col + off + 32LL * j, pol)],
+                     t);
+    }
     return t;
 }
 
@@ -140,8 +275,9 @@ __device__ __forceinline__ AT hubSum(const SellView &m, int h, const AT *x) {
 // the chunk's hub rows one at a time with the whole warp. Called by all 32
 // lanes of a warp. HUBS = false compiles the plain SELL row only (plans
 // without hub rows keep the register count, hence the occupancy, of that).
-template <typename VT, bool HUBS>
-__device__ __forceinline__ void chunkRow(const SellView &m, int c, int k, int n, double *x, float *xf) {
+template <typename VT, bool HUBS, int U = 4, int LD = 0>
+__device__ __forceinline__ void chunkRow(const SellView &m, int c, int k, int n, double *x, float *xf,
+                                         unsigned long long pol) {
     const int lane = threadIdx.x & 31;
     const int r = m.chunkRow[c] + lane;
     if (r < m.chunkRow[c + 1]) {
@@ -149,9 +285,10 @@ __device__ __forceinline__ void chunkRow(const SellView &m, int c, int k, int n,
         const long long off = m.chunkOff[c] + lane;
         if (len >= 0) {
             if constexpr (sizeof(VT) == 8) {
-                x[(size_t)(k + 1) * n + r] = sellRowD((const double *)m.val, m.col, off, len, x + (size_t)k * n);
+                x[(size_t)(k + 1) * n + r] =
+                    sellRowD<U, LD>((const double *)m.val, m.col, off, len, x + (size_t)k * n, pol);
             } else {
-                const float v = sellRowF<VT>((const VT *)m.val, m.col, off, len, xf + (size_t)k * n);
+                const float v = sellRowF<VT, U, LD>((const VT *)m.val, m.col, off, len, xf + (size_t)k * n, pol);
                 xf[(size_t)(k + 1) * n + r] = v;
                 x[(size_t)(k + 1) * n + r] = floatToDoubleExact(v);
             }
@@ -178,40 +315,93 @@ struct MpkArgs {
     double *x;      // caller's (p+1)*n powers
     float *xf;      // internal FP32 powers (reduced-precision storage only)
     int n;
-    const int *depRange;  // numChunks*6: [lo,hi] chunks read in the previous, own and next group
-    const int *itemChunk;
-    const unsigned char *itemPow;
-    int numItems, numChunks;
-    int *done;            // power * numChunks completion flags
-    int *ticket;
+    const int4 *runHead;       // numRuns: first chunk, end chunk, power k, flags (bit 0: last power of the segment)
+    const int4 *runDep;        // 2 per run: four chunk intervals [lo,hi] read at power k-1
+    const longlong2 *runSpan;  // numRuns: SELL slots [lo, hi) of the run's chunks
+    int numChunks;
+    int *done;                 // power * numChunks completion flags
+    int *ticket;               // one per die queue
     int *status;
+    int hints;                 // L2 eviction hints on the matrix
+    int prefetch;              // runs ahead (in the warp's queue) whose matrix block is prefetched into L2; 0: none
+    int valBytes;              // bytes per stored value
+    const int *smDie;          // die of every SM (numDies > 1)
+    int numDies;
+    int dieStart[3];           // die d's queue: runs dieStart[d] .. dieStart[d+1]-1
 };
 
-// Persistent warps: one (power, chunk) item per ticket. Taking several
-// items at once or requesting the next ticket early measured slower: an
-// item held but not started delays every item that depends on it.
-template <typename VT, bool HUBS>
+// Persistent warps: one run (up to 32 consecutive chunks at one power) per
+// ticket. A run waits until every chunk in its intervals is complete at the
+// previous power; those chunks belong to runs earlier in the global order,
+// taken by running warps, so the wait always ends (bounded anyway: a
+// timeout goes to the status word). The polls are relaxed loads and one
+// acquire fence follows the successful poll (a flag read by a relaxed load
+// and a later fence.acq_rel form an acquire of the writer's release).
+// A warp takes the runs of its own die's queue, so each chunk's matrix
+// block is cached by one die's L2 only; an empty queue sends it to the
+// other one. With its ticket the warp prefetches into L2 the matrix block
+// of the run `prefetch` places further down its queue (taken about one
+// round of the die's warps later), and it releases its previous run's flags
+// only after fetching the next run, when the stores they publish have
+// drained; the release still comes before any wait, so a warp never waits
+// on itself.
+template <typename VT, bool HUBS, int U, int LD>
 __global__ void __launch_bounds__(kWarpThreads) kMpk(MpkArgs a) {
     const int lane = threadIdx.x & 31;
+    const unsigned long long polKeep = l2Policy(a.hints ? 1 : 0), polDrop = l2Policy(a.hints ? 2 : 0);
+    const int myDie = a.numDies > 1 ? a.smDie[smIndex()] : 0;
+    int q = myDie;
+    int pc0 = 0, pc1 = 0, pk = 0;  // run whose flags are still to be released
     for (;;) {
         int it = 0;
-        if (lane == 0) it = atomicAdd(a.ticket, 1);
+        if (lane == 0) it = atomicAdd(a.ticket + q, 1);
         it = __shfl_sync(0xffffffffu, it, 0);
-        if (it >= a.numItems) return;
-        const int c = a.itemChunk[it];
-        const int k = a.itemPow[it];  // computes x_{k+1} from x_k
+        const int qStart = q == 0 ? a.dieStart[0] : a.dieStart[1];
+        const int qCount = q == 0 ? a.dieStart[1] - a.dieStart[0] : a.dieStart[2] - a.dieStart[1];
+        const bool have = it < qCount;
+        int4 h = make_int4(0, 0, 0, 0), d0 = h, d1 = h;
+        if (have) {
+            h = a.runHead[qStart + it];
+            d0 = a.runDep[2 * (qStart + it)];
+            d1 = a.runDep[2 * (qStart + it) + 1];
+            if (a.prefetch > 0 && it + a.prefetch < qCount) {
+                const longlong2 sp = a.runSpan[qStart + it + a.prefetch];
+                const long long slots = sp.y - sp.x;
+                // lanes 0-15: value block, lanes 16-31: column block
+                if (slots > 0) {
+                    if (lane < 16)
+                        prefetchBlockL2((const unsigned char *)a.m.val + sp.x * a.valBytes, slots * a.valBytes,
+                                        lane, polKeep);
+                    else
+                        prefetchBlockL2((const unsigned char *)a.m.col + sp.x * 4, slots * 4, lane - 16, polKeep);
+                }
+            }
+        }
+        // release the previous run; __syncwarp orders all lanes' stores
+        // before the release stores
+        __syncwarp();
+        if (lane < pc1 - pc0)
+            asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(a.done + (size_t)pk * a.numChunks + pc0 + lane),
+                         "r"(1)
+                         : "memory");
+        pc0 = pc1 = 0;
+        if (!have) {
+            if (a.numDies > 1 && q == myDie) {
+                q = 1 - myDie;
+                continue;
+            }
+            return;
+        }
+        const int k = h.z;  // computes x_{k+1} from x_k
         if (k > 0) {
-            // every chunk holding a column of this chunk must be complete at
-            // power k-1: up to three chunk ranges, one per neighbouring group
-            const int *rg = a.depRange + 6 * c;
             const int *done = a.done + (size_t)(k - 1) * a.numChunks;
             long long spins = 0;
             for (;;) {
                 bool ok = true;
-#pragma unroll
-                for (int d = 0; d < 3; ++d)
-                    for (int i = rg[2 * d] + lane; i <= rg[2 * d + 1]; i += 32)
-                        if (ldAcquire(done + i) == 0) ok = false;
+                for (int i = d0.x + lane; i <= d0.y; i += 32) ok &= ldRelaxed(done + i) != 0;
+                for (int i = d0.z + lane; i <= d0.w; i += 32) ok &= ldRelaxed(done + i) != 0;
+                for (int i = d1.x + lane; i <= d1.y; i += 32) ok &= ldRelaxed(done + i) != 0;
+                for (int i = d1.z + lane; i <= d1.w; i += 32) ok &= ldRelaxed(done + i) != 0;
                 if (__all_sync(0xffffffffu, ok)) break;
                 if (++spins > kSpinLimit || ldAcquire(a.status) != DEV_OK) {
                     if (lane == 0) atomicCAS(a.status, DEV_OK, DEV_WAIT_TIMEOUT);
@@ -219,13 +409,13 @@ __global__ void __launch_bounds__(kWarpThreads) kMpk(MpkArgs a) {
                 }
                 __nanosleep(32);
             }
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
         }
-        chunkRow<VT, HUBS>(a.m, c, k, a.n, a.x, a.xf);
-        // __syncwarp orders the lanes' stores before lane 0's release store
-        __syncwarp();
-        if (lane == 0)
-            asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(a.done + (size_t)k * a.numChunks + c), "r"(1)
-                         : "memory");
+        const unsigned long long pol = (h.w & 1) ? polDrop : polKeep;
+        for (int c = h.x; c < h.y; ++c) chunkRow<VT, HUBS, U, LD>(a.m, c, k, a.n, a.x, a.xf, pol);
+        pc0 = h.x;
+        pc1 = h.y;
+        pk = k;
     }
 }
 
@@ -235,7 +425,7 @@ __global__ void __launch_bounds__(kWarpThreads) kSpmvSell(SellView m, int numChu
                                                           float *xf) {
     const int nw = gridDim.x * (blockDim.x >> 5);
     for (int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < numChunks; c += nw)
-        chunkRow<VT, HUBS>(m, c, k, n, x, xf);
+        chunkRow<VT, HUBS>(m, c, k, n, x, xf, 0);
 }
 
 // One wavefront step of a triangular partition: one warp per (chunk,
@@ -247,7 +437,7 @@ __global__ void __launch_bounds__(kWarpThreads) kMpkStep(SellView m, const int *
                                                          double *x, float *xf) {
     const int nw = gridDim.x * (blockDim.x >> 5);
     for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < count; i += nw)
-        chunkRow<VT, HUBS>(m, itemChunk[i], itemPow[i], n, x, xf);
+        chunkRow<VT, HUBS>(m, itemChunk[i], itemPow[i], n, x, xf, 0);
 }
 
 // x0 -> FP32 copy (rounding to nearest) for the reduced-precision path.
@@ -459,50 +649,10 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
     }
     RACE_CUDA(cudaGetLastError());
-    // Issue order. RACE's wavefront (functionManager.cpp:638-647) visits
-    // step s, power k, group s-k (stride 1): power k of group g then needs
-    // power k-1 of group g+1 from the same step, one group earlier in the
-    // order, and thousands of in-flight items would queue behind that chain.
-    // With stride 2 (step s holds power k of group s-2k) every dependency
-    // sits in an earlier step, so the items in flight are independent; each
-    // group stays in use for 2p-1 steps instead of p. Both orders compute the
-    // same rows at the same powers; results are bit-identical.
-    // A triangular partition (mtxType L/U) runs step by step: stride 2 puts
-    // every earlier group's previous power in an earlier step.
     plan->stepped = e.powerLevelsType == "L" || e.powerLevelsType == "U";
-    const int stride = e.mpkStride == 1 && !plan->stepped ? 1 : 2;
-    std::vector<int> groupFirst(G + 1, C);
-    for (int t = C - 1; t >= 0; --t) groupFirst[chunkGroup[t]] = t;
-    for (int g = G - 1; g >= 0; --g) groupFirst[g] = std::min(groupFirst[g], groupFirst[g + 1]);
-    std::vector<int> itemChunk;
-    std::vector<unsigned char> itemPow;
-    itemChunk.reserve((size_t)C * power);
-    // With a split of s powers, the wavefront runs over powers 1..s, then
-    // s+1..2s, ... in one launch (each segment's items follow all items of
-    // the powers before it, so the order stays a valid wavefront): fewer
-    // groups in flight at the cost of reading the matrix once per segment.
-    const int split = e.mpkSplit > 0 && e.mpkSplit < power && !plan->stepped ? e.mpkSplit : power;
-    plan->stepPtr.assign(1, 0);
-    for (int k0 = 0; k0 < power; k0 += split) {
-        const int kn = std::min(power, k0 + split) - k0;
-        for (int st = 0; st < G + stride * (kn - 1); ++st) {
-            for (int k = 0; k < kn; ++k) {
-                int g = st - stride * k;
-                if (g < 0 || g >= G) continue;
-                for (int t = groupFirst[g]; t < groupFirst[g + 1]; ++t) {
-                    itemChunk.push_back(t);
-                    itemPow.push_back((unsigned char)(k0 + k));
-                }
-            }
-            plan->stepPtr.push_back((int)itemChunk.size());
-        }
-    }
-    plan->numItems = (int)itemChunk.size();
-    plan->itemChunk.upload(itemChunk.data(), std::max<size_t>(itemChunk.size(), 1), s);
-    plan->itemPow.upload(itemPow.data(), std::max<size_t>(itemPow.size(), 1), s);
     plan->depRange.alloc((size_t)std::max(C, 1) * 6);
     plan->done.alloc((size_t)std::max(C, 1) * power);
-    plan->ticket.alloc(1);
+    plan->ticket.alloc(2);
     plan->status.alloc(1);
     DevBuf<int> dChunkGroup, dBad(1);
     dChunkGroup.upload(chunkGroup.data(), std::max<size_t>(chunkGroup.size(), 1), s);
@@ -512,7 +662,11 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
                                        dBad.p, plan->stepped ? 1 : 0);
     RACE_CUDA(cudaGetLastError());
     int bad = 0;
+    std::vector<int> depRange((size_t)C * 6);
     RACE_CUDA(cudaMemcpyAsync(&bad, dBad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (C > 0)
+        RACE_CUDA(cudaMemcpyAsync(depRange.data(), plan->depRange.p, sizeof(int) * depRange.size(),
+                                  cudaMemcpyDeviceToHost, s));
     RACE_CUDA(cudaStreamSynchronize(s));
     // Every dependency must come earlier in the wavefront order: the columns
     // of group g lie in groups g-1..g+1 (BFS levels couple neighbours only;
@@ -522,6 +676,74 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     if (bad)
         throw Error(RACE_ERR_INVALID_ARG,
                     "MPK operand is not in the engine's level order (permute it with getPerm/getInvPerm)");
+    if (plan->stepped) {
+        // A triangular partition (mtxType L/U) lets a row read any earlier
+        // group, which the chunk intervals do not describe; it runs step by
+        // step in RACE's group order with stride 2 (step s holds power k of
+        // group s-2k), so every earlier group's previous power lies in an
+        // earlier step.
+        std::vector<int> groupFirst(G + 1, C);
+        for (int t = C - 1; t >= 0; --t) groupFirst[chunkGroup[t]] = t;
+        for (int g = G - 1; g >= 0; --g) groupFirst[g] = std::min(groupFirst[g], groupFirst[g + 1]);
+        std::vector<int> itemChunk;
+        std::vector<unsigned char> itemPow;
+        plan->stepPtr.assign(1, 0);
+        for (int st = 0; st < G + 2 * (power - 1); ++st) {
+            for (int k = 0; k < power; ++k) {
+                const int g = st - 2 * k;
+                if (g < 0 || g >= G) continue;
+                for (int t = groupFirst[g]; t < groupFirst[g + 1]; ++t) {
+                    itemChunk.push_back(t);
+                    itemPow.push_back((unsigned char)k);
+                }
+            }
+            plan->stepPtr.push_back((int)itemChunk.size());
+        }
+        plan->numItems = (int)itemChunk.size();
+        plan->itemChunk.upload(itemChunk.data(), std::max<size_t>(itemChunk.size(), 1), s);
+        plan->itemPow.upload(itemPow.data(), std::max<size_t>(itemPow.size(), 1), s);
+        RACE_CUDA(cudaStreamSynchronize(s));
+        return plan;
+    }
+    // Issue order of the persistent kernel (mpk_order.cpp): by default the
+    // chunk-level wavefront, every (chunk, power) item as early as the
+    // chunks it reads and the work in flight allow, in runs of consecutive
+    // chunks per ticket and one queue per L2 die; RACE's level-group order
+    // on request. All orders compute the same rows at the same powers:
+    // results are bit-identical.
+    const int segLen = e.mpkSplit > 0 && e.mpkSplit < power ? e.mpkSplit : power;
+    const DieMap &dies = dieMap();
+    const bool twoDies = dies.numDies == 2 && e.mpkOrder == 0 && e.mpkDieQueues;
+    const std::vector<int> chunkDie =
+        twoDies ? chunkDies(C, dies.smsPerDie[0], dies.smsPerDie[1]) : std::vector<int>();
+    const MpkOrder order = e.mpkOrder == 1
+                               ? mpkGroupOrder(depRange, chunkGroup, G, power, e.mpkStride == 1 ? 1 : 2, segLen)
+                               : mpkRunOrder(depRange, C, power, segLen, e.mpkRun, e.mpkLag, chunkDie);
+    plan->numItems = (int)((size_t)C * power);
+    plan->numRuns = order.numRuns();
+    plan->numDies = twoDies ? 2 : 1;
+    for (int d = 0; d < 3; ++d) plan->dieStart[d] = order.dieStart[d];
+    plan->smDie = dies.smDieDev.p;
+    std::vector<long long> span(2 * (size_t)std::max(plan->numRuns, 1), 0);
+    for (int r = 0; r < plan->numRuns; ++r) {
+        const int c0 = order.head[4 * (size_t)r], c1 = order.head[4 * (size_t)r + 1];
+        span[2 * (size_t)r] = chunkOff[c0];
+        span[2 * (size_t)r + 1] = c1 < C ? chunkOff[c1] : off;
+    }
+    std::vector<int> head(order.head), dep(order.dep);
+    if (plan->numRuns == 0) {
+        head.assign(4, 0);
+        dep.assign(8, 0);
+    }
+    plan->runHead.upload((const int4 *)head.data(), head.size() / 4, s);
+    plan->runDep.upload((const int4 *)dep.data(), dep.size() / 4, s);
+    plan->runSpan.upload((const longlong2 *)span.data(), span.size() / 2, s);
+    plan->hints = e.mpkHints;
+    plan->prefetch = e.mpkPrefetch;
+    plan->unroll = e.mpkUnroll;
+    plan->loads = e.mpkLoads;
+    plan->ctasPerSm = e.mpkCtasPerSm;
+    RACE_CUDA(cudaStreamSynchronize(s));
     return plan;
 }
 
@@ -552,14 +774,36 @@ SellView viewOf(const MpkPlan &p) {
                     p.hubChunkStart.p, p.hubRow.p, p.hubPtr.p, p.hubVal.p, p.hubCol.p};
 }
 
+template <typename VT, bool HUBS, int U, int LD>
+void launchMpkU(const MpkArgs &a, int ctasPerSm, cudaStream_t s) {
+    static int resident = residentBlocks(kMpk<VT, HUBS, U, LD>, kWarpThreads);
+    const int blocks = ctasPerSm > 0 ? std::min(resident, devSms() * ctasPerSm) : resident;
+    kMpk<VT, HUBS, U, LD><<<blocks, kWarpThreads, 0, s>>>(a);
+}
+
+template <typename VT, bool HUBS, int U>
+void launchMpkLd(const MpkArgs &a, int ld, int ctasPerSm, cudaStream_t s) {
+    if (ld == 0)
+        launchMpkU<VT, HUBS, U, 0>(a, ctasPerSm, s);
+    else if (ld == 1)
+        launchMpkU<VT, HUBS, U, 1>(a, ctasPerSm, s);
+    else
+        launchMpkU<VT, HUBS, U, 2>(a, ctasPerSm, s);
+}
+
 template <typename VT>
-void launchMpk(const MpkArgs &a, bool hubs, cudaStream_t s) {
+void launchMpk(const MpkArgs &a, const MpkPlan &p, cudaStream_t s) {
+    const bool hubs = p.numHubs > 0;
     if (hubs) {
-        static int blocks = residentBlocks(kMpk<VT, true>, kWarpThreads);
-        kMpk<VT, true><<<blocks, kWarpThreads, 0, s>>>(a);
+        if (p.unroll == 8)
+            launchMpkLd<VT, true, 8>(a, p.loads, p.ctasPerSm, s);
+        else
+            launchMpkLd<VT, true, 4>(a, p.loads, p.ctasPerSm, s);
     } else {
-        static int blocks = residentBlocks(kMpk<VT, false>, kWarpThreads);
-        kMpk<VT, false><<<blocks, kWarpThreads, 0, s>>>(a);
+        if (p.unroll == 8)
+            launchMpkLd<VT, false, 8>(a, p.loads, p.ctasPerSm, s);
+        else
+            launchMpkLd<VT, false, 4>(a, p.loads, p.ctasPerSm, s);
     }
 }
 
@@ -596,7 +840,7 @@ void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
     if (power != plan.power) throw Error(RACE_ERR_INVALID_ARG, "power differs from the planned power");
     cudaStream_t s = e.stream;
     RACE_CUDA(cudaMemsetAsync(plan.done.p, 0, sizeof(int) * (size_t)plan.numChunks * plan.power, s));
-    RACE_CUDA(cudaMemsetAsync(plan.ticket.p, 0, sizeof(int), s));
+    RACE_CUDA(cudaMemsetAsync(plan.ticket.p, 0, sizeof(int) * 2, s));
     RACE_CUDA(cudaMemsetAsync(plan.status.p, 0, sizeof(int), s));
     if (plan.valType != RACE_VAL_F64) kToFloat<<<ceilDiv(ops.n, 256), 256, 0, s>>>((const double *)ops.x, plan.xf.p, ops.n);
     if (plan.stepped) {
@@ -609,12 +853,14 @@ void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
         RACE_CUDA(cudaGetLastError());
         return;
     }
-    MpkArgs a{viewOf(plan), (double *)ops.x, plan.xf.p, ops.n, plan.depRange.p, plan.itemChunk.p, plan.itemPow.p,
-              plan.numItems, plan.numChunks, plan.done.p, plan.ticket.p, plan.status.p};
+    MpkArgs a{viewOf(plan), (double *)ops.x, plan.xf.p, ops.n, plan.runHead.p, plan.runDep.p, plan.runSpan.p,
+              plan.numChunks, plan.done.p, plan.ticket.p, plan.status.p, plan.hints, plan.prefetch,
+              (int)valBytes(plan.valType), plan.smDie, plan.numDies,
+              {plan.dieStart[0], plan.dieStart[1], plan.dieStart[2]}};
     switch (plan.valType) {
-    case RACE_VAL_F64: launchMpk<double>(a, plan.numHubs > 0, s); break;
-    case RACE_VAL_F32: launchMpk<float>(a, plan.numHubs > 0, s); break;
-    case RACE_VAL_BF16: launchMpk<__nv_bfloat16>(a, plan.numHubs > 0, s); break;
+    case RACE_VAL_F64: launchMpk<double>(a, plan, s); break;
+    case RACE_VAL_F32: launchMpk<float>(a, plan, s); break;
+    case RACE_VAL_BF16: launchMpk<__nv_bfloat16>(a, plan, s); break;
     default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
     }
     RACE_CUDA(cudaGetLastError());

@@ -22,6 +22,7 @@
 #include <numeric>
 
 #include "engine.h"
+#include "mpk_order.h"
 
 namespace race {
 namespace {
@@ -281,6 +282,15 @@ Engine::Engine(int nrow, int nthreads, int dist_, const int *rowPtr, const int *
     dStatus.alloc(4);
     if (const char *st = getenv("RACE_GPU_MPK_STRIDE")) mpkStride = atoi(st) == 1 ? 1 : 2;
     if (const char *sp = getenv("RACE_GPU_MPK_SPLIT")) mpkSplit = std::max(0, atoi(sp));
+    if (const char *o = getenv("RACE_GPU_MPK_ORDER")) mpkOrder = std::string(o) == "group" ? 1 : 0;
+    if (const char *r = getenv("RACE_GPU_MPK_RUN")) mpkRun = std::min(std::max(1, atoi(r)), kMpkMaxRunLen);
+    if (const char *l = getenv("RACE_GPU_MPK_LAG")) mpkLag = std::max(0, atoi(l));
+    if (const char *d = getenv("RACE_GPU_MPK_DIES")) mpkDieQueues = atoi(d) != 1;
+    if (const char *pf = getenv("RACE_GPU_MPK_PREFETCH")) mpkPrefetch = std::max(0, atoi(pf));
+    if (const char *h = getenv("RACE_GPU_MPK_HINTS")) mpkHints = atoi(h) ? 1 : 0;
+    if (const char *u = getenv("RACE_GPU_MPK_UNROLL")) mpkUnroll = atoi(u) == 8 ? 8 : 4;
+    if (const char *ld = getenv("RACE_GPU_MPK_LOADS")) mpkLoads = std::min(std::max(0, atoi(ld)), 2);
+    if (const char *b = getenv("RACE_GPU_MPK_CTAS")) mpkCtasPerSm = std::max(0, atoi(b));
     if (const char *ht = getenv("RACE_GPU_HOST_TRAVERSE_BELOW")) hostTraverseBelow = std::max(0, atoi(ht));
     if (const char *sm = getenv("RACE_GPU_SWEEP_MODE")) {
         std::string m(sm);
