@@ -920,7 +920,6 @@ void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
     if (power != plan.power) throw Error(RACE_ERR_INVALID_ARG, "power differs from the planned power");
     cudaStream_t s = e.stream;
     RACE_CUDA(cudaMemsetAsync(plan.done.p, 0, sizeof(int) * (size_t)plan.numChunks * plan.power, s));
-    RACE_CUDA(cudaMemsetAsync(plan.counters.p, 0, sizeof(int) * (plan.numQueues + 2), s));
     RACE_CUDA(cudaMemsetAsync(plan.status.p, 0, sizeof(int), s));
     if (plan.valType != RACE_VAL_F64) kToFloat<<<ceilDiv(ops.n, 256), 256, 0, s>>>((const double *)ops.x, plan.xf.p, ops.n);
     if (plan.stepped) {
@@ -933,6 +932,7 @@ void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
         RACE_CUDA(cudaGetLastError());
         return;
     }
+    RACE_CUDA(cudaMemsetAsync(plan.counters.p, 0, sizeof(int) * (plan.numQueues + 2), s));
     // group 0's lead over the die's last group (in runs): the reach of the
     // dependencies over the groups in between plus every group's runs in
     // flight, with room to spare
