@@ -402,10 +402,7 @@ int race_wave_plan(int kernel, int n, const int *rowPtr, const int *col, const i
  * L2 die (0 or 1) whose SMs run each chunk, and the runs are grouped into one
  * queue per die. order 1: RACE's level-group order
  * (functionManager.cpp:618-823) with stride `stride`, one chunk per run,
- * chunkGroup giving each chunk's level group. order 2: power-group
- * queues, segLen (1..power) warp groups per die: queue d*segLen+j holds die
- * d's runs of powers j, j+segLen, ... in chunk order, and dieStart receives
- * the dies*segLen+1 queue bounds instead. Writes, when
+ * chunkGroup giving each chunk's level group. Writes, when
  * cap >= *numRuns, per run head[4] (first chunk, end chunk, power, flags),
  * dep[8] (four chunk intervals that must be complete at the previous
  * power) and rank (its position in the global order; may be NULL), and

@@ -731,7 +731,7 @@ int race_mpk_issue_order(const int *depRange, const int *chunkGroup, const int *
                          int order, int stride, int segLen, int runLen, int lag, int *head, int *dep, int *rank,
                          int *dieStart, int cap, int *numRuns) {
     if (numChunks < 0 || (numChunks > 0 && !depRange) || power < 1 || power > 255 || !numRuns || lag < 0 ||
-        (order == 1 && numChunks > 0 && !chunkGroup) || order < 0 || order > 2 || runLen < 1 ||
+        (order == 1 && numChunks > 0 && !chunkGroup) || (order != 0 && order != 1) || runLen < 1 ||
         runLen > race::kMpkMaxRunLen)
         return RACE_ERR_INVALID_ARG;
     int numGroups = 0;
@@ -750,22 +750,16 @@ int race_mpk_issue_order(const int *depRange, const int *chunkGroup, const int *
         const std::vector<int> dr(depRange, depRange + 6 * (size_t)numChunks);
         const std::vector<int> cd = chunkDie ? std::vector<int>(chunkDie, chunkDie + numChunks) : std::vector<int>();
         const race::MpkOrder o =
-            order == 1   ? race::mpkGroupOrder(dr, std::vector<int>(chunkGroup, chunkGroup + numChunks), numGroups,
-                                               power, stride == 1 ? 1 : 2, segLen)
-            : order == 2 ? race::mpkPowerQueues(dr, numChunks, power, segLen, runLen, cd)
-                         : race::mpkRunOrder(dr, numChunks, power, segLen, runLen, lag, cd);
+            order == 1 ? race::mpkGroupOrder(dr, std::vector<int>(chunkGroup, chunkGroup + numChunks), numGroups,
+                                             power, stride == 1 ? 1 : 2, segLen)
+                       : race::mpkRunOrder(dr, numChunks, power, segLen, runLen, lag, cd);
         *numRuns = o.numRuns();
         if (head && dep && cap >= o.numRuns()) {
             memcpy(head, o.head.data(), sizeof(int) * o.head.size());
             memcpy(dep, o.dep.data(), sizeof(int) * o.dep.size());
             if (rank) memcpy(rank, o.rank.data(), sizeof(int) * o.rank.size());
         }
-        if (dieStart) {
-            if (order == 2)
-                memcpy(dieStart, o.queueStart.data(), sizeof(int) * o.queueStart.size());
-            else
-                memcpy(dieStart, o.dieStart.data(), sizeof(int) * 3);
-        }
+        if (dieStart) memcpy(dieStart, o.dieStart.data(), sizeof(int) * 3);
     });
 }
 

@@ -52,22 +52,15 @@ struct MpkPlan {
     int numRuns = 0;            // runs of the persistent kernel (mpk_order.h)
     DevBuf<int4> runHead;       // numRuns: first chunk, end chunk, power, flags
     DevBuf<int4> runDep;        // 2 per run: four chunk intervals read at the previous power
-    DevBuf<longlong2> runSpan;  // numRuns: SELL slots [lo, hi) of the run's chunks
-    int numDies = 1;            // L2 dies the runs are split over (dies.h)
-    int groups = 1;             // warp groups per die (power-group queues, mpk_order.h)
-    int numQueues = 1;          // dies * groups
-    DevBuf<int> queueStart;     // numQueues+1 run offsets
-    DevBuf<int> counters;       // numQueues tickets, then one warp counter per die
-    int maxReach = 0;           // largest chunk distance from a chunk to the highest chunk it reads
-    int runLen = 1;             // chunks per run
-    int throttleScale = 100;    // percent of the computed group-0 throttle distance
+    int numDies = 1;            // run queues, one per L2 die (dies.h): die d's are dieStart[d] .. dieStart[d+1]-1
+    int dieStart[3] = {0, 0, 0};
     const int *smDie = nullptr; // device table: die of every SM
     int hints = 1;              // L2 eviction hints on the matrix loads
-    int prefetch = 0;           // runs ahead whose matrix block kMpk prefetches into L2 (0: off)
     int unroll = 4;             // row-loop unroll of kMpk (4 or 8)
     int loads = 1;              // kMpk matrix loads: 0 plain, 1 with an L2 policy, 2 non-coherent without L1
     int ctasPerSm = 0;          // kMpk blocks per SM (0: as many as fit)
     DevBuf<int> done;           // power * numChunks completion flags
+    DevBuf<int> ticket;         // next run of each die queue
     DevBuf<int> status;         // 1: device status word
     // Triangular partitions (mtxType L/U): a row may read any earlier group,
     // so the items run as one launch per wavefront step, without waits;
@@ -196,23 +189,20 @@ class Engine {
     // power results
     // MPK issue order and kernel (mpk_order.h, mpk.cu): order 0 the
     // chunk-level wavefront, 1 the level-group order with stride mpkStride
-    // (1: RACE's, 2), 2 power-group queues (mpkSplit groups); powers per
-    // segment (0: all powers in one sweep); throttle scale (percent);
-    // chunks per run; lag in chunks; one queue per L2 die; L2 prefetch
-    // distance in runs; eviction hints; row unroll; matrix load flavour;
-    // blocks per SM (0: as many as fit)
+    // (1: RACE's, 2); powers per segment (0: all powers in one sweep);
+    // chunks per run; lag in chunks; one queue per L2 die; eviction hints;
+    // row unroll; matrix load flavour; blocks per SM (0: as many as fit).
+    // The defaults are the fastest measured on the 128^3 27-point stencil.
     int mpkOrder = 0;
     int mpkStride = 2;
     int mpkSplit = 0;
     int mpkRun = 2;
-    int mpkLag = 0;
+    int mpkLag = 8192;
     bool mpkDieQueues = true;
-    int mpkPrefetch = 0;
     int mpkHints = 1;
     int mpkUnroll = 4;
     int mpkLoads = 1;
     int mpkCtasPerSm = 0;
-    int mpkThrottle = 100;
     // Ranges shorter than this are traversed on the host (RACE_GPU_HOST_TRAVERSE_BELOW,
     // 0: never); the device permutation is then refreshed before the next
     // GPU traversal and at the end of the coloring.

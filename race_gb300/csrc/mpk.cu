@@ -37,7 +37,6 @@
 // caller's FP64 x through an exact float->double bit conversion, so the FP32
 // path issues no FP64 instructions in its inner loop.
 #include <algorithm>
-#include <climits>
 #include <numeric>
 
 #include <cuda_bf16.h>
@@ -132,20 +131,6 @@ __device__ __forceinline__ T ldEntry(const T *a, unsigned long long pol) {
         return ldMat<LD>(a, pol);
     else
         return *a;
-}
-
-// Asynchronous copy of [p, p+bytes) from HBM into L2 (bulk prefetch; p and
-// bytes multiples of 16). Piece index j in 0..15 takes the 32 KB piece j
-// (blocks above 512 KB are prefetched in part).
-__device__ __forceinline__ void prefetchBlockL2(const unsigned char *p, long long bytes, int piece,
-                                                unsigned long long pol) {
-    constexpr long long kPiece = 32 * 1024;
-    const long long o = (long long)piece * kPiece;
-    if (piece >= 0 && piece < 16 && o < bytes) {
-        const unsigned b = (unsigned)(bytes - o < kPiece ? bytes - o : kPiece);
-        asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;" ::"l"(p + o), "r"(b), "l"(pol)
-                     : "memory");
-    }
 }
 
 template <typename VT>
@@ -318,141 +303,88 @@ struct MpkArgs {
     int n;
     const int4 *runHead;       // numRuns: first chunk, end chunk, power k, flags (bit 0: last power of the segment)
     const int4 *runDep;        // 2 per run: four chunk intervals [lo,hi] read at power k-1
-    const longlong2 *runSpan;  // numRuns: SELL slots [lo, hi) of the run's chunks
     int numChunks;
     int *done;                 // power * numChunks completion flags
-    const int *queueStart;     // numQueues+1: queue q is runs queueStart[q] .. queueStart[q+1]-1
-    int numQueues;             // dies * groups
-    int groups;                // warp groups per die (power-group queues); 1: one queue per die
-    int throttle;              // group 0 stays within this many runs of its die's last group
-    int *counters;             // numQueues tickets, then one warp counter per die
+    int *ticket;               // one per die queue
     int *status;
     int hints;                 // L2 eviction hints on the matrix
-    int prefetch;              // runs ahead (in the warp's queue) whose matrix block is prefetched into L2; 0: none
-    int valBytes;              // bytes per stored value
     const int *smDie;          // die of every SM (numDies > 1)
     int numDies;
+    int dieStart[3];           // die d's queue: runs dieStart[d] .. dieStart[d+1]-1
 };
 
 // Persistent warps: one run (up to 32 consecutive chunks at one power) per
 // ticket. A run waits until every chunk in its intervals is complete at the
-// previous power. The polls are relaxed loads and one acquire fence follows
-// the successful poll (a flag read by a relaxed load and a later
-// fence.acq_rel form an acquire of the writer's release).
-// Queues. A warp works on the queues of its own L2 die, so each chunk's
-// matrix block is cached by one die only. With groups > 1 the die's warps
-// are dealt to the groups, and group j's queue holds the die's runs of
-// powers j, j+groups, ... in chunk order; group 0, which has no waits at its
-// first power, stays within `throttle` runs of the die's last group so the
-// powers of a sweep keep close together. A warp whose queue is empty helps
-// with the die's other groups, then with the other die's.
-// No deadlock: a run waits only on the previous power, which its queue
-// order and the throttle (a bound on tickets taken, sized on the host from
-// the dependency reach and the warps in flight) keep ahead of it; every wait
-// is bounded anyway and reports a timeout through the status word.
-// Overlap: a warp releases its previous run's flags only after fetching the
-// next run, when the stores they publish have drained, but always before it
-// waits or holds back, so a warp never waits on itself. With `prefetch` it
-// also prefetches into L2 the matrix block of the run that many places
-// further down its queue.
+// previous power; those chunks belong to runs earlier in the global order,
+// taken by running warps, so the wait always ends (bounded anyway: a
+// timeout goes to the status word). The polls are relaxed loads and one
+// acquire fence follows the successful poll (a flag read by a relaxed load
+// and a later fence.acq_rel form an acquire of the writer's release).
+// A warp takes the runs of its own die's queue, so each chunk's matrix
+// block is cached by one die's L2 only; an empty queue sends it to the
+// other one. A warp releases its previous run's flags only after fetching
+// the next run, when the stores they publish have drained; the release
+// still comes before any wait, so a warp never waits on itself.
 template <typename VT, bool HUBS, int U, int LD>
 __global__ void __launch_bounds__(kWarpThreads) kMpk(MpkArgs a) {
     const int lane = threadIdx.x & 31;
     const unsigned long long polKeep = l2Policy(a.hints ? 1 : 0), polDrop = l2Policy(a.hints ? 2 : 0);
     const int myDie = a.numDies > 1 ? a.smDie[smIndex()] : 0;
-    int group = 0;
-    if (a.groups > 1) {
-        int idx = 0;
-        if (lane == 0) idx = atomicAdd(a.counters + a.numQueues + myDie, 1);
-        group = __shfl_sync(0xffffffffu, idx, 0) % a.groups;
-    }
+    int q = myDie;
     int pc0 = 0, pc1 = 0, pk = 0;  // run whose flags are still to be released
-    auto releasePending = [&]() {
-        // __syncwarp orders all lanes' stores before the release stores
+    for (;;) {
+        int it = 0;
+        if (lane == 0) it = atomicAdd(a.ticket + q, 1);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        const int qStart = q == 0 ? a.dieStart[0] : a.dieStart[1];
+        const int qCount = q == 0 ? a.dieStart[1] - a.dieStart[0] : a.dieStart[2] - a.dieStart[1];
+        const bool have = it < qCount;
+        int4 h = make_int4(0, 0, 0, 0), d0 = h, d1 = h;
+        if (have) {
+            h = a.runHead[qStart + it];
+            d0 = a.runDep[2 * (qStart + it)];
+            d1 = a.runDep[2 * (qStart + it) + 1];
+        }
+        // release the previous run; __syncwarp orders all lanes' stores
+        // before the release stores
         __syncwarp();
         if (lane < pc1 - pc0)
             asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(a.done + (size_t)pk * a.numChunks + pc0 + lane),
                          "r"(1)
                          : "memory");
         pc0 = pc1 = 0;
-    };
-    const int otherDie = a.numDies > 1 ? 1 - myDie : myDie;
-    const int visits = a.numDies > 1 ? a.numQueues : a.groups;
-    for (int t = 0; t < visits; ++t) {
-        const int die = t < a.groups ? myDie : otherDie;
-        const int g = (group + t) % a.groups;
-        const int q = die * a.groups + g;
-        const int qStart = a.queueStart[q], qCount = a.queueStart[q + 1] - qStart;
-        int *ticket = a.counters + q;
-        const bool throttled = t == 0 && g == 0 && a.groups > 1;
-        for (;;) {
-            if (throttled) {
-                const int qL = q + a.groups - 1;
-                const int countL = a.queueStart[qL + 1] - a.queueStart[qL];
-                long long spins = 0;
-                for (;;) {
-                    int mine = 0, last = 0;
-                    if (lane == 0) {
-                        mine = ldRelaxed(ticket);
-                        last = ldRelaxed(a.counters + qL);
-                    }
-                    mine = __shfl_sync(0xffffffffu, mine, 0);
-                    last = __shfl_sync(0xffffffffu, last, 0);
-                    if (last >= countL || mine >= qCount || mine - last <= a.throttle) break;
-                    releasePending();
-                    if (++spins > kSpinLimit || ldAcquire(a.status) != DEV_OK) {
-                        if (lane == 0) atomicCAS(a.status, DEV_OK, DEV_WAIT_TIMEOUT);
-                        return;
-                    }
-                    __nanosleep(64);
-                }
+        if (!have) {
+            if (a.numDies > 1 && q == myDie) {
+                q = 1 - myDie;
+                continue;
             }
-            int it = 0;
-            if (lane == 0) it = atomicAdd(ticket, 1);
-            it = __shfl_sync(0xffffffffu, it, 0);
-            if (it >= qCount) break;
-            const int r = qStart + it;
-            const int4 h = a.runHead[r], d0 = a.runDep[2 * r], d1 = a.runDep[2 * r + 1];
-            if (a.prefetch > 0 && it + a.prefetch < qCount) {
-                const longlong2 sp = a.runSpan[r + a.prefetch];
-                const long long slots = sp.y - sp.x;
-                // lanes 0-15: value block, lanes 16-31: column block
-                if (slots > 0) {
-                    if (lane < 16)
-                        prefetchBlockL2((const unsigned char *)a.m.val + sp.x * a.valBytes, slots * a.valBytes,
-                                        lane, polKeep);
-                    else
-                        prefetchBlockL2((const unsigned char *)a.m.col + sp.x * 4, slots * 4, lane - 16, polKeep);
-                }
-            }
-            releasePending();
-            const int k = h.z;  // computes x_{k+1} from x_k
-            if (k > 0) {
-                const int *done = a.done + (size_t)(k - 1) * a.numChunks;
-                long long spins = 0;
-                for (;;) {
-                    bool ok = true;
-                    for (int i = d0.x + lane; i <= d0.y; i += 32) ok &= ldRelaxed(done + i) != 0;
-                    for (int i = d0.z + lane; i <= d0.w; i += 32) ok &= ldRelaxed(done + i) != 0;
-                    for (int i = d1.x + lane; i <= d1.y; i += 32) ok &= ldRelaxed(done + i) != 0;
-                    for (int i = d1.z + lane; i <= d1.w; i += 32) ok &= ldRelaxed(done + i) != 0;
-                    if (__all_sync(0xffffffffu, ok)) break;
-                    if (++spins > kSpinLimit || ldAcquire(a.status) != DEV_OK) {
-                        if (lane == 0) atomicCAS(a.status, DEV_OK, DEV_WAIT_TIMEOUT);
-                        return;
-                    }
-                    __nanosleep(32);
-                }
-                asm volatile("fence.acq_rel.gpu;" ::: "memory");
-            }
-            const unsigned long long pol = (h.w & 1) ? polDrop : polKeep;
-            for (int c = h.x; c < h.y; ++c) chunkRow<VT, HUBS, U, LD>(a.m, c, k, a.n, a.x, a.xf, pol);
-            pc0 = h.x;
-            pc1 = h.y;
-            pk = k;
+            return;
         }
+        const int k = h.z;  // computes x_{k+1} from x_k
+        if (k > 0) {
+            const int *done = a.done + (size_t)(k - 1) * a.numChunks;
+            long long spins = 0;
+            for (;;) {
+                bool ok = true;
+                for (int i = d0.x + lane; i <= d0.y; i += 32) ok &= ldRelaxed(done + i) != 0;
+                for (int i = d0.z + lane; i <= d0.w; i += 32) ok &= ldRelaxed(done + i) != 0;
+                for (int i = d1.x + lane; i <= d1.y; i += 32) ok &= ldRelaxed(done + i) != 0;
+                for (int i = d1.z + lane; i <= d1.w; i += 32) ok &= ldRelaxed(done + i) != 0;
+                if (__all_sync(0xffffffffu, ok)) break;
+                if (++spins > kSpinLimit || ldAcquire(a.status) != DEV_OK) {
+                    if (lane == 0) atomicCAS(a.status, DEV_OK, DEV_WAIT_TIMEOUT);
+                    return;
+                }
+                __nanosleep(32);
+            }
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        }
+        const unsigned long long pol = (h.w & 1) ? polDrop : polKeep;
+        for (int c = h.x; c < h.y; ++c) chunkRow<VT, HUBS, U, LD>(a.m, c, k, a.n, a.x, a.xf, pol);
+        pc0 = h.x;
+        pc1 = h.y;
+        pk = k;
     }
-    releasePending();
 }
 
 // Plain y = A x on the SELL layout, no schedule: one warp per chunk.
@@ -688,6 +620,7 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     plan->stepped = e.powerLevelsType == "L" || e.powerLevelsType == "U";
     plan->depRange.alloc((size_t)std::max(C, 1) * 6);
     plan->done.alloc((size_t)std::max(C, 1) * power);
+    plan->ticket.alloc(2);
     plan->status.alloc(1);
     DevBuf<int> dChunkGroup, dBad(1);
     dChunkGroup.upload(chunkGroup.data(), std::max<size_t>(chunkGroup.size(), 1), s);
@@ -751,40 +684,14 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     const bool twoDies = dies.numDies == 2 && e.mpkOrder == 0 && e.mpkDieQueues;
     const std::vector<int> chunkDie =
         twoDies ? chunkDies(C, dies.smsPerDie[0], dies.smsPerDie[1]) : std::vector<int>();
-    const bool twoDiesAny = dies.numDies == 2 && e.mpkOrder != 1 && e.mpkDieQueues;
-    const std::vector<int> chunkDieAny =
-        twoDiesAny ? chunkDies(C, dies.smsPerDie[0], dies.smsPerDie[1]) : std::vector<int>();
-    const MpkOrder order =
-        e.mpkOrder == 1   ? mpkGroupOrder(depRange, chunkGroup, G, power, e.mpkStride == 1 ? 1 : 2, segLen)
-        : e.mpkOrder == 2 ? mpkPowerQueues(depRange, C, power, segLen, e.mpkRun, chunkDieAny)
-                          : mpkRunOrder(depRange, C, power, segLen, e.mpkRun, e.mpkLag, chunkDie);
+    const MpkOrder order = e.mpkOrder == 1
+                               ? mpkGroupOrder(depRange, chunkGroup, G, power, e.mpkStride == 1 ? 1 : 2, segLen)
+                               : mpkRunOrder(depRange, C, power, segLen, e.mpkRun, e.mpkLag, chunkDie);
     plan->numItems = (int)((size_t)C * power);
     plan->numRuns = order.numRuns();
-    plan->numDies = e.mpkOrder == 2 ? (twoDiesAny ? 2 : 1) : (twoDies ? 2 : 1);
+    plan->numDies = twoDies ? 2 : 1;
+    for (int d = 0; d < 3; ++d) plan->dieStart[d] = order.dieStart[d];
     plan->smDie = dies.smDieDev.p;
-    // queues: one per die, or (power groups) dies x groups
-    std::vector<int> qs;
-    if (e.mpkOrder == 2) {
-        plan->groups = order.groups;
-        qs = order.queueStart;
-        if (plan->numDies == 1) qs.resize(order.groups + 1);
-        plan->maxReach = order.maxReach;
-    } else {
-        plan->groups = 1;
-        qs = {order.dieStart[0], order.dieStart[1], order.dieStart[2]};
-        if (plan->numDies == 1) qs.resize(2);
-    }
-    plan->numQueues = (int)qs.size() - 1;
-    plan->runLen = std::max(1, e.mpkRun);
-    plan->queueStart.upload(qs.data(), qs.size(), s);
-    plan->counters.alloc(plan->numQueues + 2);
-    plan->throttleScale = e.mpkThrottle;
-    std::vector<long long> span(2 * (size_t)std::max(plan->numRuns, 1), 0);
-    for (int r = 0; r < plan->numRuns; ++r) {
-        const int c0 = order.head[4 * (size_t)r], c1 = order.head[4 * (size_t)r + 1];
-        span[2 * (size_t)r] = chunkOff[c0];
-        span[2 * (size_t)r + 1] = c1 < C ? chunkOff[c1] : off;
-    }
     std::vector<int> head(order.head), dep(order.dep);
     if (plan->numRuns == 0) {
         head.assign(4, 0);
@@ -792,9 +699,7 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     }
     plan->runHead.upload((const int4 *)head.data(), head.size() / 4, s);
     plan->runDep.upload((const int4 *)dep.data(), dep.size() / 4, s);
-    plan->runSpan.upload((const longlong2 *)span.data(), span.size() / 2, s);
     plan->hints = e.mpkHints;
-    plan->prefetch = e.mpkPrefetch;
     plan->unroll = e.mpkUnroll;
     plan->loads = e.mpkLoads;
     plan->ctasPerSm = e.mpkCtasPerSm;
@@ -891,35 +796,11 @@ void launchSpmvSell(const SellView &v, int numChunks, int n, int k, double *x, f
 }
 }  // namespace
 
-namespace {
-// Warps of one kMpk launch for the plan's kernel variant.
-template <typename VT>
-int residentWarpsT(const MpkPlan &p) {
-    const bool h = p.numHubs > 0;
-    int blocks = 0;
-#define RACE_MPK_OCC(HB, UU, LL)                                                        \
-    if (h == HB && p.unroll == UU && p.loads == LL) blocks = residentBlocks(kMpk<VT, HB, UU, LL>, kWarpThreads);
-    RACE_MPK_OCC(true, 8, 0) RACE_MPK_OCC(true, 8, 1) RACE_MPK_OCC(true, 8, 2)
-    RACE_MPK_OCC(true, 4, 0) RACE_MPK_OCC(true, 4, 1) RACE_MPK_OCC(true, 4, 2)
-    RACE_MPK_OCC(false, 8, 0) RACE_MPK_OCC(false, 8, 1) RACE_MPK_OCC(false, 8, 2)
-    RACE_MPK_OCC(false, 4, 0) RACE_MPK_OCC(false, 4, 1) RACE_MPK_OCC(false, 4, 2)
-#undef RACE_MPK_OCC
-    if (p.ctasPerSm > 0) blocks = std::min(blocks, devSms() * p.ctasPerSm);
-    return blocks * (kWarpThreads / 32);
-}
-int mpkResidentWarps(const MpkPlan &p) {
-    switch (p.valType) {
-    case RACE_VAL_F64: return residentWarpsT<double>(p);
-    case RACE_VAL_F32: return residentWarpsT<float>(p);
-    default: return residentWarpsT<__nv_bfloat16>(p);
-    }
-}
-}  // namespace
-
 void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
     if (power != plan.power) throw Error(RACE_ERR_INVALID_ARG, "power differs from the planned power");
     cudaStream_t s = e.stream;
     RACE_CUDA(cudaMemsetAsync(plan.done.p, 0, sizeof(int) * (size_t)plan.numChunks * plan.power, s));
+    RACE_CUDA(cudaMemsetAsync(plan.ticket.p, 0, sizeof(int) * 2, s));
     RACE_CUDA(cudaMemsetAsync(plan.status.p, 0, sizeof(int), s));
     if (plan.valType != RACE_VAL_F64) kToFloat<<<ceilDiv(ops.n, 256), 256, 0, s>>>((const double *)ops.x, plan.xf.p, ops.n);
     if (plan.stepped) {
@@ -932,22 +813,9 @@ void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
         RACE_CUDA(cudaGetLastError());
         return;
     }
-    RACE_CUDA(cudaMemsetAsync(plan.counters.p, 0, sizeof(int) * (plan.numQueues + 2), s));
-    // group 0's lead over the die's last group (in runs): the reach of the
-    // dependencies over the groups in between plus every group's runs in
-    // flight, with room to spare
-    int throttle = 0;
-    if (plan.groups > 1) {
-        const long long warps = (long long)mpkResidentWarps(plan);
-        const long long perGroup = (warps + plan.numDies * plan.groups - 1) / (plan.numDies * plan.groups);
-        const long long reachRuns = (plan.maxReach + plan.runLen - 1) / plan.runLen + 2;
-        const long long t = ((plan.groups - 1) * reachRuns + plan.groups * perGroup + 64) * plan.throttleScale / 100;
-        throttle = (int)std::min<long long>(t, INT_MAX / 2);
-    }
-    MpkArgs a{viewOf(plan),   (double *)ops.x,  plan.xf.p,        ops.n,        plan.runHead.p, plan.runDep.p,
-              plan.runSpan.p, plan.numChunks,   plan.done.p,      plan.queueStart.p, plan.numQueues, plan.groups,
-              throttle,       plan.counters.p,  plan.status.p,    plan.hints,   plan.prefetch,
-              (int)valBytes(plan.valType),      plan.smDie,       plan.numDies};
+    MpkArgs a{viewOf(plan), (double *)ops.x, plan.xf.p, ops.n, plan.runHead.p, plan.runDep.p,
+              plan.numChunks, plan.done.p, plan.ticket.p, plan.status.p, plan.hints, plan.smDie, plan.numDies,
+              {plan.dieStart[0], plan.dieStart[1], plan.dieStart[2]}};
     switch (plan.valType) {
     case RACE_VAL_F64: launchMpk<double>(a, plan, s); break;
     case RACE_VAL_F32: launchMpk<float>(a, plan, s); break;

@@ -156,42 +156,6 @@ MpkOrder mpkGroupOrder(const std::vector<int> &depRange, const std::vector<int> 
     return o;
 }
 
-MpkOrder mpkPowerQueues(const std::vector<int> &depRange, int numChunks, int power, int groups, int runLen,
-                        const std::vector<int> &chunkDie) {
-    const int C = numChunks;
-    if (C < 0 || power < 1 || (size_t)C * 6 > depRange.size() || (!chunkDie.empty() && (int)chunkDie.size() != C))
-        throw std::invalid_argument("mpkPowerQueues: sizes");
-    groups = std::clamp(groups, 1, power);
-    runLen = std::clamp(runLen, 1, kMpkMaxRunLen);
-    const int dies = chunkDie.empty() ? 1 : 2;
-    auto dieOf = [&](int c) { return chunkDie.empty() ? 0 : (chunkDie[c] ? 1 : 0); };
-    MpkOrder o;
-    o.groups = groups;
-    for (int c = 0; c < C; ++c)
-        for (int d = 0; d < 3; ++d) {
-            const int lo = depRange[6 * (size_t)c + 2 * d], hi = depRange[6 * (size_t)c + 2 * d + 1];
-            if (hi >= lo) o.maxReach = std::max(o.maxReach, hi - c);
-        }
-    o.queueStart.assign(1, 0);
-    for (int d = 0; d < dies; ++d)
-        for (int j = 0; j < groups; ++j) {
-            for (int k = j; k < power; k += groups)
-                for (int c = 0; c < C;) {
-                    if (dieOf(c) != d) {
-                        ++c;
-                        continue;
-                    }
-                    int e = c + 1;
-                    while (e < C && e - c < runLen && dieOf(e) == d) ++e;
-                    appendRun(o, depRange, c, e, k, lastOfSegment(k, power, groups), o.numRuns());
-                    c = e;
-                }
-            o.queueStart.push_back(o.numRuns());
-        }
-    o.dieStart = {0, o.queueStart[groups], o.numRuns()};
-    return o;
-}
-
 std::vector<int> chunkDies(int numChunks, int smsDie0, int smsDie1) {
     std::vector<int> die(std::max(numChunks, 0), 0);
     const long long total = (long long)smsDie0 + smsDie1;

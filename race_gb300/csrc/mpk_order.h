@@ -20,13 +20,6 @@ struct MpkOrder {
     // smaller rank).
     std::vector<int> dieStart{0, 0, 0};
     std::vector<int> rank;
-    // Power-group queues (mpkPowerQueues): queue d*groups+j holds die d's
-    // runs of powers j, j+groups, j+2*groups, ...; queueStart has
-    // numDies*groups+1 entries. maxReach: the largest distance in chunks
-    // from a chunk to the highest chunk it reads.
-    int groups = 0;
-    std::vector<int> queueStart;
-    int maxReach = 0;
     int numRuns() const { return (int)head.size() / 4; }
 };
 
@@ -56,19 +49,6 @@ MpkOrder mpkRunOrder(const std::vector<int> &depRange, int numChunks, int power,
 // of split powers.
 MpkOrder mpkGroupOrder(const std::vector<int> &depRange, const std::vector<int> &chunkGroup, int numGroups,
                        int power, int stride, int split);
-
-// Power-group queues. The warps of each die form `groups` groups; group j
-// sweeps the die's chunks in order at power j, then at power j+groups, and
-// so on, in runs of up to runLen consecutive chunks (one die's chunks). A
-// group's runs wait only on the previous power, i.e. on the group before
-// it, which is ahead in the same sweep, so each power trails the one before
-// it by the rows its chunks read ahead plus its own work in flight: the
-// matrix entries read between two uses of a chunk stay within about
-// groups x (reach + runs in flight) chunks. Group 0 has no waits at its
-// first power and is held back (in the kernel) to stay within a throttle
-// distance of the last group.
-MpkOrder mpkPowerQueues(const std::vector<int> &depRange, int numChunks, int power, int groups, int runLen,
-                        const std::vector<int> &chunkDie = {});
 
 // Chunks go to the two dies in blocks of kDieBlockChunks consecutive
 // chunks, the blocks dealt in proportion to the dies' SM counts, so both

@@ -282,13 +282,10 @@ Engine::Engine(int nrow, int nthreads, int dist_, const int *rowPtr, const int *
     dStatus.alloc(4);
     if (const char *st = getenv("RACE_GPU_MPK_STRIDE")) mpkStride = atoi(st) == 1 ? 1 : 2;
     if (const char *sp = getenv("RACE_GPU_MPK_SPLIT")) mpkSplit = std::max(0, atoi(sp));
-    if (const char *o = getenv("RACE_GPU_MPK_ORDER"))
-        mpkOrder = std::string(o) == "group" ? 1 : std::string(o) == "powers" ? 2 : 0;
-    if (const char *th = getenv("RACE_GPU_MPK_THROTTLE")) mpkThrottle = std::max(1, atoi(th));
+    if (const char *o = getenv("RACE_GPU_MPK_ORDER")) mpkOrder = std::string(o) == "group" ? 1 : 0;
     if (const char *r = getenv("RACE_GPU_MPK_RUN")) mpkRun = std::min(std::max(1, atoi(r)), kMpkMaxRunLen);
     if (const char *l = getenv("RACE_GPU_MPK_LAG")) mpkLag = std::max(0, atoi(l));
     if (const char *d = getenv("RACE_GPU_MPK_DIES")) mpkDieQueues = atoi(d) != 1;
-    if (const char *pf = getenv("RACE_GPU_MPK_PREFETCH")) mpkPrefetch = std::max(0, atoi(pf));
     if (const char *h = getenv("RACE_GPU_MPK_HINTS")) mpkHints = atoi(h) ? 1 : 0;
     if (const char *u = getenv("RACE_GPU_MPK_UNROLL")) mpkUnroll = atoi(u) == 8 ? 8 : 4;
     if (const char *ld = getenv("RACE_GPU_MPK_LOADS")) mpkLoads = std::min(std::max(0, atoi(ld)), 2);

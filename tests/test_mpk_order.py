@@ -198,135 +198,3 @@ def test_issue_order_rejects_bad_input():
     bad_die = np.array([2], np.int32)
     assert call(ok, bad_die.ctypes.data, 2, 2) == _lib.RACE_ERR_INVALID_ARG
     assert call(ok, None, 2, 2) == _lib.RACE_SUCCESS and nr.value == 2
-
-
-def power_queues(dep, groups_of_chunk, power, groups, run, dies=None):
-    L = _lib.lib()
-    C_ = len(groups_of_chunk)
-    dep = np.ascontiguousarray(dep, np.int32)
-    g = np.ascontiguousarray(groups_of_chunk, np.int32)
-    dd = None if dies is None else np.ascontiguousarray(dies, np.int32)
-    dp = None if dd is None else dd.ctypes.data
-    nr = C.c_int(0)
-    qs = np.zeros(2 * groups + 1, np.int32)
-    _lib.check(L.race_mpk_issue_order(dep.ctypes.data, g.ctypes.data, dp, C_, power, 2, 2, groups, run, 0, None,
-                                      None, None, qs.ctypes.data, 0, C.byref(nr)))
-    head = np.zeros((nr.value, 4), np.int32)
-    deps = np.zeros((nr.value, 8), np.int32)
-    _lib.check(L.race_mpk_issue_order(dep.ctypes.data, g.ctypes.data, dp, C_, power, 2, 2, groups, run, 0,
-                                      head.ctypes.data, deps.ctypes.data, None, qs.ctypes.data, nr.value,
-                                      C.byref(nr)))
-    nq = groups * (1 if dies is None else 2)
-    return head, deps, qs[:nq + 1]
-
-
-def simulate(head, deps, qs, C_, power, ndies, groups, warps_per_group, throttle, seed):
-    """The kernel's warp protocol, one step per warp in random order: take a
-    ticket (group 0 of each die holds back while it is more than `throttle`
-    runs ahead of its die's last group), release the previous run, wait for
-    the run's intervals at the previous power, compute. Returns True when
-    every run completes, False on a state where no warp can move."""
-    rng = np.random.default_rng(seed)
-    nq = ndies * groups
-    ticket = [0] * nq
-    done = np.zeros((power, C_), bool)
-    warps = []
-    for d in range(ndies):
-        for j in range(groups):
-            for _ in range(warps_per_group):
-                order = [d * groups + (j + t) % groups for t in range(groups)]
-                order += [(1 - d) * groups + (j + t) % groups for t in range(groups)] if ndies == 2 else []
-                warps.append({"order": order, "t": 0, "hold": None, "pend": None, "g0": j == 0, "fin": False})
-
-    def release(w):
-        if w["pend"] is not None:
-            c0, c1, k = w["pend"]
-            done[k, c0:c1] = True
-            w["pend"] = None
-
-    def ready(r):
-        c0, c1, k, _ = head[r]
-        if k == 0:
-            return True
-        for lo, hi in deps[r].reshape(4, 2):
-            if hi >= lo and not done[k - 1, lo:hi + 1].all():
-                return False
-        return True
-
-    while True:
-        moved = False
-        for i in rng.permutation(len(warps)):
-            w = warps[i]
-            if w["fin"]:
-                continue
-            if w["hold"] is not None:
-                if ready(w["hold"]):
-                    c0, c1, k, _ = head[w["hold"]]
-                    w["pend"], w["hold"] = (c0, c1, k), None
-                    moved = True
-                continue
-            q = w["order"][w["t"]]
-            cnt = qs[q + 1] - qs[q]
-            if w["t"] == 0 and w["g0"] and groups > 1:
-                qL = q + groups - 1
-                if ticket[qL] < qs[qL + 1] - qs[qL] and ticket[q] < cnt and ticket[q] - ticket[qL] > throttle:
-                    if w["pend"] is not None:
-                        release(w)
-                        moved = True
-                    continue
-            it = ticket[q]
-            ticket[q] += 1
-            moved = True
-            if it >= cnt:
-                w["t"] += 1
-                if w["t"] == len(w["order"]):
-                    release(w)
-                    w["fin"] = True
-                continue
-            w["hold"] = qs[q] + it
-            release(w)
-        if all(w["fin"] for w in warps):
-            return bool(done.all())
-        if not moved:
-            return False
-
-
-@pytest.mark.parametrize("name,gen,power,cache", CASES[:4], ids=[c[0] for c in CASES[:4]])
-def test_power_group_queues_complete(name, gen, power, cache):
-    """Power-group queues (order 2): coverage, intervals, and the kernel's
-    throttle protocol completing under simulation with one and three warps
-    per group, with the engine's throttle distance
-    ((groups-1)(ceil(maxReach/run)+2) + groups*warpsPerGroup + 64 runs)."""
-    A = gen()
-    P, gp = partition(A, power, cache)
-    dep, groups_of_chunk, reads, _ = chunk_tables(P, gp)
-    C_ = len(groups_of_chunk)
-    max_reach = max([max(0, dep[c, 1::2].max() - c) for c in range(C_)])
-    for groups in (2, min(3, power), power):
-        for run in (1, 2):
-            for dies in (None, two_dies(C_, 72, 80)):
-                head, deps, qs = power_queues(dep, groups_of_chunk, power, groups, run, dies)
-                ndies = 1 if dies is None else 2
-                assert len(qs) == ndies * groups + 1 and qs[-1] == len(head)
-                pos = -np.ones((power, C_), np.int64)
-                for q in range(ndies * groups):
-                    for r in range(qs[q], qs[q + 1]):
-                        c0, c1, k, _ = head[r]
-                        assert k % groups == q % groups and c1 - c0 <= run
-                        if dies is not None:
-                            assert (dies[c0:c1] == q // groups).all()
-                        assert (pos[k, c0:c1] < 0).all()
-                        pos[k, c0:c1] = r
-                        if k > 0:
-                            waited = np.zeros(C_, bool)
-                            for lo, hi in deps[r].reshape(4, 2):
-                                if hi >= lo:
-                                    waited[lo:hi + 1] = True
-                            for c in range(c0, c1):
-                                assert waited[reads[c]].all()
-                    ks = head[qs[q]:qs[q + 1], 2]
-                    assert (np.diff(ks) >= 0).all(), "queue not power-major"
-                assert (pos >= 0).all()
-                for wpg in (1, 3):
-                    throttle = (groups - 1) * (-(-max_reach // run) + 2) + groups * wpg + 64
-                    assert simulate(head, deps, qs, C_, power, ndies, groups, wpg, throttle, seed=wpg)
