@@ -174,7 +174,7 @@ def cpu_partition(A, x0, threads):
             best = (groups, c)
     if best is None:
         raise RuntimeError("no cache budget gives a partition without hopeless regions for the CPU wavefront")
-    return P, best[0], best[1], times
+    return P, best[0], best[1], times, perm
 
 
 def run_reference(args, rank, world):
@@ -186,7 +186,7 @@ def run_reference(args, rank, world):
     A = build_workload()
     threads = os.cpu_count() or 1
     x0 = matgen.uniform_vector(A.n, 0)
-    P, (gp, ur, dr), budget, _ = cpu_partition(A, x0, threads)
+    P, (gp, ur, dr), budget, _, _ = cpu_partition(A, x0, threads)
     for _ in range(args.warmup):
         orc.mpk_wavefront(P, x0, POWER, gp, ur, dr, threads)
     times = []
@@ -356,6 +356,7 @@ def main():
     assert rc.executeFunction(f32) == 0
     torch.cuda.synchronize()
     exact = bool(torch.equal(x64, y))
+    x64_check = x64.clone()
     ref_last = y[POWER * n:]
     rel32 = float(((x32[POWER * n:] - ref_last).abs().max() / ref_last.abs().max()).item())
 
@@ -483,7 +484,12 @@ def main():
     if tpath.exists():
         traffic = json.loads(tpath.read_text()).get("dram_bytes_per_launch")
 
-    cpu = cpu_baseline(A, x0, args.cpu_seconds) if rank == 0 else None
+    # the GPU's FP64 powers in original row order, for the CPU leg's comparison
+    g = x64_check.reshape(POWER + 1, n)[1:].cpu().numpy()
+    gpu_powers = np.empty_like(g)
+    gpu_powers[:, perm] = g
+    del g
+    cpu = cpu_baseline(A, x0, args.cpu_seconds, gpu_powers) if rank == 0 else None
     del dm32, x32
     symmgs = bench_symmgs(args, ri, matgen, torch) if args.symmgs_rows > 0 else None
     batched = bench_batch(args, ri, matgen, torch) if args.batch_count > 0 else None
@@ -515,6 +521,8 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clocks,
             "fp64_bit_exact_vs_plain_chain": exact,
+            "fp64_bit_exact_vs_cpu_reference": cpu["fp64_powers_equal_gpu"] if cpu else None,
+            "mpk_kernel": mpk_kernel_info(),
             "mixed_f32": {"ms_per_step": ms32, "effective_gbs": eff_bytes / (ms32 * 1e-3) / 1e9,
                           "rel_err_vs_f64": rel32, "meets_1e-10": rel32 <= 1e-10},
             "plain_f64": {"ms_per_step": ms_plain, "effective_gbs": eff_bytes / (ms_plain * 1e-3) / 1e9,
@@ -528,6 +536,20 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def mpk_kernel_info():
+    """The MPK kernel's schedule settings and the L2 die map it used."""
+    import ctypes
+    from race_gb300 import _lib
+    nd, ns = ctypes.c_int(0), ctypes.c_int(0)
+    smd = (ctypes.c_int * 4096)()
+    _lib.check(_lib.lib().race_device_dies(ctypes.byref(nd), smd, 4096, ctypes.byref(ns)))
+    env = {k: v for k, v in os.environ.items() if k.startswith("RACE_GPU_MPK")}
+    return {"order": "chunk-level wavefront, per-die run queues", "lag_chunks": int(env.get("RACE_GPU_MPK_LAG", 8192)),
+            "chunks_per_run": int(env.get("RACE_GPU_MPK_RUN", 2)), "l2_dies": nd.value,
+            "sms_per_die": [sum(1 for i in range(ns.value) if smd[i] == d) for d in range(nd.value)],
+            "env_overrides": env}
 
 
 def bench_symmgs(args, ri, matgen, torch):
@@ -756,21 +778,30 @@ def bench_tuner(torch):
     return out or None
 
 
-def cpu_baseline(A, x0, budget_s: float):
+def cpu_baseline(A, x0, budget_s: float, gpu_powers=None):
     """The reference algorithm (RACE wavefront, oracle port) on all host
     cores, with the host's fastest cache budget, on full MPK calls of the
-    same workload until the time budget is spent."""
+    same workload until the time budget is spent. With gpu_powers (the GPU's
+    FP64 powers 1..p in original row order) it also reports whether the CPU
+    wavefront's powers equal them bit for bit."""
     from oracle import oracle as orc
     threads = os.cpu_count() or 1
-    P, (gp, ur, dr), cache, _ = cpu_partition(A, x0, threads)
+    P, (gp, ur, dr), cache, _, perm = cpu_partition(A, x0, threads)
     times = []
     t_start = time.perf_counter()
+    y = None
     while time.perf_counter() - t_start < budget_s and len(times) < 50:
         t0 = time.perf_counter()
-        orc.mpk_wavefront(P, x0, POWER, gp, ur, dr, threads)
+        y = orc.mpk_wavefront(P, x0, POWER, gp, ur, dr, threads)
         times.append(time.perf_counter() - t0)
     t = statistics.median(times)
+    same = None
+    if gpu_powers is not None:
+        y_orig = np.empty_like(y[1:])
+        y_orig[:, perm] = y[1:]
+        same = bool(np.array_equal(y_orig, gpu_powers))
     return {"value": POWER * spmv_bytes(A.n, A.nnz) / t / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+            "fp64_powers_equal_gpu": same,
             "sample": f"{len(times)} full MPK p={POWER} calls (median), RACE level-group wavefront "
                       f"restated in C on {threads} OpenMP threads, cacheSize {cache / 1e6:.0f} MB (the fastest "
                       f"on this host of {'/'.join(f'{c / 1e6:.0f}' for c in CPU_CACHE_CANDIDATES)} MB)"}

@@ -158,3 +158,30 @@ def test_batch_and_block_errors(mats):
     assert fid_single >= 0
     with pytest.raises(_lib.RaceError):
         ri.Batch().add(rc, fid_single)
+
+
+def test_batch_configured_64_matrices_against_oracle():
+    """The benchmark's batch: 64 anisotropic 2D stencils (aniso2d_batch(64,
+    seed 0), 10k-490k rows), 16 right-hand sides each, p = 4, FP64, RACE
+    level groups at 256 MB each, all in one persistent launch replayed from
+    its CUDA graph. Eight members spread over the batch (the largest among
+    them) are compared with the CPU oracle's fma chains per right-hand side
+    (orc.mpk_block) bit for bit; every member must equal its plain path."""
+    p, nrhs = 4, 16
+    mats = matgen.aniso2d_batch(64, seed=0)
+    b, members = _make_batch(mats, p, nrhs, 256e6, seed=100)
+    b.graphLaunch()
+    assert b.getStatus() == 0
+    torch.cuda.synchronize()
+    largest = int(np.argmax([P.n for _, P, *_ in members]))
+    pick = sorted({0, 9, 21, 33, 47, 58, 63, largest})
+    for i in pick:
+        rc, P, X0, dm, x, fid = members[i]
+        np.testing.assert_array_equal(_powers(x, p, P.n, nrhs), orc.mpk_block(P, X0, p), err_msg=f"member {i}")
+    for rc, P, X0, dm, x, fid in members:
+        got = x[P.n * nrhs:].clone()
+        x[P.n * nrhs:] = 0
+        for k in range(p):
+            rc.spmvPowerLayout(fid, k)
+        torch.cuda.synchronize()
+        assert torch.equal(got, x[P.n * nrhs:])
