@@ -223,9 +223,14 @@ int race_spmv_power_layout(race_engine *e, int func_id, int k);
  * 2 * numGroups + 2 * power ints is rejected with RACE_ERR_INVALID_ARG.
  * Inputs: the FP64 CRS matrix permuted with the engine's MPK permutation
  * (device), the level groups from race_get_power_groups (numGroups+1 row
- * offsets, both a device and a host copy), and x with (power+1)*n doubles,
- * power-major, x[0:n] the input vector (device). Results equal the
- * registered RACE_K_MPK path bit for bit. The first call on a device looks
+ * offsets, both a device and a host copy holding the same offsets: the host
+ * copy sizes the scratch, the kernel reads the device copy; both must run
+ * from 0 to n without decreasing and the device copy must give the same
+ * number of 32-row chunks, otherwise RACE_ERR_INVALID_ARG before any work
+ * item runs), and x with (power+1)*n doubles, power-major, x[0:n] the input
+ * vector (device). A matrix not in the engine's level order is refused with
+ * RACE_ERR_INVALID_ARG too. Results equal the registered RACE_K_MPK path bit
+ * for bit, rows above 256 entries included. The first call on a device looks
  * up the array's device address, so make that first call before any CUDA
  * stream capture. Calls share the array: calls that overlap on the GPU
  * (other streams, other host threads) race and must be serialised by the

@@ -36,6 +36,11 @@ enum DevStatus : int {
 // with an error status instead of hanging.
 constexpr long long kSpinLimit = 1LL << 22;
 
+// Matrix-power rows longer than this are summed by a whole warp: lane l
+// takes entries l, l+32, ... as one fma chain, then an xor butterfly over
+// offsets 16, 8, 4, 2, 1 combines the 32 partial sums.
+constexpr int kMpkHubRowLen = 256;
+
 template <typename T>
 struct DevBuf {
     T *p = nullptr;

@@ -49,7 +49,7 @@ namespace race {
 
 constexpr int kWarpThreads = 256;
 // Rows longer than this are summed by a whole warp from a contiguous copy.
-constexpr int kHubRowLen = 256;
+constexpr int kHubRowLen = kMpkHubRowLen;
 
 namespace {
 

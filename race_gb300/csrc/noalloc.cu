@@ -11,8 +11,9 @@
 // kNoAllocScratchInts ints. Each GPU that loads the library holds that
 // array until the process exits.
 //
-// Work decomposition (same results as the registered MPK path, bit for bit):
-// chunks of 32 consecutive rows inside each level group; work items
+// Work decomposition (same results as the registered MPK path, bit for bit,
+// rows longer than kMpkHubRowLen included: they are summed by the whole warp
+// in the same order): chunks of 32 consecutive rows inside each level group; work items
 // (power k, chunk) in diagonals d = group + 2k; an item waits until, at
 // power k-1, the chunks holding its columns are complete. Chunk positions,
 // diagonal offsets and dependency ranges are derived on the fly from the
@@ -39,17 +40,31 @@ __device__ __forceinline__ int ldAcq(const int *p) {
 }
 
 // Single-block setup: chunk starts per group and item starts per diagonal.
-__global__ void kNaSetup(int *scr, const int *__restrict__ groupPtr, int G, int power, int stride) {
+// The device copy of the groups must describe the layout the host sized
+// the scratch for: rows 0..n in non-decreasing offsets and hostChunks chunks
+// in all. Otherwise the status word reports a bad schedule and no item is
+// issued (all diagonals empty), so no flag beyond the checked region is
+// touched.
+__global__ void kNaSetup(int *scr, const int *__restrict__ groupPtr, int G, int power, int stride, int n,
+                         long long hostChunks) {
     int *chunkStart = scr + 4;
     int *diagStart = chunkStart + G + 1;
     if (threadIdx.x == 0) {
-        int c = 0;
-        for (int g = 0; g < G; ++g) {
-            chunkStart[g] = c;
+        const int D = G + stride * (power - 1);
+        bool ok = groupPtr[0] == 0 && groupPtr[G] == n;
+        long long c = 0;
+        for (int g = 0; g < G && ok; ++g) {
+            if (groupPtr[g + 1] < groupPtr[g]) ok = false;
+            chunkStart[g] = (int)c;
             c += (groupPtr[g + 1] - groupPtr[g] + 31) / 32;
         }
-        chunkStart[G] = c;
-        const int D = G + stride * (power - 1);
+        if (!ok || c != hostChunks) {
+            scr[1] = DEV_BAD_SCHEDULE;
+            for (int g = 0; g <= G; ++g) chunkStart[g] = 0;
+            for (int d = 0; d <= D; ++d) diagStart[d] = 0;
+            return;
+        }
+        chunkStart[G] = (int)c;
         int it = 0;
         for (int d = 0; d < D; ++d) {
             diagStart[d] = it;
@@ -169,11 +184,24 @@ __global__ void __launch_bounds__(kNaThreads) kMpkNoAlloc(NaArgs a) {
                 __nanosleep(32);
             }
         }
-        if (live) {
-            const double *xin = a.x + (size_t)k * a.n;
+        const double *xin = a.x + (size_t)k * a.n;
+        if (live && e - s <= kMpkHubRowLen) {
             double t = 0.0;
             for (int j = s; j < e; ++j) t = fma(a.val[j], xin[a.col[j]], t);
             a.x[(size_t)(k + 1) * a.n + r] = t;
+        }
+        // rows longer than kMpkHubRowLen: the whole warp, in the registered
+        // path's order (lane l: entries l, l+32, ...; then the xor butterfly)
+        unsigned hubs = __ballot_sync(0xffffffffu, live && e - s > kMpkHubRowLen);
+        while (hubs) {
+            const int h = __ffs(hubs) - 1;
+            hubs &= hubs - 1;
+            const int hs = __shfl_sync(0xffffffffu, s, h), he = __shfl_sync(0xffffffffu, e, h);
+            double t = 0.0;
+            for (int j = hs + lane; j < he; j += 32) t = fma(a.val[j], xin[a.col[j]], t);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0) a.x[(size_t)(k + 1) * a.n + r0 + h] = t;
         }
         __syncwarp();
         if (lane == 0)
@@ -199,6 +227,11 @@ extern "C" int race_mpk_noalloc(int n, const int *rowPtr, const int *col, const 
         fprintf(stderr, "[RACE-GB300] race_mpk_noalloc: level groups must cover rows 0..n\n");
         return RACE_ERR_INVALID_ARG;
     }
+    for (int g = 0; g < numGroups; ++g)
+        if (groupPtr_host[g + 1] < groupPtr_host[g]) {
+            fprintf(stderr, "[RACE-GB300] race_mpk_noalloc: level group offsets must not decrease\n");
+            return RACE_ERR_INVALID_ARG;
+        }
     // scratch needed: 4 + (G+1) + (G + 2(p-1) + 1) + p * chunks
     long long chunks = 0;
     for (int g = 0; g < numGroups; ++g) chunks += (groupPtr_host[g + 1] - groupPtr_host[g] + 31) / 32;
@@ -233,7 +266,7 @@ extern "C" int race_mpk_noalloc(int n, const int *rowPtr, const int *col, const 
     if (cudaMemsetAsync(scr, 0, 4 * sizeof(int), s) != cudaSuccess) return RACE_ERR_CUDA;
     if (cudaMemsetAsync(scr + flagsOff, 0, sizeof(int) * (size_t)(power * chunks), s) != cudaSuccess)
         return RACE_ERR_CUDA;
-    kNaSetup<<<1, 32, 0, s>>>(scr, groupPtr_dev, numGroups, power, stride);
+    kNaSetup<<<1, 32, 0, s>>>(scr, groupPtr_dev, numGroups, power, stride, n, chunks);
     int sms = 0, occ = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return RACE_ERR_CUDA;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kMpkNoAlloc, kNaThreads, 0) != cudaSuccess)
