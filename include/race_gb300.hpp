@@ -76,6 +76,13 @@ class Interface {
                   int highestSubPower = 1) {
         return race_power_prepare(e_, highestPower, cacheSize, safetyFactor, mtxType.c_str(), highestSubPower);
     }
+    // RACEing(): the same two entry points under the name the RACE papers
+    // use for the coloring / partitioning step
+    int RACEing() { return RACEColor(); }
+    int RACEing(int highestPower, double cacheSize, double safetyFactor = 2, std::string mtxType = "N",
+                int highestSubPower = 1) {
+        return RACEColor(highestPower, cacheSize, safetyFactor, mtxType, highestSubPower);
+    }
 
     // getPerm / getInvPerm hand over new[]-allocated arrays, as the reference
     // does (the caller delete[]s them; interface.cpp:333-383).

@@ -188,6 +188,11 @@ class Interface:
         return lib().race_power_prepare(self._h, int(highestPower), float(cacheSize), float(safetyFactor),
                                         mtxType.encode(), int(highestSubPower))
 
+    def RACEing(self, *args, **kwargs) -> int:
+        """RACEColor under the name the RACE papers use for the coloring /
+        partitioning step (same arguments, same result)."""
+        return self.RACEColor(*args, **kwargs)
+
     def getPerm(self) -> np.ndarray:
         p = np.zeros(self.nrow, np.int32)
         self._check(lib().race_get_perm(self._h, p.ctypes.data, None))

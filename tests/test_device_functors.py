@@ -96,24 +96,13 @@ def test_device_power_function_matches_spmv_chain(mats, fnlib, m, p, c):
         np.testing.assert_array_equal(x.cpu().numpy().reshape(p + 1, A.n), Y)
 
 
-def test_integration_cuda_example_compiles(tmp_path):
-    """The CUDA example in INTEGRATION.md compiles for sm_103a (the functor
-    at file scope, the calls wrapped in a function)."""
-    import re
-    blocks = re.findall(r"```cuda\n(.*?)```", (ROOT / "INTEGRATION.md").read_text(), re.S)
-    assert blocks
-    for i, b in enumerate(blocks):
-        top, _, calls = b.partition("// after")
-        src = tmp_path / f"ex{i}.cu"
-        src.write_text(f"""#include "race_gb300.hpp"
-{top}
-void example(RACE::gb300::Interface &ce, int *d_rowPtr, int *d_col, double *d_val, double *d_b, double *d_x,
-             cudaStream_t stream) {{
-// after{calls}
-}}
-""")
-        r = subprocess.run([_nvcc(), *NVCC, "-c", str(src), "-o", str(tmp_path / f"ex{i}.o")], capture_output=True,
-                           text=True)
+def test_integration_cuda_examples_compile(tmp_path):
+    """The CUDA examples under tests/examples compile for sm_103a."""
+    srcs = sorted((ROOT / "tests" / "examples").glob("*.cu"))
+    assert srcs
+    for src in srcs:
+        r = subprocess.run([_nvcc(), *NVCC, "-c", str(src), "-o", str(tmp_path / (src.stem + ".o"))],
+                           capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
 
 

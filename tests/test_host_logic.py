@@ -376,28 +376,16 @@ def test_conflict_check_detects_a_bad_phase(golden, mats):
 
 
 def test_integration_examples_compile(tmp_path):
-    """The C++ examples in INTEGRATION.md compile against the headers (each
-    snippet wrapped in a function that declares the caller's arrays)."""
-    import re
+    """The C++ examples under tests/examples compile against the headers."""
     import shutil
     import subprocess
     gxx = shutil.which("g++")
     if gxx is None:
         pytest.skip("no g++")
     root = pathlib.Path(__file__).resolve().parents[1]
-    blocks = re.findall(r"```cpp\n(.*?)```", (root / "INTEGRATION.md").read_text(), re.S)
-    assert blocks
-    for i, b in enumerate(blocks):
-        lines = b.splitlines()
-        head = "\n".join(l for l in lines if l.startswith("#include"))
-        body = "\n".join(l for l in lines if not l.startswith("#include"))
-        src = tmp_path / f"ex{i}.cpp"
-        src.write_text(f"""{head}
-#include "race_gb300.hpp"
-void example(int n, int *rowPtr, int *col, int *d_rowPtr, int *d_col, double *d_val, double *d_x, double *d_b) {{
-{body}
-}}
-""")
+    srcs = sorted((root / "tests" / "examples").glob("*.cpp"))
+    assert srcs
+    for src in srcs:
         r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wno-unused-variable", "-I", str(root / "include"),
                             str(src)], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
