@@ -472,3 +472,34 @@ def test_medium_rows_warp_path_is_bit_exact():
         assert rc.executeFunction(fid) == 0
         out = (b if zero_b else x).cpu().numpy()
         assert np.array_equal(out, br if zero_b else xr), (kern, _rel_err(out, br if zero_b else xr))
+
+
+def test_tune_function_on_registered_mpk(mats):
+    """tuneFunction (src/interface.cpp:605-647) on a registered matrix power:
+    it times powers 1..p, keeps the fastest in its tuned map (a second call
+    returns it without timing again) and leaves the function at that power;
+    the results are then the oracle's first `best` powers, and after
+    setPower back to p all p powers again."""
+    import time
+    A, p = mats["st27_24"], 8
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, 2e6) == 0
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    x0 = matgen.uniform_vector(A.n, 0)
+    ref = orc.mpk_plain(P, x0, p)
+    x = torch.zeros((p + 1) * A.n, dtype=torch.float64, device="cuda")
+    x[: A.n] = torch.tensor(x0, device="cuda")
+    fid = rc.registerFunction(ri.MPK, ri.Operands(_upload(P), x), power=p)
+    best = rc.tuneFunction(fid)
+    assert 1 <= best <= p and rc.getPower(fid) == best
+    t0 = time.perf_counter()
+    assert rc.tuneFunction(fid) == best  # from the tuned map
+    assert time.perf_counter() - t0 < 0.1
+    x[A.n:] = 0
+    assert rc.executeFunction(fid) == 0
+    got = x.cpu().numpy().reshape(p + 1, A.n)
+    np.testing.assert_array_equal(got[: best + 1], ref[: best + 1])
+    assert not got[best + 1:].any()
+    rc.setPower(fid, p)
+    assert rc.executeFunction(fid) == 0
+    np.testing.assert_array_equal(x.cpu().numpy().reshape(p + 1, A.n), ref)
