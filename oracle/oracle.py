@@ -55,6 +55,7 @@ def lib():
             getattr(L, nm).argtypes = [C.c_int, C.c_int, IP, IP, DP, DP, DP]
         L.orc_exec_tree.argtypes = [C.c_int, IP, IP, IP, IP, IP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                     IP, IP, DP, DP, DP]
+        L.orc_exec_phases_omp.argtypes = [C.c_int, C.c_int, IP, IP, IP, C.c_int, C.c_int, IP, IP, DP, DP, DP]
         L.orc_mpk_plain.argtypes = [C.c_int, C.c_int, IP, IP, DP, DP]
         FP = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
         L.orc_mpk_block.argtypes = [C.c_int, C.c_int, C.c_int, IP, IP, DP, DP]
@@ -259,6 +260,13 @@ def exec_tree(nodes, block_per_thread: int, serial_part, kernel: int, rev: bool,
     lib().orc_exec_tree(len(nodes), vs, val, cs, ch, sb, block_per_thread, int(serial_part[0]),
                         int(serial_part[1]), kernel, int(rev), _i32(pcsr.row_ptr), _i32(pcsr.col),
                         _f64(pcsr.val), x, b)
+
+
+def exec_phases_omp(kernel: int, phase_ptr, leaf_lo, leaf_hi, nthreads: int, reps: int, pcsr, x, b):
+    """The colored executor on `nthreads` OpenMP threads over a phase table
+    (x and b float64 arrays, updated in place; `reps` calls)."""
+    lib().orc_exec_phases_omp(kernel, len(phase_ptr) - 1, _i32(phase_ptr), _i32(leaf_lo), _i32(leaf_hi),
+                              int(nthreads), int(reps), _i32(pcsr.row_ptr), _i32(pcsr.col), _f64(pcsr.val), x, b)
 
 
 def mpk_plain(csr, x0, p: int):

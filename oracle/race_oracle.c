@@ -392,6 +392,26 @@ void orc_exec_tree(int nnodes, const int *valueStart, const int *value, const in
         orc_call(kernel, serialHi, serialLo, rowPtr, col, val, x, b);
 }
 
+/* The colored executor on OpenMP threads over a zone tree flattened into
+ * phases (the engine's race_get_phases; leaves of one phase are
+ * conflict-free for the coloring's distance): the leaves of a phase run in
+ * parallel, one static share per thread, and the phases run in order with a
+ * barrier between them, as RACE's executor runs block 0 of all threads, a
+ * barrier, then block 1 (functionManager.cpp:201-265, 1453-1501). A leaf
+ * with lo > hi runs backwards (a reverse sweep). reps calls are made in one
+ * parallel region, as the reference's thread pool stays up between calls. */
+void orc_exec_phases_omp(int kernel, int numPhases, const int *phasePtr, const int *leafLo, const int *leafHi,
+                         int nthreads, int reps, const int *rowPtr, const int *col, const double *val, double *x,
+                         double *b) {
+#pragma omp parallel num_threads(nthreads)
+    for (int r = 0; r < reps; ++r)
+        for (int ph = 0; ph < numPhases; ++ph) {
+#pragma omp for schedule(static)
+            for (int l = phasePtr[ph]; l < phasePtr[ph + 1]; ++l)
+                orc_call(kernel, leafLo[l], leafHi[l], rowPtr, col, val, x, b);
+        }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Matrix power                                                              */
 /* ------------------------------------------------------------------------ */

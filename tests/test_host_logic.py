@@ -940,3 +940,31 @@ def test_stage_partition_with_other_safety_factors(golden, mats):
         gp, hid = _stage_partition(lr, ln, A.n, A.nnz, p, c, safety=sf)
         np.testing.assert_array_equal(gp, golden[k + "__lp"], err_msg=k)
         np.testing.assert_array_equal(hid, golden[k + "__hid"], err_msg=k)
+
+
+@pytest.mark.parametrize("m,d,t", [("lap7_32", 2, 8), ("lap7_32", 2, 64), ("lap7_16", 2, 16), ("st27_16", 2, 128),
+                                   ("lap7_32", 1, 256)])
+def test_openmp_phase_executor_matches_sequential_walk(golden, mats, m, d, t):
+    """The C1 CPU baseline's executor (orc.exec_phases_omp: leaves of a phase
+    on parallel OpenMP threads, a barrier between phases) gives the
+    sequential phase walk's bits: the leaves of a phase never conflict."""
+    A = mats[m]
+    k = key_color(m, d, t)
+    perm = golden[k + "__perm"]
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(A.n, dtype=np.int32)
+    P = A.permuted(perm, inv)
+    U = P.upper()
+    x0 = matgen.uniform_vector(A.n, 0)
+    b0 = matgen.uniform_vector(A.n, 1)
+    kernels = [(orc.K_GS, P, False), (orc.K_GS, P, True)]
+    if d == 2:
+        kernels += [(orc.K_SYMMSPMV, U, False), (orc.K_KACZ, P, False)]
+    for kern, mat, rev in kernels:
+        pp, lo, hi = _flatten(golden[k + "__tree"], d, rev, A.n)
+        xs, bs = x0.copy(), (np.zeros(A.n) if kern == orc.K_SYMMSPMV else b0.copy())
+        _run_phases(pp, lo, hi, kern, mat, xs, bs)
+        for threads in (1, 4, 8):
+            xp, bp = x0.copy(), (np.zeros(A.n) if kern == orc.K_SYMMSPMV else b0.copy())
+            orc.exec_phases_omp(kern, pp, lo, hi, threads, 1, mat, xp, bp)
+            assert np.array_equal(xp, xs) and np.array_equal(bp, bs), (kern, rev, threads)
