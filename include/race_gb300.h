@@ -61,8 +61,10 @@ enum { RACE_VAL_F64 = 0, RACE_VAL_F32 = 1, RACE_VAL_BF16 = 2 };
  * conflict-free waves, one thread per row, results identical bit for bit to
  * RACE's sequential walk (rows above 512 entries use a warp reduction).
  * LEAF: one warp per RACE leaf, rows in order, warp-shuffle row reductions.
- * AUTO (default): per function and direction, whichever is estimated
- * cheaper. */
+ * GATHER (SpMV, SpMTV, SymmSpMV only): one launch, one thread per entry of b
+ * replaying RACE's updates to it in RACE's order (bit-identical to WAVE).
+ * AUTO (default): GATHER for SpMV, SpMTV and SymmSpMV; for GS and KACZ, per
+ * function and direction, whichever of WAVE and LEAF is estimated cheaper. */
 enum { RACE_SWEEP_AUTO = 0, RACE_SWEEP_WAVE = 1, RACE_SWEEP_LEAF = 2, RACE_SWEEP_GATHER = 3 };
 
 typedef struct race_engine race_engine;
@@ -169,7 +171,8 @@ int race_get_status(race_engine *e);
  * as in RACE_SWEEP_AUTO. */
 /* Sweep execution mode of this engine (RACE_SWEEP_*), and the schedule
  * sizes of a registered sweep function in one direction: waves and the
- * largest wave, phases and the longest leaf, and the mode AUTO picks. No
+ * largest wave, phases and the longest leaf, and the mode that runs
+ * (*waveModeChosen: 0 leaf, 1 wave, 2 gather). No
  * counterpart in the reference (its executor has one mode). */
 int race_set_sweep_mode(race_engine *e, int mode);
 int race_get_sweep_info(race_engine *e, int func_id, int rev, int *numWaves, int *maxWaveRows, int *numPhases,

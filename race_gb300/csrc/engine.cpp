@@ -21,6 +21,7 @@ void uploadPhases(Engine &e, int dir);
 void buildSweepWaves(Engine &e, FuncEntry &f);
 void runSweep(Engine &e, FuncEntry &f, bool rev);
 bool useWaveMode(const Engine &e, const FuncEntry &f, int dir);
+bool usesGather(const Engine &e, const FuncEntry &f);
 void symmGsIr(Engine &e, int inner, int n, const int *rowPtr, const int *col, const double *val, const double *b,
               double *x, double tol, int maxIter, int sweeps, int *itersOut, double *relresOut);
 std::unique_ptr<BlockPlan> buildBlockPlan(Engine &e, const race_operands &ops, int power, int nrhs);
@@ -439,7 +440,7 @@ int race_get_sweep_info(race_engine *e, int func_id, int rev, int *numWaves, int
     *maxWaveRows = f.waves[dir].maxRows;
     *numPhases = e->eng->dPhases[dir].numPhases;
     *maxLeafRows = e->eng->dPhases[dir].maxLeafRows;
-    *waveModeChosen = race::useWaveMode(*e->eng, f, dir) ? 1 : 0;
+    *waveModeChosen = race::usesGather(*e->eng, f) ? 2 : race::useWaveMode(*e->eng, f, dir) ? 1 : 0;
     return RACE_SUCCESS;
 }
 

@@ -175,8 +175,9 @@ class Engine {
     DevBuf<unsigned char> dCubTemp;
     int stamp = 0;
 
-    // sweep execution: SWEEP_AUTO, SWEEP_WAVE (bit-exact wave plans) or
-    // SWEEP_LEAF (warp per leaf)
+    // sweep execution: SWEEP_AUTO (gather for SpMV/SpMTV/SymmSpMV, else wave
+    // or leaf by cost), SWEEP_WAVE (bit-exact wave plans), SWEEP_LEAF (warp
+    // per leaf), SWEEP_GATHER
     int sweepMode = SWEEP_AUTO;
 
     // coloring results
@@ -197,7 +198,7 @@ class Engine {
     int mpkStride = 2;
     int mpkSplit = 0;
     int mpkRun = 2;
-    int mpkLag = 8192;
+    int mpkLag = 32768;
     bool mpkDieQueues = true;
     int mpkHints = 1;
     int mpkUnroll = 4;

@@ -331,7 +331,7 @@ class Interface:
         v = [C.c_int() for _ in range(5)]
         self._check(lib().race_get_sweep_info(self._h, int(funcId), int(bool(rev)), *[C.byref(a) for a in v]))
         return dict(waves=v[0].value, max_wave_rows=v[1].value, phases=v[2].value, max_leaf_rows=v[3].value,
-                    wave_mode=bool(v[4].value))
+                    wave_mode=v[4].value == 1, mode={0: "leaf", 1: "wave", 2: "gather"}[v[4].value])
 
     def setStream(self, stream: torch.cuda.Stream):
         self.stream = stream
