@@ -68,22 +68,36 @@ struct Splitter {
         return (lbTarget == LB_ROW || forceRow) ? ld.levelRow : ld.levelNnz;
     }
 
+    // Per-block sums of the level counts: integer sums, taken from prefix
+    // sums (the same values as adding the levels of each block one by one).
+    std::vector<long long> prefixRow, prefixTarget;
+    void prefixSums() {
+        for (int f = 0; f < 2; ++f) {
+            const std::vector<int> &t = target(f == 1);
+            std::vector<long long> &p = f == 1 ? prefixRow : prefixTarget;
+            p.assign(t.size() + 1, 0);
+            for (size_t j = 0; j < t.size(); ++j) p[j + 1] = p[j] + t[j];
+        }
+    }
     void chunkSum(const std::vector<int> &lp, int len, bool forceRow, std::vector<int> &out) const {
-        const std::vector<int> &t = target(forceRow);
+        const std::vector<long long> &p = forceRow || lbTarget == LB_ROW ? prefixRow : prefixTarget;
         out.assign(len, 0);
-        for (int i = 0; i < len; ++i)
-            for (int j = lp[i]; j < lp[i + 1]; ++j) out[i] += t[j];
+        for (int i = 0; i < len; ++i) out[i] = (int)(p[lp[i + 1]] - p[lp[i]]);
     }
 
-    // findNeighbour (lb.cpp:134-169)
+    // findNeighbour (lb.cpp:134-169): the first index of the weights in
+    // stable descending order (for acquire: the first whose block is wider
+    // than minGapV). That is the largest weight, the smallest index among
+    // equal weights, so a linear scan gives it without sorting.
     int findNeighbour(const Stat &s, bool acquire) const {
-        std::vector<int> perm = rankDescending(acquire ? s.acquireWeight : s.giveWeight);
-        if (!acquire) return perm[0];
-        for (int r = 0; r < totalBlocks; ++r) {
-            int idx = perm[r];
-            if ((levelPtr[idx + 1] - levelPtr[idx]) > minGapV) return idx;
+        const std::vector<double> &w = acquire ? s.acquireWeight : s.giveWeight;
+        int best = -1;
+        const int m = acquire ? totalBlocks : (int)w.size();
+        for (int idx = 0; idx < m; ++idx) {
+            if (acquire && (levelPtr[idx + 1] - levelPtr[idx]) <= minGapV) continue;
+            if (best < 0 || w[idx] > w[best]) best = idx;
         }
-        return -1;
+        return best;
     }
 
     // moveOneStep (lb.cpp:171-185); fromIdx may be -1 (the reference then
@@ -98,6 +112,7 @@ struct Splitter {
 
     void run() {
         const int totalLevel = ld.totalLevel;
+        prefixSums();
         // calcEffectiveRatio (lb.cpp:114-132). The product of a level count
         // and the thread count is formed in 32-bit int arithmetic, as in the
         // reference, before the division.

@@ -23,14 +23,34 @@ bool traverseRangeHost(int n, const int *rowPtr, const int *col, std::vector<int
     s.frontier.assign(1, lo);
     s.stamp[lo] = st;
     s.dist[0] = 0;
+    if (mode == 2 && (int)s.mark.size() < n) s.mark.assign(n, 0);
+    // non-zeros of the range's unvisited rows (the work of a pull step)
+    long long unvisitedNnz = 0;
+    if (mode == 2)
+        for (int i = lo; i < hi; ++i) unvisitedNnz += rowPtr[totalPerm[i] + 1] - rowPtr[totalPerm[i]];
+    unvisitedNnz -= rowPtr[totalPerm[lo] + 1] - rowPtr[totalPerm[lo]];
     long long counter = 1;
     int currLvl = 0, prevIslandStop = lo;
     while (!s.frontier.empty()) {
         ++currLvl;
         s.next.clear();
+        // distance-2: push from the frontier's rows outside the range, or
+        // let the unvisited rows of the range pull from them
+        bool pull = false;
+        if (mode == 2) {
+            long long outNnz = 0;
+            for (int u : s.frontier)
+                if (u < lo || u >= hi) outNnz += rowPtr[totalPerm[u] + 1] - rowPtr[totalPerm[u]];
+            pull = outNnz > unvisitedNnz;
+        }
+        const long long mk = ++s.markVal;
         for (int u : s.frontier) {
             const int pu = totalPerm[u];
             const bool uIn = u >= lo && u < hi;
+            if (pull && !uIn) {
+                s.mark[u] = mk;
+                continue;
+            }
             for (int j = rowPtr[pu]; j < rowPtr[pu + 1]; ++j) {
                 const int c = col[j];
                 if (c < 0 || c >= n) continue;  // columns beyond the matrix are remote
@@ -43,6 +63,26 @@ bool traverseRangeHost(int n, const int *rowPtr, const int *col, std::vector<int
                 if (inRange) {
                     s.dist[c2 - lo] = currLvl;
                     ++counter;
+                    unvisitedNnz -= rowPtr[c + 1] - rowPtr[c];
+                }
+            }
+        }
+        if (pull) {
+            for (int w = lo; w < hi; ++w) {
+                if (s.stamp[w] == st) continue;
+                const int pw = totalPerm[w];
+                for (int j = rowPtr[pw]; j < rowPtr[pw + 1]; ++j) {
+                    const int c = col[j];
+                    if (c < 0 || c >= n) continue;
+                    const int c2 = totalInvPerm[c];
+                    if ((c2 < lo || c2 >= hi) && s.mark[c2] == mk) {
+                        s.stamp[w] = st;
+                        s.next.push_back(w);
+                        s.dist[w - lo] = currLvl;
+                        ++counter;
+                        unvisitedNnz -= rowPtr[pw + 1] - rowPtr[pw];
+                        break;
+                    }
                 }
             }
         }
@@ -59,6 +99,7 @@ bool traverseRangeHost(int n, const int *rowPtr, const int *col, std::vector<int
             ++currLvl;
             s.stamp[isl] = st;
             s.dist[isl - lo] = currLvl;
+            if (mode == 2) unvisitedNnz -= rowPtr[totalPerm[isl] + 1] - rowPtr[totalPerm[isl]];
             s.frontier.assign(1, isl);
             ++counter;
             prevIslandStop = isl;

@@ -10,10 +10,13 @@
 namespace race {
 
 // Per-row scratch of host traversals: a stamp per row (a row belongs to the
-// traversal whose stamp it carries) and a level per row of the range.
+// traversal whose stamp it carries), a level per row of the range, and a
+// frontier mark per row for the pull steps.
 struct HostTraverseScratch {
     std::vector<int> stamp, dist, frontier, next;
     int stampVal = 0;
+    std::vector<long long> mark;
+    long long markVal = 0;
 };
 
 // Traverse::calculateDistance + createLevelData + permuteGraph
@@ -26,6 +29,12 @@ struct HostTraverseScratch {
 // rowPtr/col, indexed by original rows); the range is then sorted stably by
 // level and the sort is composed into totalPerm/totalInvPerm (new index ->
 // original row and back). Returns false if rows of the range went missing.
+// Distance-2 steps are direction-optimised (Beamer, Asanovic, Patterson,
+// SC 2012): when the rows outside the range in the frontier have more
+// non-zeros than the unvisited rows of the range, those rows are marked and
+// every unvisited row of the range looks for a marked neighbour in its own
+// row instead (the graph must be structurally symmetric, as the engine's
+// traversal graph is). BFS levels, hence the result, do not depend on it.
 bool traverseRangeHost(int n, const int *rowPtr, const int *col, std::vector<int> &totalPerm,
                        std::vector<int> &totalInvPerm, int lo, int hi, int mode, HostTraverseScratch &s,
                        LevelData &ld);
