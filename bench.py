@@ -291,8 +291,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="budget of the CPU baseline sample")
-    ap.add_argument("--symmgs-rows", type=int, default=1 << 20,
-                    help="rows of the power-law SymmGS system (0 skips it; the full configuration is 4194304)")
+    ap.add_argument("--symmgs-rows", type=int, default=4194304,
+                    help="rows of the power-law SymmGS system (the configuration's 4,194,304; 0 skips it)")
     ap.add_argument("--profile", choices=["mpk", "batch", "symmgs"], default=None,
                     help="profiling case (mpk, batch or symmgs; see run_profile_case); prints no JSON")
     ap.add_argument("--no-tuner", action="store_true", help="skip the MLP tuner training/evaluation")

@@ -204,12 +204,14 @@ class Engine {
     int mpkUnroll = 4;
     int mpkLoads = 1;
     int mpkCtasPerSm = 0;
-    // Ranges shorter than this are traversed on the host (RACE_GPU_HOST_TRAVERSE_BELOW,
-    // 0: never); the device permutation is then refreshed before the next
-    // GPU traversal and at the end of the coloring.
     // the MPK partition's leaf tree (the root alone without hopeless regions)
     std::vector<MpkLeaf> powerTree;
-    int hostTraverseBelow = 0;
+    // Coloring ranges shorter than this are traversed on the host (all of
+    // them for graphs with rows above 1024 entries, else below 2^20 rows;
+    // RACE_GPU_HOST_TRAVERSE_BELOW overrides, 0: never); the device
+    // permutation is then refreshed before the next GPU traversal and at the
+    // end of the coloring.
+    int hostTraverseBelow = 1 << 20;
     bool devPermStale = false;
     HostTraverseScratch hostScratch;
     void syncDevicePerm();

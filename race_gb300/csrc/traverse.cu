@@ -19,6 +19,7 @@
 #include <cub/cub.cuh>
 
 #include <algorithm>
+#include <climits>
 #include <numeric>
 
 #include "engine.h"
@@ -290,6 +291,16 @@ Engine::Engine(int nrow, int nthreads, int dist_, const int *rowPtr, const int *
     if (const char *u = getenv("RACE_GPU_MPK_UNROLL")) mpkUnroll = atoi(u) == 8 ? 8 : 4;
     if (const char *ld = getenv("RACE_GPU_MPK_LOADS")) mpkLoads = std::min(std::max(0, atoi(ld)), 2);
     if (const char *b = getenv("RACE_GPU_MPK_CTAS")) mpkCtasPerSm = std::max(0, atoi(b));
+    // Coloring traversals (distance-1/-2) of ranges shorter than
+    // hostTraverseBelow run on the host (direction-optimised BFS, a few
+    // microseconds for the many short ranges of a level recursion, where a
+    // GPU traversal pays launches and host round trips per level). On a
+    // GB300 host a graph with hub rows colours fastest entirely on the host
+    // (4.2M-row power-law graph, distance 2: 1.9 s against 24 s with GPU
+    // traversals); without hubs the GPU takes ranges from 2^20 rows on.
+    int maxRowLen = 0;
+    for (int r = 0; r < nrow; ++r) maxRowLen = std::max(maxRowLen, hRowPtr[r + 1] - hRowPtr[r]);
+    hostTraverseBelow = maxRowLen > 1024 ? INT_MAX : (1 << 20);
     if (const char *ht = getenv("RACE_GPU_HOST_TRAVERSE_BELOW")) hostTraverseBelow = std::max(0, atoi(ht));
     if (const char *sm = getenv("RACE_GPU_SWEEP_MODE")) {
         std::string m(sm);
