@@ -215,6 +215,16 @@ int race_symmgs_ir(race_engine *e, int inner_func_id, int n, const int *rowPtr_d
  * the reference, whose examples time it separately as tradPower). */
 int race_spmv_power_layout(race_engine *e, int func_id, int k);
 
+/* The device layout of a registered RACE_K_MPK function (no counterpart in
+ * the reference, which keeps the caller's CRS): SELL-32 chunks, the bits of
+ * a stored column index (16: a 2-bit window and a 14-bit offset from one of
+ * the chunk's four window bases; 32: plain indices), the chunks that keep
+ * 32-bit columns in the 16-bit layout, the SELL slots with padding, and the
+ * bytes of the matrix arrays one power reads (values, columns, row lengths,
+ * chunk tables, hub copies). */
+int race_get_mpk_layout(race_engine *e, int func_id, int *numChunks, int *colBits, int *wideChunks,
+                        long long *sellSlots, long long *matrixBytes);
+
 /* Matrix power without any device allocation. No counterpart in the
  * reference (its executor runs on the host and allocates freely).
  * For callers that cannot allocate device memory when they run the kernel:

@@ -40,6 +40,8 @@ constexpr long long kSpinLimit = 1LL << 22;
 // takes entries l, l+32, ... as one fma chain, then an xor butterfly over
 // offsets 16, 8, 4, 2, 1 combines the 32 partial sums.
 constexpr int kMpkHubRowLen = 256;
+// Largest column window of the MPK's 16-bit column layout (14-bit offsets).
+constexpr int kMpkColWindow = 1 << 14;
 
 template <typename T>
 struct DevBuf {

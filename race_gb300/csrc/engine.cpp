@@ -444,6 +444,26 @@ int race_get_sweep_info(race_engine *e, int func_id, int rev, int *numWaves, int
     return RACE_SUCCESS;
 }
 
+int race_get_mpk_layout(race_engine *e, int func_id, int *numChunks, int *colBits, int *wideChunks,
+                        long long *sellSlots, long long *matrixBytes) {
+    if (!e || func_id < 0 || func_id >= (int)e->eng->funcs.size() || !numChunks || !colBits || !wideChunks ||
+        !sellSlots || !matrixBytes)
+        return RACE_ERR_INVALID_ARG;
+    const race::FuncEntry &f = e->eng->funcs[func_id];
+    if (f.kernel != RACE_K_MPK || !f.mpk) return RACE_ERR_INVALID_ARG;
+    const race::MpkPlan &p = *f.mpk;
+    *numChunks = p.numChunks;
+    *colBits = p.col16 ? 16 : 32;
+    *wideChunks = p.wideChunks;
+    *sellSlots = p.sellSlots;
+    const long long vb = p.valType == RACE_VAL_F64 ? 8 : p.valType == RACE_VAL_F32 ? 4 : 2;
+    *matrixBytes = p.sellSlots * vb + (p.col16 ? 2 * p.sellSlots + 4 * p.wideSlots + 16LL * p.numChunks
+                                                : 4 * p.sellSlots) +
+                   4LL * (long long)p.rowLen.n + 12LL * p.numChunks + 4LL * (long long)p.hubRow.n +
+                   (vb + 4) * (long long)p.hubCol.n;
+    return RACE_SUCCESS;
+}
+
 int race_set_power(race_engine *e, int func_id, int power) {
     if (!e || func_id < 0 || func_id >= (int)e->eng->funcs.size()) return RACE_ERR_INVALID_ARG;
     return guard(e, [&] {

@@ -46,7 +46,16 @@ struct MpkPlan {
     DevBuf<unsigned char> hubVal;  // hub entries (type valType)
     DevBuf<int> hubCol;
     DevBuf<unsigned char> sellVal;  // sellSlots values (type valType)
-    DevBuf<int> sellCol;        // sellSlots column indices
+    DevBuf<int> sellCol;        // sellSlots column indices (32-bit layout)
+    // 16-bit layout (col16): per chunk four column window bases, per slot a
+    // 2-bit window and a 14-bit offset; chunks whose columns need more
+    // windows (base x < 0) keep 32-bit columns in wideCol from slot y on
+    bool col16 = false;
+    DevBuf<int4> chunkBase;
+    DevBuf<unsigned short> sellCol16;
+    DevBuf<int> wideCol;
+    int wideChunks = 0;
+    long long wideSlots = 0;
     DevBuf<float> xf;           // (power+1)*n FP32 powers (reduced-precision storage)
     DevBuf<int> depRange;       // numChunks*6: chunks read in the previous/own/next group
     int numRuns = 0;            // runs of the persistent kernel (mpk_order.h)
@@ -56,8 +65,6 @@ struct MpkPlan {
     int dieStart[3] = {0, 0, 0};
     const int *smDie = nullptr; // device table: die of every SM
     int hints = 1;              // L2 eviction hints on the matrix loads
-    int unroll = 4;             // row-loop unroll of kMpk (4 or 8)
-    int loads = 1;              // kMpk matrix loads: 0 plain, 1 with an L2 policy, 2 non-coherent without L1
     int ctasPerSm = 0;          // kMpk blocks per SM (0: as many as fit)
     DevBuf<int> done;           // power * numChunks completion flags
     DevBuf<int> ticket;         // next run of each die queue
@@ -192,8 +199,11 @@ class Engine {
     // chunk-level wavefront, 1 the level-group order with stride mpkStride
     // (1: RACE's, 2); powers per segment (0: all powers in one sweep);
     // chunks per run; lag in chunks; one queue per L2 die; eviction hints;
-    // row unroll; matrix load flavour; blocks per SM (0: as many as fit).
-    // The defaults are the fastest measured on the 128^3 27-point stencil.
+    // blocks per SM (0: as many as fit); 16-bit column layout where the
+    // columns fit, with windows of mpkColWindow rows (at most
+    // kMpkColWindow; smaller windows only make more chunks keep 32-bit
+    // columns). The defaults are the fastest measured on the 128^3 27-point
+    // stencil.
     int mpkOrder = 0;
     int mpkStride = 2;
     int mpkSplit = 0;
@@ -201,9 +211,9 @@ class Engine {
     int mpkLag = 32768;
     bool mpkDieQueues = true;
     int mpkHints = 1;
-    int mpkUnroll = 4;
-    int mpkLoads = 1;
     int mpkCtasPerSm = 0;
+    bool mpkCol16 = true;
+    int mpkColWindow = kMpkColWindow;
     // the MPK partition's leaf tree (the root alone without hopeless regions)
     std::vector<MpkLeaf> powerTree;
     // Coloring ranges shorter than this are traversed on the host (all of

@@ -83,52 +83,38 @@ __device__ __forceinline__ unsigned long long l2Policy(int kind) {
     return p;
 }
 
-// Matrix loads of the wavefront kernel with an L2 policy. LD 1: through L1
-// as plain loads are; LD 2: the matrix is read-only while a kernel runs and
-// each entry is read once per item, so the loads take the non-coherent path
-// without allocating in L1 (which keeps the gathered x).
-template <int LD>
-__device__ __forceinline__ double ldMat(const double *a, unsigned long long pol) {
+// Matrix loads of the wavefront kernel with an L2 eviction policy.
+__device__ __forceinline__ double ldPol(const double *a, unsigned long long pol) {
     double v;
-    if constexpr (LD == 2)
-        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
-    else
-        asm("ld.global.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+    asm("ld.global.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
     return v;
 }
-template <int LD>
-__device__ __forceinline__ float ldMat(const float *a, unsigned long long pol) {
+__device__ __forceinline__ float ldPol(const float *a, unsigned long long pol) {
     float v;
-    if constexpr (LD == 2)
-        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
-    else
-        asm("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+    asm("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
     return v;
 }
-template <int LD>
-__device__ __forceinline__ __nv_bfloat16 ldMat(const __nv_bfloat16 *a, unsigned long long pol) {
+__device__ __forceinline__ __nv_bfloat16 ldPol(const __nv_bfloat16 *a, unsigned long long pol) {
     unsigned short v;
-    if constexpr (LD == 2)
-        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(a), "l"(pol));
-    else
-        asm("ld.global.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(a), "l"(pol));
+    asm("ld.global.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(a), "l"(pol));
     return __ushort_as_bfloat16(v);
 }
-template <int LD>
-__device__ __forceinline__ int ldMat(const int *a, unsigned long long pol) {
+__device__ __forceinline__ int ldPol(const int *a, unsigned long long pol) {
     int v;
-    if constexpr (LD == 2)
-        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
-    else
-        asm("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    asm("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ unsigned short ldPol(const unsigned short *a, unsigned long long pol) {
+    unsigned short v;
+    asm("ld.global.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(a), "l"(pol));
     return v;
 }
 
-// Matrix entry loads: LD 0 plain loads, 1 and 2 with an L2 policy (ldMat).
-template <int LD, typename T>
+// Matrix entry loads: POL false plain loads, true with an L2 policy.
+template <bool POL, typename T>
 __device__ __forceinline__ T ldEntry(const T *a, unsigned long long pol) {
-    if constexpr (LD > 0)
-        return ldMat<LD>(a, pol);
+    if constexpr (POL)
+        return ldPol(a, pol);
     else
         return *a;
 }
@@ -163,7 +149,7 @@ __device__ __forceinline__ double floatToDoubleExact(float f) {
 
 struct SellView {
     const void *val;
-    const int *col;
+    const int *col;             // 32-bit layout: sellSlots column indices
     const long long *chunkOff;  // numChunks: element offset of each chunk
     const int *chunkRow;        // numChunks+1: first row of each chunk
     const int *rowLen;          // n (-1: hub row)
@@ -171,69 +157,101 @@ struct SellView {
     const int *hubRow, *hubPtr;
     const void *hubVal;
     const int *hubCol;
+    // 16-bit layout: per chunk four window bases (x < 0: the chunk keeps
+    // 32-bit columns in wideCol from slot y on), per slot the window in bits
+    // 14-15 and the offset from its base in bits 0-13
+    const int4 *chunkBase;
+    const unsigned short *col16;
+    const int *wideCol;
 };
 
-// One row of a SELL-32 chunk, FP64 storage: lane-owned fma chain. U = 8
-// issues the row in batches: eight column and value loads, then the eight
-// gathers of x, then the eight fused multiply-adds in entry order (the same
-// sequential chain, more loads in flight per warp).
-template <int U, int LD>
-__device__ __forceinline__ double sellRowD(const double *__restrict__ val, const int *__restrict__ col, long long off,
-                                           int len, const double *x, unsigned long long pol) {
-    double t = 0.0;
-    if constexpr (U == 8) {
-        for (int j = 0; j < len; j += 8) {
-            int cc[8];
-            double vv[8], xx[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-                if (j + i < len) {
-                    cc[i] = ldEntry<LD>(col + off + 32LL * (j + i), pol);
-                    vv[i] = ldEntry<LD>(val + off + 32LL * (j + i), pol);
-                }
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-                if (j + i < len) xx[i] = x[cc[i]];
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-                if (j + i < len) t = fma(vv[i], xx[i], t);
-        }
+// Column j of the lane's row: a stored 32-bit index (C16 false), or the
+// base of window v >> 14 plus the low 14 bits of the stored entry v.
+template <bool C16, bool POL>
+__device__ __forceinline__ int sellColumn(const void *col, long long off, int j, int4 b, unsigned long long pol) {
+    if constexpr (C16) {
+        const unsigned v = ldEntry<POL>((const unsigned short *)col + off + 32LL * j, pol);
+        const int base = (v & 0x8000u) ? ((v & 0x4000u) ? b.w : b.z) : ((v & 0x4000u) ? b.y : b.x);
+        return base + (int)(v & 0x3fffu);
     } else {
-#pragma unroll 4
-        for (int j = 0; j < len; ++j)
-            t = fma(ldEntry<LD>(val + off + 32LL * j, pol), x[ldEntry<LD>(col + off + 32LL * j, pol)], t);
+        return ldEntry<POL>((const int *)col + off + 32LL * j, pol);
     }
+}
+
+// One row of a SELL-32 chunk, FP64 storage: the lane's fma chain over its
+// entries in CRS order (values at voff + 32 j, columns at coff + 32 j).
+// B > 0 (16-bit columns only) issues the row in batches of B entries: B
+// column and value loads, then B gathers of x, then B fmas in entry order
+// (the same chain; the code the compiler schedules differs, and which one
+// is faster depends on the kernel and value type).
+template <bool C16, bool POL, int B>
+__device__ __forceinline__ double sellRowD(const double *__restrict__ val, long long voff, const void *col,
+                                           long long coff, int4 b, int len, const double *x,
+                                           unsigned long long pol) {
+    double t = 0.0;
+    int j = 0;
+    if constexpr (C16 && B > 0) {
+        for (; j + B <= len; j += B) {
+            int cc[B];
+            double vv[B], xx[B];
+#pragma unroll
+            for (int i = 0; i < B; ++i) {
+                cc[i] = sellColumn<C16, POL>(col, coff, j + i, b, pol);
+                vv[i] = ldEntry<POL>(val + voff + 32LL * (j + i), pol);
+            }
+#pragma unroll
+            for (int i = 0; i < B; ++i) xx[i] = x[cc[i]];
+#pragma unroll
+            for (int i = 0; i < B; ++i) t = fma(vv[i], xx[i], t);
+        }
+    }
+#pragma unroll 4
+    for (; j < len; ++j)
+        t = fma(ldEntry<POL>(val + voff + 32LL * j, pol), x[sellColumn<C16, POL>(col, coff, j, b, pol)], t);
     return t;
 }
 // FP32/BF16 storage with an FP32 vector.
-template <typename VT, int U, int LD>
-__device__ __forceinline__ float sellRowF(const VT *__restrict__ val, const int *__restrict__ col, long long off,
-                                          int len, const float *x, unsigned long long pol) {
+template <typename VT, bool C16, bool POL, int B>
+__device__ __forceinline__ float sellRowF(const VT *__restrict__ val, long long voff, const void *col, long long coff,
+                                          int4 b, int len, const float *x, unsigned long long pol) {
     float t = 0.0f;
-    if constexpr (U == 8) {
-        for (int j = 0; j < len; j += 8) {
-            int cc[8];
-            float vv[8], xx[8];
+    int j = 0;
+    if constexpr (C16 && B > 0) {
+        for (; j + B <= len; j += B) {
+            int cc[B];
+            float vv[B], xx[B];
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
-                if (j + i < len) {
-                    cc[i] = ldEntry<LD>(col + off + 32LL * (j + i), pol);
-                    vv[i] = toF<VT>(ldEntry<LD>(val + off + 32LL * (j + i), pol));
-                }
+            for (int i = 0; i < B; ++i) {
+                cc[i] = sellColumn<C16, POL>(col, coff, j + i, b, pol);
+                vv[i] = toF<VT>(ldEntry<POL>(val + voff + 32LL * (j + i), pol));
+            }
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
-                if (j + i < len) xx[i] = x[cc[i]];
+            for (int i = 0; i < B; ++i) xx[i] = x[cc[i]];
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
-                if (j + i < len) t = fmaf(vv[i], xx[i], t);
+            for (int i = 0; i < B; ++i) t = fmaf(vv[i], xx[i], t);
         }
-    } else {
-#pragma unroll 4
-        for (int j = 0; j < len; ++j)
-            t = fmaf(toF<VT>(ldEntry<LD>(val + off + 32LL * j, pol)), x[ldEntry<LD>(col + off + 32LL * j, pol)],
-                     t);
     }
+#pragma unroll 4
+    for (; j < len; ++j)
+        t = fmaf(toF<VT>(ldEntry<POL>(val + voff + 32LL * j, pol)), x[sellColumn<C16, POL>(col, coff, j, b, pol)],
+                 t);
     return t;
+}
+
+// Row r at power k -> k+1 from its SELL entries; FP32/BF16 results also go
+// to the FP64 powers through the exact conversion.
+template <typename VT, bool C16, bool POL, int B>
+__device__ __forceinline__ void sellRow(const SellView &m, const void *col, long long voff, long long coff, int4 b,
+                                        int len, int r, int k, int n, double *x, float *xf,
+                                        unsigned long long pol) {
+    if constexpr (sizeof(VT) == 8) {
+        x[(size_t)(k + 1) * n + r] =
+            sellRowD<C16, POL, B>((const double *)m.val, voff, col, coff, b, len, x + (size_t)k * n, pol);
+    } else {
+        const float v = sellRowF<VT, C16, POL, B>((const VT *)m.val, voff, col, coff, b, len, xf + (size_t)k * n, pol);
+        xf[(size_t)(k + 1) * n + r] = v;
+        x[(size_t)(k + 1) * n + r] = floatToDoubleExact(v);
+    }
 }
 
 // A hub row summed by the whole warp: lane l takes entries l, l+32, ... in
@@ -260,8 +278,9 @@ __device__ __forceinline__ AT hubSum(const SellView &m, int h, const AT *x) {
 // Chunk c at power k -> k+1: the lane's row (unless it is a hub row), then
 // the chunk's hub rows one at a time with the whole warp. Called by all 32
 // lanes of a warp. HUBS = false compiles the plain SELL row only (plans
-// without hub rows keep the register count, hence the occupancy, of that).
-template <typename VT, bool HUBS, int U = 4, int LD = 0>
+// without hub rows keep the register count, hence the occupancy, of that);
+// C16 reads the 16-bit column layout.
+template <typename VT, bool HUBS, bool C16, bool POL = false, int B = 0>
 __device__ __forceinline__ void chunkRow(const SellView &m, int c, int k, int n, double *x, float *xf,
                                          unsigned long long pol) {
     const int lane = threadIdx.x & 31;
@@ -270,13 +289,14 @@ __device__ __forceinline__ void chunkRow(const SellView &m, int c, int k, int n,
         const int len = m.rowLen[r];
         const long long off = m.chunkOff[c] + lane;
         if (len >= 0) {
-            if constexpr (sizeof(VT) == 8) {
-                x[(size_t)(k + 1) * n + r] =
-                    sellRowD<U, LD>((const double *)m.val, m.col, off, len, x + (size_t)k * n, pol);
+            if constexpr (C16) {
+                const int4 b = m.chunkBase[c];
+                if (b.x >= 0)
+                    sellRow<VT, true, POL, B>(m, m.col16, off, off, b, len, r, k, n, x, xf, pol);
+                else
+                    sellRow<VT, false, POL, B>(m, m.wideCol, off, (long long)b.y + lane, b, len, r, k, n, x, xf, pol);
             } else {
-                const float v = sellRowF<VT, U, LD>((const VT *)m.val, m.col, off, len, xf + (size_t)k * n, pol);
-                xf[(size_t)(k + 1) * n + r] = v;
-                x[(size_t)(k + 1) * n + r] = floatToDoubleExact(v);
+                sellRow<VT, false, POL, B>(m, m.col, off, off, make_int4(0, 0, 0, 0), len, r, k, n, x, xf, pol);
             }
         }
     }
@@ -325,8 +345,18 @@ struct MpkArgs {
 // other one. A warp releases its previous run's flags only after fetching
 // the next run, when the stores they publish have drained; the release
 // still comes before any wait, so a warp never waits on itself.
-template <typename VT, bool HUBS, int U, int LD>
-__global__ void __launch_bounds__(kWarpThreads) kMpk(MpkArgs a) {
+// Code shape of kMpk per value type, the fastest measured on the 128^3
+// 27-point stencil (p = 8): with 16-bit columns FP64 in batches of 4
+// entries with at least 6 resident blocks per SM (38 registers), FP32
+// unbatched with 6, BF16 in batches of 8 with 8 (32 registers); with 32-bit
+// columns unbatched with 8.
+template <typename VT>
+constexpr int kMpkBatch = sizeof(VT) == 8 ? 4 : sizeof(VT) == 4 ? 0 : 8;
+template <typename VT, bool C16>
+constexpr int kMpkMinBlocks = C16 && sizeof(VT) != 2 ? 6 : 8;
+
+template <typename VT, bool HUBS, bool C16>
+__global__ void __launch_bounds__(kWarpThreads, (kMpkMinBlocks<VT, C16>)) kMpk(MpkArgs a) {
     const int lane = threadIdx.x & 31;
     const unsigned long long polKeep = l2Policy(a.hints ? 1 : 0), polDrop = l2Policy(a.hints ? 2 : 0);
     const int myDie = a.numDies > 1 ? a.smDie[smIndex()] : 0;
@@ -380,7 +410,7 @@ __global__ void __launch_bounds__(kWarpThreads) kMpk(MpkArgs a) {
             asm volatile("fence.acq_rel.gpu;" ::: "memory");
         }
         const unsigned long long pol = (h.w & 1) ? polDrop : polKeep;
-        for (int c = h.x; c < h.y; ++c) chunkRow<VT, HUBS, U, LD>(a.m, c, k, a.n, a.x, a.xf, pol);
+        for (int c = h.x; c < h.y; ++c) chunkRow<VT, HUBS, C16, true, kMpkBatch<VT>>(a.m, c, k, a.n, a.x, a.xf, pol);
         pc0 = h.x;
         pc1 = h.y;
         pk = k;
@@ -388,24 +418,24 @@ __global__ void __launch_bounds__(kWarpThreads) kMpk(MpkArgs a) {
 }
 
 // Plain y = A x on the SELL layout, no schedule: one warp per chunk.
-template <typename VT, bool HUBS>
+template <typename VT, bool HUBS, bool C16>
 __global__ void __launch_bounds__(kWarpThreads) kSpmvSell(SellView m, int numChunks, int n, int k, double *x,
                                                           float *xf) {
     const int nw = gridDim.x * (blockDim.x >> 5);
     for (int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < numChunks; c += nw)
-        chunkRow<VT, HUBS>(m, c, k, n, x, xf, 0);
+        chunkRow<VT, HUBS, C16>(m, c, k, n, x, xf, 0);
 }
 
 // One wavefront step of a triangular partition: one warp per (chunk,
 // power) item of the step. Every item's inputs were written by earlier
 // launches, so nothing waits.
-template <typename VT, bool HUBS>
+template <typename VT, bool HUBS, bool C16>
 __global__ void __launch_bounds__(kWarpThreads) kMpkStep(SellView m, const int *__restrict__ itemChunk,
                                                          const unsigned char *__restrict__ itemPow, int count, int n,
                                                          double *x, float *xf) {
     const int nw = gridDim.x * (blockDim.x >> 5);
     for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < count; i += nw)
-        chunkRow<VT, HUBS>(m, itemChunk[i], itemPow[i], n, x, xf, 0);
+        chunkRow<VT, HUBS, C16>(m, itemChunk[i], itemPow[i], n, x, xf, 0);
 }
 
 // x0 -> FP32 copy (rounding to nearest) for the reduced-precision path.
@@ -462,6 +492,82 @@ __global__ void kToSell(const int *__restrict__ rowPtr, const int *__restrict__ 
             sval[o] = VT(0);
             scol[o] = live ? r : chunkRowP[c];
         }
+    }
+}
+
+// 16-bit column layout. Every chunk's columns (hub rows excluded) are
+// covered by at most four windows of `window` rows (at most 2^14, the
+// offset field): the first starts at the smallest column, each next one at
+// the smallest column at least `window` beyond the previous start (the
+// greedy cover, which uses the fewest windows). A chunk that needs more
+// gets x = -1 and keeps 32-bit columns; unused windows get INT_MAX. One
+// block of 128 threads per chunk, a warp per row.
+__global__ void kChunkWindows(const int *__restrict__ rowPtr, const int *__restrict__ col,
+                              const int *__restrict__ chunkRowP, const int *__restrict__ rowLen, int numChunks,
+                              int window, int4 *__restrict__ base) {
+    const int c = blockIdx.x;
+    if (c >= numChunks) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ int wmin[4];
+    const int r0 = chunkRowP[c], r1 = chunkRowP[c + 1];
+    int b[5] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX, INT_MAX};
+    for (int w = 0; w < 5; ++w) {
+        const int prev = w > 0 ? b[w - 1] : 0;
+        int m = INT_MAX;
+        for (int r = r0 + warp; r < r1; r += 4) {
+            if (rowLen[r] < 0) continue;
+            for (int j = rowPtr[r] + lane; j < rowPtr[r + 1]; j += 32) {
+                const int cc = col[j];
+                if (w == 0 || cc - prev >= window) m = min(m, cc);
+            }
+        }
+        m = __reduce_min_sync(0xffffffffu, m);
+        if (lane == 0) wmin[warp] = m;
+        __syncthreads();
+        b[w] = min(min(wmin[0], wmin[1]), min(wmin[2], wmin[3]));
+        __syncthreads();
+        if (b[w] == INT_MAX) break;
+    }
+    if (threadIdx.x == 0) base[c] = b[4] != INT_MAX ? make_int4(-1, 0, 0, 0) : make_int4(b[0], b[1], b[2], b[3]);
+}
+
+// CRS -> SELL-32 copy with 16-bit columns (kChunkWindows' bases; chunks
+// with x = -1 write 32-bit columns to wideCol from slot y on). Padding
+// slots get value 0 and column entry 0 (wide chunks: the row's own
+// column); hub rows are padding here, their entries live in the hub copy.
+template <typename VT>
+__global__ void kToSell16(const int *__restrict__ rowPtr, const int *__restrict__ col, const VT *__restrict__ val,
+                          const long long *__restrict__ chunkOff, const int *__restrict__ chunkRowP,
+                          const int *__restrict__ chunkLen, const int4 *__restrict__ chunkBase, int numChunks,
+                          VT *__restrict__ sval, unsigned short *__restrict__ col16, int *__restrict__ wideCol) {
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= numChunks) return;
+    const int lane = threadIdx.x & 31;
+    const int r = chunkRowP[c] + lane;
+    const bool live = r < chunkRowP[c + 1];
+    const int s = live ? rowPtr[r] : 0;
+    int len = live ? rowPtr[r + 1] - s : 0;
+    if (len > kMpkHubRowLen) len = 0;
+    const int L = chunkLen[c];
+    const int4 b = chunkBase[c];
+    for (int j = 0; j < L; ++j) {
+        const long long o = chunkOff[c] + 32LL * j + lane;
+        unsigned short v = 0;
+        if (j < len) {
+            sval[o] = val[s + j];
+            const int cc = col[s + j];
+            if (b.x >= 0) {
+                const int sel = (cc >= b.y) + (cc >= b.z) + (cc >= b.w);
+                const int bs = sel == 0 ? b.x : sel == 1 ? b.y : sel == 2 ? b.z : b.w;
+                v = (unsigned short)((sel << 14) | (cc - bs));
+            } else {
+                wideCol[b.y + 32 * j + lane] = cc;
+            }
+        } else {
+            sval[o] = VT(0);
+            if (b.x < 0) wideCol[b.y + 32 * j + lane] = live ? r : chunkRowP[c];
+        }
+        col16[o] = v;
     }
 }
 
@@ -525,6 +631,25 @@ int residentBlocks(K kernel, int threads) {
 
 size_t valBytes(int vt) { return vt == RACE_VAL_F64 ? 8 : vt == RACE_VAL_F32 ? 4 : 2; }
 
+// The SELL copy of the plan's chunks (32- or 16-bit columns) and the
+// contiguous hub copies.
+template <typename VT>
+void copySell(const race_operands &ops, MpkPlan &p, const int *chunkLen, cudaStream_t s) {
+    const int C = p.numChunks, H = p.numHubs;
+    const int blocksC = ceilDiv(std::max(C, 1), 8);
+    if (p.col16)
+        kToSell16<VT><<<blocksC, 256, 0, s>>>(ops.rowPtr, ops.col, (const VT *)ops.val, p.chunkOff.p, p.chunkRow.p,
+                                              chunkLen, p.chunkBase.p, C, (VT *)p.sellVal.p, p.sellCol16.p,
+                                              p.wideCol.p);
+    else
+        kToSell<VT><<<blocksC, 256, 0, s>>>(ops.rowPtr, ops.col, (const VT *)ops.val, p.chunkOff.p, p.chunkRow.p,
+                                            chunkLen, C, (VT *)p.sellVal.p, p.sellCol.p);
+    if (H)
+        kGatherHubs<VT><<<ceilDiv(H, 8), 256, 0, s>>>(ops.rowPtr, ops.col, (const VT *)ops.val, p.hubRow.p,
+                                                      p.hubPtr.p, H, (VT *)p.hubVal.p, p.hubCol.p);
+    RACE_CUDA(cudaGetLastError());
+}
+
 }  // namespace
 
 // Builds the SELL-32 copy, the chunk dependency ranges and the wavefront
@@ -583,37 +708,47 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     plan->rowLen.upload(rowLen.data(), n, s);
     DevBuf<int> dChunkLen;
     dChunkLen.upload(chunkLen.data(), std::max(C, 1), s);
+    // 16-bit columns where the chunks' columns fit their windows: worth it
+    // while at most half of the slots stay 32-bit
+    plan->col16 = e.mpkCol16 && C > 0;
+    std::vector<int4> baseH;
+    if (plan->col16) {
+        plan->chunkBase.alloc(C);
+        kChunkWindows<<<C, 128, 0, s>>>(ops.rowPtr, ops.col, plan->chunkRow.p, plan->rowLen.p, C,
+                                        std::min(std::max(e.mpkColWindow, 1), kMpkColWindow), plan->chunkBase.p);
+        RACE_CUDA(cudaGetLastError());
+        baseH.resize(C);
+        RACE_CUDA(cudaMemcpyAsync(baseH.data(), plan->chunkBase.p, sizeof(int4) * C, cudaMemcpyDeviceToHost, s));
+        RACE_CUDA(cudaStreamSynchronize(s));
+        long long wide = 0;
+        for (int c = 0; c < C; ++c)
+            if (baseH[c].x < 0) {
+                baseH[c].y = (int)std::min<long long>(wide, INT_MAX);
+                wide += 32LL * chunkLen[c];
+                ++plan->wideChunks;
+            }
+        plan->wideSlots = wide;
+        plan->col16 = 2 * wide <= off && wide < INT_MAX;
+        if (plan->col16) {
+            plan->chunkBase.upload(baseH.data(), C, s);
+        } else {
+            plan->chunkBase.free();
+            plan->wideChunks = 0;
+            plan->wideSlots = 0;
+        }
+    }
     plan->sellVal.alloc(std::max<long long>(off, 1) * valBytes(ops.val_type));
-    plan->sellCol.alloc(std::max<long long>(off, 1));
+    if (plan->col16) {
+        plan->sellCol16.alloc(std::max<long long>(off, 1));
+        plan->wideCol.alloc(std::max<long long>(plan->wideSlots, 1));
+    } else {
+        plan->sellCol.alloc(std::max<long long>(off, 1));
+    }
     if (ops.val_type != RACE_VAL_F64) plan->xf.alloc((size_t)(power + 1) * n);
-    const int blocksC = ceilDiv(std::max(C, 1), 8);
-    const int blocksH = ceilDiv(std::max(H, 1), 8);
     switch (ops.val_type) {
-    case RACE_VAL_F64:
-        kToSell<double><<<blocksC, 256, 0, s>>>(ops.rowPtr, ops.col, (const double *)ops.val, plan->chunkOff.p,
-                                                plan->chunkRow.p, dChunkLen.p, C, (double *)plan->sellVal.p,
-                                                plan->sellCol.p);
-        if (H)
-            kGatherHubs<double><<<blocksH, 256, 0, s>>>(ops.rowPtr, ops.col, (const double *)ops.val, plan->hubRow.p,
-                                                        plan->hubPtr.p, H, (double *)plan->hubVal.p, plan->hubCol.p);
-        break;
-    case RACE_VAL_F32:
-        kToSell<float><<<blocksC, 256, 0, s>>>(ops.rowPtr, ops.col, (const float *)ops.val, plan->chunkOff.p,
-                                               plan->chunkRow.p, dChunkLen.p, C, (float *)plan->sellVal.p,
-                                               plan->sellCol.p);
-        if (H)
-            kGatherHubs<float><<<blocksH, 256, 0, s>>>(ops.rowPtr, ops.col, (const float *)ops.val, plan->hubRow.p,
-                                                       plan->hubPtr.p, H, (float *)plan->hubVal.p, plan->hubCol.p);
-        break;
-    case RACE_VAL_BF16:
-        kToSell<__nv_bfloat16><<<blocksC, 256, 0, s>>>(ops.rowPtr, ops.col, (const __nv_bfloat16 *)ops.val,
-                                                        plan->chunkOff.p, plan->chunkRow.p, dChunkLen.p, C,
-                                                        (__nv_bfloat16 *)plan->sellVal.p, plan->sellCol.p);
-        if (H)
-            kGatherHubs<__nv_bfloat16><<<blocksH, 256, 0, s>>>(ops.rowPtr, ops.col, (const __nv_bfloat16 *)ops.val,
-                                                               plan->hubRow.p, plan->hubPtr.p, H,
-                                                               (__nv_bfloat16 *)plan->hubVal.p, plan->hubCol.p);
-        break;
+    case RACE_VAL_F64: copySell<double>(ops, *plan, dChunkLen.p, s); break;
+    case RACE_VAL_F32: copySell<float>(ops, *plan, dChunkLen.p, s); break;
+    case RACE_VAL_BF16: copySell<__nv_bfloat16>(ops, *plan, dChunkLen.p, s); break;
     default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
     }
     RACE_CUDA(cudaGetLastError());
@@ -700,8 +835,6 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     plan->runHead.upload((const int4 *)head.data(), head.size() / 4, s);
     plan->runDep.upload((const int4 *)dep.data(), dep.size() / 4, s);
     plan->hints = e.mpkHints;
-    plan->unroll = e.mpkUnroll;
-    plan->loads = e.mpkLoads;
     plan->ctasPerSm = e.mpkCtasPerSm;
     RACE_CUDA(cudaStreamSynchronize(s));
     return plan;
@@ -730,68 +863,67 @@ bool chunkDependencyRanges(const int *rowPtr, const int *col, const std::vector<
 
 namespace {
 SellView viewOf(const MpkPlan &p) {
-    return SellView{p.sellVal.p, p.sellCol.p, p.chunkOff.p, p.chunkRow.p, p.rowLen.p,
-                    p.hubChunkStart.p, p.hubRow.p, p.hubPtr.p, p.hubVal.p, p.hubCol.p};
+    return SellView{p.sellVal.p,       p.sellCol.p, p.chunkOff.p, p.chunkRow.p, p.rowLen.p,
+                    p.hubChunkStart.p, p.hubRow.p,  p.hubPtr.p,   p.hubVal.p,   p.hubCol.p,
+                    p.chunkBase.p,     p.sellCol16.p, p.wideCol.p};
 }
 
-template <typename VT, bool HUBS, int U, int LD>
-void launchMpkU(const MpkArgs &a, int ctasPerSm, cudaStream_t s) {
-    static int resident = residentBlocks(kMpk<VT, HUBS, U, LD>, kWarpThreads);
+template <typename VT, bool HUBS, bool C16>
+void launchMpkK(const MpkArgs &a, int ctasPerSm, cudaStream_t s) {
+    static int resident = residentBlocks(kMpk<VT, HUBS, C16>, kWarpThreads);
     const int blocks = ctasPerSm > 0 ? std::min(resident, devSms() * ctasPerSm) : resident;
-    kMpk<VT, HUBS, U, LD><<<blocks, kWarpThreads, 0, s>>>(a);
-}
-
-template <typename VT, bool HUBS, int U>
-void launchMpkLd(const MpkArgs &a, int ld, int ctasPerSm, cudaStream_t s) {
-    if (ld == 0)
-        launchMpkU<VT, HUBS, U, 0>(a, ctasPerSm, s);
-    else if (ld == 1)
-        launchMpkU<VT, HUBS, U, 1>(a, ctasPerSm, s);
-    else
-        launchMpkU<VT, HUBS, U, 2>(a, ctasPerSm, s);
+    kMpk<VT, HUBS, C16><<<blocks, kWarpThreads, 0, s>>>(a);
 }
 
 template <typename VT>
 void launchMpk(const MpkArgs &a, const MpkPlan &p, cudaStream_t s) {
-    const bool hubs = p.numHubs > 0;
-    if (hubs) {
-        if (p.unroll == 8)
-            launchMpkLd<VT, true, 8>(a, p.loads, p.ctasPerSm, s);
-        else
-            launchMpkLd<VT, true, 4>(a, p.loads, p.ctasPerSm, s);
+    if (p.numHubs > 0) {
+        if (p.col16) launchMpkK<VT, true, true>(a, p.ctasPerSm, s);
+        else launchMpkK<VT, true, false>(a, p.ctasPerSm, s);
     } else {
-        if (p.unroll == 8)
-            launchMpkLd<VT, false, 8>(a, p.loads, p.ctasPerSm, s);
-        else
-            launchMpkLd<VT, false, 4>(a, p.loads, p.ctasPerSm, s);
+        if (p.col16) launchMpkK<VT, false, true>(a, p.ctasPerSm, s);
+        else launchMpkK<VT, false, false>(a, p.ctasPerSm, s);
     }
 }
 
-template <typename VT>
-void launchMpkSteps(const MpkPlan &p, int n, double *x, cudaStream_t s) {
+template <typename VT, bool HUBS, bool C16>
+void launchMpkStepsK(const MpkPlan &p, int n, double *x, cudaStream_t s) {
     const SellView v = viewOf(p);
     for (size_t st = 0; st + 1 < p.stepPtr.size(); ++st) {
         const int first = p.stepPtr[st], count = p.stepPtr[st + 1] - first;
         if (count == 0) continue;
         const int blocks = std::min(ceilDiv(count, kWarpThreads / 32), devSms() * 16);
-        if (p.numHubs > 0)
-            kMpkStep<VT, true><<<blocks, kWarpThreads, 0, s>>>(v, p.itemChunk.p + first, p.itemPow.p + first, count,
-                                                                n, x, p.xf.p);
-        else
-            kMpkStep<VT, false><<<blocks, kWarpThreads, 0, s>>>(v, p.itemChunk.p + first, p.itemPow.p + first, count,
-                                                                 n, x, p.xf.p);
+        kMpkStep<VT, HUBS, C16><<<blocks, kWarpThreads, 0, s>>>(v, p.itemChunk.p + first, p.itemPow.p + first,
+                                                                 count, n, x, p.xf.p);
     }
 }
 
 template <typename VT>
-void launchSpmvSell(const SellView &v, int numChunks, int n, int k, double *x, float *xf, bool hubs,
-                    cudaStream_t s) {
-    if (hubs) {
-        static int blocks = residentBlocks(kSpmvSell<VT, true>, kWarpThreads);
-        kSpmvSell<VT, true><<<blocks, kWarpThreads, 0, s>>>(v, numChunks, n, k, x, xf);
+void launchMpkSteps(const MpkPlan &p, int n, double *x, cudaStream_t s) {
+    if (p.numHubs > 0) {
+        if (p.col16) launchMpkStepsK<VT, true, true>(p, n, x, s);
+        else launchMpkStepsK<VT, true, false>(p, n, x, s);
     } else {
-        static int blocks = residentBlocks(kSpmvSell<VT, false>, kWarpThreads);
-        kSpmvSell<VT, false><<<blocks, kWarpThreads, 0, s>>>(v, numChunks, n, k, x, xf);
+        if (p.col16) launchMpkStepsK<VT, false, true>(p, n, x, s);
+        else launchMpkStepsK<VT, false, false>(p, n, x, s);
+    }
+}
+
+template <typename VT, bool HUBS, bool C16>
+void launchSpmvSellK(const SellView &v, int numChunks, int n, int k, double *x, float *xf, cudaStream_t s) {
+    static int blocks = residentBlocks(kSpmvSell<VT, HUBS, C16>, kWarpThreads);
+    kSpmvSell<VT, HUBS, C16><<<blocks, kWarpThreads, 0, s>>>(v, numChunks, n, k, x, xf);
+}
+
+template <typename VT>
+void launchSpmvSell(const MpkPlan &p, int n, int k, double *x, cudaStream_t s) {
+    const SellView v = viewOf(p);
+    if (p.numHubs > 0) {
+        if (p.col16) launchSpmvSellK<VT, true, true>(v, p.numChunks, n, k, x, p.xf.p, s);
+        else launchSpmvSellK<VT, true, false>(v, p.numChunks, n, k, x, p.xf.p, s);
+    } else {
+        if (p.col16) launchSpmvSellK<VT, false, true>(v, p.numChunks, n, k, x, p.xf.p, s);
+        else launchSpmvSellK<VT, false, false>(v, p.numChunks, n, k, x, p.xf.p, s);
     }
 }
 }  // namespace
@@ -830,13 +962,10 @@ void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
 void runSpmvSell(Engine &e, MpkPlan &plan, double *x, int n, int k) {
     cudaStream_t s = e.stream;
     if (plan.valType != RACE_VAL_F64 && k == 0) kToFloat<<<ceilDiv(n, 256), 256, 0, s>>>(x, plan.xf.p, n);
-    SellView v = viewOf(plan);
     switch (plan.valType) {
-    case RACE_VAL_F64: launchSpmvSell<double>(v, plan.numChunks, n, k, x, plan.xf.p, plan.numHubs > 0, s); break;
-    case RACE_VAL_F32: launchSpmvSell<float>(v, plan.numChunks, n, k, x, plan.xf.p, plan.numHubs > 0, s); break;
-    case RACE_VAL_BF16:
-        launchSpmvSell<__nv_bfloat16>(v, plan.numChunks, n, k, x, plan.xf.p, plan.numHubs > 0, s);
-        break;
+    case RACE_VAL_F64: launchSpmvSell<double>(plan, n, k, x, s); break;
+    case RACE_VAL_F32: launchSpmvSell<float>(plan, n, k, x, s); break;
+    case RACE_VAL_BF16: launchSpmvSell<__nv_bfloat16>(plan, n, k, x, s); break;
     default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
     }
     RACE_CUDA(cudaGetLastError());

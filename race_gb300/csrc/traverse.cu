@@ -288,8 +288,8 @@ Engine::Engine(int nrow, int nthreads, int dist_, const int *rowPtr, const int *
     if (const char *l = getenv("RACE_GPU_MPK_LAG")) mpkLag = std::max(0, atoi(l));
     if (const char *d = getenv("RACE_GPU_MPK_DIES")) mpkDieQueues = atoi(d) != 1;
     if (const char *h = getenv("RACE_GPU_MPK_HINTS")) mpkHints = atoi(h) ? 1 : 0;
-    if (const char *u = getenv("RACE_GPU_MPK_UNROLL")) mpkUnroll = atoi(u) == 8 ? 8 : 4;
-    if (const char *ld = getenv("RACE_GPU_MPK_LOADS")) mpkLoads = std::min(std::max(0, atoi(ld)), 2);
+    if (const char *c16 = getenv("RACE_GPU_MPK_COL16")) mpkCol16 = atoi(c16) != 0;
+    if (const char *w = getenv("RACE_GPU_MPK_COL_WINDOW")) mpkColWindow = std::min(std::max(1, atoi(w)), kMpkColWindow);
     if (const char *b = getenv("RACE_GPU_MPK_CTAS")) mpkCtasPerSm = std::max(0, atoi(b));
     // Coloring traversals (distance-1/-2) of ranges shorter than
     // hostTraverseBelow run on the host (direction-optimised BFS, a few

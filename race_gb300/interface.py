@@ -327,6 +327,14 @@ class Interface:
         SWEEP_GATHER (SpMV, SpMTV, SymmSpMV in one launch, bit-exact)."""
         self._check(lib().race_set_sweep_mode(self._h, int(mode)))
 
+    def getMpkLayout(self, funcId: int) -> dict:
+        """Device layout of a registered MPK function (race_get_mpk_layout)."""
+        v = [C.c_int() for _ in range(3)]
+        w = [C.c_longlong() for _ in range(2)]
+        self._check(lib().race_get_mpk_layout(self._h, int(funcId), *[C.byref(a) for a in v + w]))
+        return dict(chunks=v[0].value, col_bits=v[1].value, wide_chunks=v[2].value, sell_slots=w[0].value,
+                    matrix_bytes=w[1].value)
+
     def getSweepInfo(self, funcId: int, rev: bool = False) -> dict:
         v = [C.c_int() for _ in range(5)]
         self._check(lib().race_get_sweep_info(self._h, int(funcId), int(bool(rev)), *[C.byref(a) for a in v]))

@@ -337,6 +337,83 @@ def test_mpk_full_size_c2(golden):
     assert torch.equal(x, y)
 
 
+def _col_layout(P, gp, window, hub=HUB_ROW_LEN):
+    """Restatement of the MPK's column layout choice: chunks of <= 32 rows
+    inside the level groups gp, each chunk's columns (hub rows excluded)
+    covered greedily by windows of `window` rows; chunks needing more than
+    four windows keep 32-bit columns, and the plan stays 32-bit when those
+    chunks hold more than half of the SELL slots. Returns (chunks, chunks
+    with 32-bit columns, column bits)."""
+    lens = np.diff(P.row_ptr)
+    cr = [0]
+    for g in range(len(gp) - 1):
+        for r in range(gp[g], gp[g + 1], 32):
+            cr.append(min(gp[g + 1], r + 32))
+    slots = wide = wide_slots = 0
+    for c in range(len(cr) - 1):
+        rows = [r for r in range(cr[c], cr[c + 1]) if lens[r] <= hub]
+        L = int(max((lens[r] for r in rows), default=0))
+        slots += 32 * L
+        v = np.unique(np.concatenate([P.col[P.row_ptr[r]:P.row_ptr[r + 1]] for r in rows] or [np.zeros(0, int)]))
+        i = w = 0
+        while i < len(v):
+            w += 1
+            i = int(np.searchsorted(v, v[i] + window, "left"))
+        if w > 4:
+            wide += 1
+            wide_slots += 32 * L
+    return (len(cr) - 1, 0, 32) if 2 * wide_slots > slots else (len(cr) - 1, wide, 16)
+
+
+def test_mpk_column_layouts(monkeypatch):
+    """The 16-bit column layout (per chunk four window bases, per entry a
+    2-bit window and a 14-bit offset) and the 32-bit one give identical
+    powers: FP64 equal to the oracle's p sequential fma SpMVs, FP32 equal to
+    the 32-bit layout's, for the MPK and the plain SpMV on the layout. Small
+    windows force plans that mix 16-bit chunks with chunks that keep 32-bit
+    columns (window 512 on the 40^3 stencil) and plans that fall back to 32
+    bits (window 64); the reported layout matches the restatement."""
+    A = matgen.stencil3d_27pt(40)
+    p = 4
+    x0 = matgen.uniform_vector(A.n, 0)
+    ref32 = None
+    mixed = False
+    for col16, window in [("0", None), ("1", None), ("1", "512"), ("1", "64")]:
+        monkeypatch.setenv("RACE_GPU_MPK_COL16", col16)
+        if window:
+            monkeypatch.setenv("RACE_GPU_MPK_COL_WINDOW", window)
+        else:
+            monkeypatch.delenv("RACE_GPU_MPK_COL_WINDOW", raising=False)
+        rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+        assert rc.RACEColor(p, 2e6) == 0
+        P = A.permuted(rc.getPerm(), rc.getInvPerm())
+        Y = orc.mpk_plain(P, x0, p)
+        outs = []
+        for dtype in (torch.float64, torch.float32):
+            x = torch.zeros((p + 1) * A.n, dtype=torch.float64, device="cuda")
+            x[: A.n] = torch.tensor(x0, device="cuda")
+            fid = rc.registerFunction(ri.MPK, ri.Operands(_upload(P, dtype), x), power=p)
+            assert fid >= 0
+            lay = rc.getMpkLayout(fid)
+            want = (lay["chunks"], 0, 32) if col16 == "0" else _col_layout(P, rc.getPowerGroups(),
+                                                                             int(window or 16384))
+            assert (lay["chunks"], lay["wide_chunks"], lay["col_bits"]) == want, (col16, window, lay)
+            mixed |= lay["col_bits"] == 16 and 0 < lay["wide_chunks"] < lay["chunks"]
+            assert rc.executeFunction(fid) == 0
+            got = x.clone()
+            x[A.n:] = 0
+            for kk in range(p):
+                rc.spmvPowerLayout(fid, kk)
+            torch.cuda.synchronize()
+            assert torch.equal(x, got)  # plain SpMVs on the layout == MPK
+            outs.append(got.cpu().numpy().reshape(p + 1, A.n))
+        np.testing.assert_array_equal(outs[0], Y)
+        if ref32 is None:
+            ref32 = outs[1]
+        np.testing.assert_array_equal(outs[1], ref32)
+    assert mixed
+
+
 @pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-5), (torch.bfloat16, 5e-2)])
 def test_mpk_reduced_precision_error(mats, dtype, tol):
     """FP32/BF16 value storage with FP32 accumulation: error against the FP64
