@@ -215,8 +215,9 @@ def run_reference(args, rank, world):
 
 def run_profile_case(args):
     """Short, fixed sequences of launches for ncu.
-    mpk: --steps MPK calls, then --steps rounds of the p plain SpMVs on the
-    same SELL-32 layout (27-point stencil, --grid^3).
+    mpk: --steps MPK calls of the wavefront kernel, then --steps rounds of
+    the p plain SpMVs on the same SELL-32 layout (27-point stencil,
+    --grid^3).
     batch: the batched block MPK of --batch-count matrices, --steps graph
     replays, then --steps rounds of the plain per-matrix launches.
     symmgs: --steps forward+backward GS sweeps (FP32 values) on the
@@ -274,6 +275,7 @@ def run_profile_case(args):
     x[:A.n] = torch.tensor(matgen.uniform_vector(A.n, 0), device="cuda")
     fid = rc.registerFunction(ri.MPK, ri.Operands(dm, x), power=POWER)
     assert fid >= 0
+    rc.setMpkSchedule(fid, "wavefront")  # the persistent kernel, not the timed choice
     for _ in range(args.steps):
         assert rc.executeFunction(fid) == 0
     for _ in range(args.steps):
@@ -415,6 +417,17 @@ def main():
                    "effective_gbs": POWER * spmv_bytes(n, nnz) / (ms_b * 1e-3) / 1e9,
                    "bit_exact_vs_plain_chain": blocked_exact}
 
+    # both MPK schedules of each function, forced, then the default (auto:
+    # the faster of the two, timed at the first call, inside the warm-up)
+    schedules = {}
+    for name, fid, fn in (("f64", f64, mpk64), ("f32", f32, mpk32)):
+        sched = {}
+        for sc in ("wavefront", "sweeps"):
+            rc.setMpkSchedule(fid, sc)
+            sched[f"{sc}_ms"] = timed(fn, args.steps)
+            assert rc.getStatus() == 0
+        rc.setMpkSchedule(fid, "auto")
+        schedules[name] = sched
     with ClockSampler(local) as clk:
         ms64 = timed(mpk64, args.steps)
     clocks = clk.summary()
@@ -422,6 +435,8 @@ def main():
     ms32 = timed(mpk32, args.steps)
     assert rc.getStatus() == 0
     ms_plain = timed(plain64, args.steps)
+    for name, fid in (("f64", f64), ("f32", f32)):
+        schedules[name]["auto_chose"] = rc.getMpkLayout(fid)["schedule"]
 
     # End to end through the public API with host buffers, every step: the
     # step's x0 from pinned host memory to the device, the MPK, all p powers
@@ -532,6 +547,7 @@ def main():
                           "note": "hbm_frac from the bytes p SpMVs move on the registered layout "
                                   f"({plain_bytes} B: p x (layout matrix bytes + x_k + x_k+1))"},
             "mpk_layout": layout,
+            "mpk_schedules": schedules,
             "symmgs_ir": symmgs,
             "batched_mpk": batched,
             "mlp_tuner": tuned,
@@ -552,7 +568,7 @@ def mpk_kernel_info():
     _lib.check(_lib.lib().race_device_dies(ctypes.byref(nd), smd, 4096, ctypes.byref(ns)))
     env = {k: v for k, v in os.environ.items() if k.startswith("RACE_GPU_MPK")}
     return {"order": "chunk-level wavefront, per-die run queues", "lag_chunks": int(env.get("RACE_GPU_MPK_LAG", 32768)),
-            "chunks_per_run": int(env.get("RACE_GPU_MPK_RUN", 2)), "l2_dies": nd.value,
+            "chunks_per_run": int(env.get("RACE_GPU_MPK_RUN", 4)), "l2_dies": nd.value,
             "sms_per_die": [sum(1 for i in range(ns.value) if smd[i] == d) for d in range(nd.value)],
             "env_overrides": env}
 

@@ -221,9 +221,24 @@ int race_spmv_power_layout(race_engine *e, int func_id, int k);
  * the chunk's four window bases; 32: plain indices), the chunks that keep
  * 32-bit columns in the 16-bit layout, the SELL slots with padding, and the
  * bytes of the matrix arrays one power reads (values, columns, row lengths,
- * chunk tables, hub copies). */
+ * chunk tables, hub copies), and the schedule that runs (see
+ * race_set_mpk_schedule). */
 int race_get_mpk_layout(race_engine *e, int func_id, int *numChunks, int *colBits, int *wideChunks,
-                        long long *sellSlots, long long *matrixBytes);
+                        long long *sellSlots, long long *matrixBytes, int *schedule);
+
+/* Schedule of a registered RACE_K_MPK function (no counterpart in the
+ * reference, whose executor always runs the level-group wavefront):
+ * RACE_MPK_WAVEFRONT runs all powers in one persistent kernel in the
+ * chunk-level wavefront order; RACE_MPK_SWEEPS runs p plain SpMV launches on
+ * the same layout (no level blocking); RACE_MPK_AUTO (the default) times
+ * both once, at the function's first call on a stream that is not being
+ * captured (that call synchronises), and keeps the faster; while capturing
+ * it runs the wavefront for FP64 values and the sweeps otherwise. All give
+ * bit-identical powers. Triangular partitions (mtxType L/U) always run
+ * their own step-by-step schedule. race_get_mpk_layout's *schedule reports
+ * the schedule that runs (RACE_MPK_AUTO before the first timed call). */
+enum { RACE_MPK_AUTO = 0, RACE_MPK_WAVEFRONT = 1, RACE_MPK_SWEEPS = 2 };
+int race_set_mpk_schedule(race_engine *e, int func_id, int schedule);
 
 /* Matrix power without any device allocation. No counterpart in the
  * reference (its executor runs on the host and allocates freely).
@@ -424,7 +439,10 @@ int race_wave_plan(int kernel, int n, const int *rowPtr, const int *col, const i
  * cap >= *numRuns, per run head[4] (first chunk, end chunk, power, flags),
  * dep[8] (four chunk intervals that must be complete at the previous
  * power) and rank (its position in the global order; may be NULL), and
- * dieStart[3] (die d's queue is runs dieStart[d] .. dieStart[d+1]-1). No
+ * dieStart[3] (die d's queue is runs dieStart[d] .. dieStart[d+1]-1). The
+ * dependency ranges are first widened to the kernel's completion blocks
+ * (at most 16 consecutive chunks inside one level group of chunkGroup, or
+ * by index alone when chunkGroup is NULL), as the engine does. No
  * counterpart in the reference; exposed for tests. */
 int race_mpk_issue_order(const int *depRange, const int *chunkGroup, const int *chunkDie, int numChunks, int power,
                          int order, int stride, int segLen, int runLen, int lag, int *head, int *dep, int *rank,

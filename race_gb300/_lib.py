@@ -29,7 +29,8 @@ EXPORTS = [
     "race_get_perm", "race_get_num_threads", "race_get_efficiency", "race_get_max_stage_depth", "race_get_zone_tree",
     "race_get_phases", "race_get_power_groups", "race_register_function", "race_execute_function",
     "race_execute_function_async", "race_get_status", "race_set_sweep_mode", "race_get_sweep_info", "race_set_power",
-    "race_get_power", "race_spmv_plain", "race_spmv_power_layout", "race_get_mpk_layout", "race_mpk_noalloc",
+    "race_get_power", "race_spmv_plain", "race_spmv_power_layout", "race_get_mpk_layout", "race_set_mpk_schedule",
+    "race_mpk_noalloc",
     "race_symmgs_ir", "race_lb_balance", "race_flatten_zone_tree", "race_last_error", "race_register_mpk_block",
     "race_batch_create", "race_batch_destroy", "race_batch_add", "race_batch_prepare", "race_batch_execute",
     "race_batch_graph_launch", "race_batch_get_status", "race_batch_info", "race_batch_last_error",
@@ -92,7 +93,8 @@ def lib():
             "race_get_power_tree": [vp, vp, i, ip],
             "race_set_sweep_mode": [vp, i], "race_get_sweep_info": [vp, i, i, ip, ip, ip, ip, ip],
             "race_spmv_plain": [vp, i, vp, vp, vp, vp, vp], "race_spmv_power_layout": [vp, i, i],
-            "race_get_mpk_layout": [vp, i, ip, ip, ip, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
+            "race_get_mpk_layout": [vp, i, ip, ip, ip, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), ip],
+            "race_set_mpk_schedule": [vp, i, i],
             "race_mpk_noalloc": [i, vp, vp, vp, vp, vp, i, i, vp, vp],
             "race_symmgs_ir": [vp, i, i, vp, vp, vp, vp, vp, C.c_double, i, i, ip, C.POINTER(C.c_double)],
             "race_lb_balance": [vp, vp, i, i, C.c_double, i, i, i, i, vp, i, ip],

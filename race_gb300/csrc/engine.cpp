@@ -445,9 +445,9 @@ int race_get_sweep_info(race_engine *e, int func_id, int rev, int *numWaves, int
 }
 
 int race_get_mpk_layout(race_engine *e, int func_id, int *numChunks, int *colBits, int *wideChunks,
-                        long long *sellSlots, long long *matrixBytes) {
+                        long long *sellSlots, long long *matrixBytes, int *schedule) {
     if (!e || func_id < 0 || func_id >= (int)e->eng->funcs.size() || !numChunks || !colBits || !wideChunks ||
-        !sellSlots || !matrixBytes)
+        !sellSlots || !matrixBytes || !schedule)
         return RACE_ERR_INVALID_ARG;
     const race::FuncEntry &f = e->eng->funcs[func_id];
     if (f.kernel != RACE_K_MPK || !f.mpk) return RACE_ERR_INVALID_ARG;
@@ -461,6 +461,18 @@ int race_get_mpk_layout(race_engine *e, int func_id, int *numChunks, int *colBit
                                                 : 4 * p.sellSlots) +
                    4LL * (long long)p.rowLen.n + 12LL * p.numChunks + 4LL * (long long)p.hubRow.n +
                    (vb + 4) * (long long)p.hubCol.n;
+    *schedule = p.schedule != RACE_MPK_AUTO ? p.schedule : p.chosen;
+    return RACE_SUCCESS;
+}
+
+int race_set_mpk_schedule(race_engine *e, int func_id, int schedule) {
+    if (!e || func_id < 0 || func_id >= (int)e->eng->funcs.size() || schedule < RACE_MPK_AUTO ||
+        schedule > RACE_MPK_SWEEPS)
+        return RACE_ERR_INVALID_ARG;
+    race::FuncEntry &f = e->eng->funcs[func_id];
+    if (f.kernel != RACE_K_MPK || !f.mpk) return RACE_ERR_INVALID_ARG;
+    f.mpk->schedule = schedule;
+    f.mpk->chosen = 0;
     return RACE_SUCCESS;
 }
 
@@ -768,11 +780,13 @@ int race_mpk_issue_order(const int *depRange, const int *chunkGroup, const int *
         if (chunkDie && chunkDie[c] != 0 && chunkDie[c] != 1) return RACE_ERR_INVALID_ARG;
     }
     return guard(nullptr, [&] {
-        const std::vector<int> dr(depRange, depRange + 6 * (size_t)numChunks);
+        const std::vector<int> cg =
+            chunkGroup ? std::vector<int>(chunkGroup, chunkGroup + numChunks) : std::vector<int>();
+        const std::vector<int> dr = race::widenDepsToBlocks(
+            std::vector<int>(depRange, depRange + 6 * (size_t)numChunks), race::mpkFlagBlocks(numChunks, cg));
         const std::vector<int> cd = chunkDie ? std::vector<int>(chunkDie, chunkDie + numChunks) : std::vector<int>();
         const race::MpkOrder o =
-            order == 1 ? race::mpkGroupOrder(dr, std::vector<int>(chunkGroup, chunkGroup + numChunks), numGroups,
-                                             power, stride == 1 ? 1 : 2, segLen)
+            order == 1 ? race::mpkGroupOrder(dr, cg, numGroups, power, stride == 1 ? 1 : 2, segLen)
                        : race::mpkRunOrder(dr, numChunks, power, segLen, runLen, lag, cd);
         *numRuns = o.numRuns();
         if (head && dep && cap >= o.numRuns()) {

@@ -59,14 +59,18 @@ struct MpkPlan {
     DevBuf<float> xf;           // (power+1)*n FP32 powers (reduced-precision storage)
     DevBuf<int> depRange;       // numChunks*6: chunks read in the previous/own/next group
     int numRuns = 0;            // runs of the persistent kernel (mpk_order.h)
-    DevBuf<int4> runHead;       // numRuns: first chunk, end chunk, power, flags
-    DevBuf<int4> runDep;        // 2 per run: four chunk intervals read at the previous power
+    DevBuf<int4> runHead;       // numRuns: first chunk, end chunk, power, flags | first block << 1
+    DevBuf<int4> runDep;        // 2 per run: four block intervals read at the previous power
     int numDies = 1;            // run queues, one per L2 die (dies.h): die d's are dieStart[d] .. dieStart[d+1]-1
     int dieStart[3] = {0, 0, 0};
     const int *smDie = nullptr; // device table: die of every SM
     int hints = 1;              // L2 eviction hints on the matrix loads
+    int schedule = 0;           // RACE_MPK_AUTO / WAVEFRONT / SWEEPS
+    int chosen = 0;             // the schedule AUTO chose (0: not yet)
     int ctasPerSm = 0;          // kMpk blocks per SM (0: as many as fit)
-    DevBuf<int> done;           // power * numChunks completion flags
+    int numBlocks = 0;          // completion blocks (mpk_order.h mpkFlagBlocks)
+    DevBuf<int> blockStart;     // numBlocks+1
+    DevBuf<int> done;           // power * numBlocks: chunks complete per block
     DevBuf<int> ticket;         // next run of each die queue
     DevBuf<int> status;         // 1: device status word
     // Triangular partitions (mtxType L/U): a row may read any earlier group,
@@ -207,12 +211,14 @@ class Engine {
     int mpkOrder = 0;
     int mpkStride = 2;
     int mpkSplit = 0;
-    int mpkRun = 2;
+    int mpkRun = 4;
     int mpkLag = 32768;
     bool mpkDieQueues = true;
     int mpkHints = 1;
     int mpkCtasPerSm = 0;
     bool mpkCol16 = true;
+    // the default schedule of new MPK functions (RACE_MPK_*)
+    int mpkSchedule = 0;
     int mpkColWindow = kMpkColWindow;
     // the MPK partition's leaf tree (the root alone without hopeless regions)
     std::vector<MpkLeaf> powerTree;

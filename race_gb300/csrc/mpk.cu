@@ -83,42 +83,6 @@ __device__ __forceinline__ unsigned long long l2Policy(int kind) {
     return p;
 }
 
-// Matrix loads of the wavefront kernel with an L2 eviction policy.
-__device__ __forceinline__ double ldPol(const double *a, unsigned long long pol) {
-    double v;
-    asm("ld.global.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
-    return v;
-}
-__device__ __forceinline__ float ldPol(const float *a, unsigned long long pol) {
-    float v;
-    asm("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
-    return v;
-}
-__device__ __forceinline__ __nv_bfloat16 ldPol(const __nv_bfloat16 *a, unsigned long long pol) {
-    unsigned short v;
-    asm("ld.global.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(a), "l"(pol));
-    return __ushort_as_bfloat16(v);
-}
-__device__ __forceinline__ int ldPol(const int *a, unsigned long long pol) {
-    int v;
-    asm("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
-    return v;
-}
-__device__ __forceinline__ unsigned short ldPol(const unsigned short *a, unsigned long long pol) {
-    unsigned short v;
-    asm("ld.global.L2::cache_hint.b16 %0, [%1], %2;" : "=h"(v) : "l"(a), "l"(pol));
-    return v;
-}
-
-// Matrix entry loads: POL false plain loads, true with an L2 policy.
-template <bool POL, typename T>
-__device__ __forceinline__ T ldEntry(const T *a, unsigned long long pol) {
-    if constexpr (POL)
-        return ldPol(a, pol);
-    else
-        return *a;
-}
-
 template <typename VT>
 __device__ __forceinline__ float toF(VT v);
 template <>
@@ -165,90 +129,139 @@ struct SellView {
     const int *wideCol;
 };
 
-// Column j of the lane's row: a stored 32-bit index (C16 false), or the
-// base of window v >> 14 plus the low 14 bits of the stored entry v.
+// Vector loads of one entry group (four consecutive entries of a lane's
+// row), with an L2 policy (POL) or plain.
+template <bool POL>
+__device__ __forceinline__ double2 ldVec(const double2 *a, unsigned long long pol) {
+    double2 v;
+    if constexpr (POL)
+        asm("ld.global.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(a), "l"(pol));
+    else
+        v = *a;
+    return v;
+}
+template <bool POL>
+__device__ __forceinline__ float4 ldVec(const float4 *a, unsigned long long pol) {
+    float4 v;
+    if constexpr (POL)
+        asm("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+            : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+            : "l"(a), "l"(pol));
+    else
+        v = *a;
+    return v;
+}
+template <bool POL>
+__device__ __forceinline__ uint2 ldVec(const uint2 *a, unsigned long long pol) {
+    uint2 v;
+    if constexpr (POL)
+        asm("ld.global.L2::cache_hint.v2.b32 {%0, %1}, [%2], %3;" : "=r"(v.x), "=r"(v.y) : "l"(a), "l"(pol));
+    else
+        v = *a;
+    return v;
+}
+template <bool POL>
+__device__ __forceinline__ int4 ldVec(const int4 *a, unsigned long long pol) {
+    int4 v;
+    if constexpr (POL)
+        asm("ld.global.L2::cache_hint.v4.b32 {%0, %1, %2, %3}, [%4], %5;"
+            : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+            : "l"(a), "l"(pol));
+    else
+        v = *a;
+    return v;
+}
+
+// Column of a stored 16-bit entry v: the base of window v >> 14 plus the
+// low 14 bits.
+__device__ __forceinline__ int col16Of(unsigned v, int4 b) {
+    const int base = (v & 0x8000u) ? ((v & 0x4000u) ? b.w : b.z) : ((v & 0x4000u) ? b.y : b.x);
+    return base + (int)(v & 0x3fffu);
+}
+
+// The four columns of an entry group at element offset o: one 8-byte load
+// of 16-bit entries (C16) or one 16-byte load of 32-bit indices.
 template <bool C16, bool POL>
-__device__ __forceinline__ int sellColumn(const void *col, long long off, int j, int4 b, unsigned long long pol) {
+__device__ __forceinline__ int4 groupCols(const void *col, long long o, int4 b, unsigned long long pol) {
     if constexpr (C16) {
-        const unsigned v = ldEntry<POL>((const unsigned short *)col + off + 32LL * j, pol);
-        const int base = (v & 0x8000u) ? ((v & 0x4000u) ? b.w : b.z) : ((v & 0x4000u) ? b.y : b.x);
-        return base + (int)(v & 0x3fffu);
+        const uint2 w = ldVec<POL>((const uint2 *)((const unsigned short *)col + o), pol);
+        return make_int4(col16Of(w.x & 0xffffu, b), col16Of(w.x >> 16, b), col16Of(w.y & 0xffffu, b),
+                         col16Of(w.y >> 16, b));
     } else {
-        return ldEntry<POL>((const int *)col + off + 32LL * j, pol);
+        return ldVec<POL>((const int4 *)((const int *)col + o), pol);
     }
 }
 
-// One row of a SELL-32 chunk, FP64 storage: the lane's fma chain over its
-// entries in CRS order (values at voff + 32 j, columns at coff + 32 j).
-// B > 0 (16-bit columns only) issues the row in batches of B entries: B
-// column and value loads, then B gathers of x, then B fmas in entry order
-// (the same chain; the code the compiler schedules differs, and which one
-// is faster depends on the kernel and value type).
-template <bool C16, bool POL, int B>
-__device__ __forceinline__ double sellRowD(const double *__restrict__ val, long long voff, const void *col,
-                                           long long coff, int4 b, int len, const double *x,
-                                           unsigned long long pol) {
-    double t = 0.0;
-    int j = 0;
-    if constexpr (C16 && B > 0) {
-        for (; j + B <= len; j += B) {
-            int cc[B];
-            double vv[B], xx[B];
-#pragma unroll
-            for (int i = 0; i < B; ++i) {
-                cc[i] = sellColumn<C16, POL>(col, coff, j + i, b, pol);
-                vv[i] = ldEntry<POL>(val + voff + 32LL * (j + i), pol);
-            }
-#pragma unroll
-            for (int i = 0; i < B; ++i) xx[i] = x[cc[i]];
-#pragma unroll
-            for (int i = 0; i < B; ++i) t = fma(vv[i], xx[i], t);
-        }
-    }
-#pragma unroll 4
-    for (; j < len; ++j)
-        t = fma(ldEntry<POL>(val + voff + 32LL * j, pol), x[sellColumn<C16, POL>(col, coff, j, b, pol)], t);
-    return t;
+// The four values of an entry group at element offset o (FP32/BF16 as
+// floats).
+template <bool POL>
+__device__ __forceinline__ void groupVals(const double *val, long long o, double v[4], unsigned long long pol) {
+    const double2 a = ldVec<POL>((const double2 *)(val + o), pol), c = ldVec<POL>((const double2 *)(val + o + 2), pol);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = c.x;
+    v[3] = c.y;
 }
-// FP32/BF16 storage with an FP32 vector.
-template <typename VT, bool C16, bool POL, int B>
-__device__ __forceinline__ float sellRowF(const VT *__restrict__ val, long long voff, const void *col, long long coff,
-                                          int4 b, int len, const float *x, unsigned long long pol) {
-    float t = 0.0f;
-    int j = 0;
-    if constexpr (C16 && B > 0) {
-        for (; j + B <= len; j += B) {
-            int cc[B];
-            float vv[B], xx[B];
-#pragma unroll
-            for (int i = 0; i < B; ++i) {
-                cc[i] = sellColumn<C16, POL>(col, coff, j + i, b, pol);
-                vv[i] = toF<VT>(ldEntry<POL>(val + voff + 32LL * (j + i), pol));
-            }
-#pragma unroll
-            for (int i = 0; i < B; ++i) xx[i] = x[cc[i]];
-#pragma unroll
-            for (int i = 0; i < B; ++i) t = fmaf(vv[i], xx[i], t);
+template <bool POL>
+__device__ __forceinline__ void groupVals(const float *val, long long o, float v[4], unsigned long long pol) {
+    const float4 a = ldVec<POL>((const float4 *)(val + o), pol);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = a.z;
+    v[3] = a.w;
+}
+template <bool POL>
+__device__ __forceinline__ void groupVals(const __nv_bfloat16 *val, long long o, float v[4],
+                                          unsigned long long pol) {
+    const uint2 a = ldVec<POL>((const uint2 *)(val + o), pol);
+    v[0] = __uint_as_float(a.x << 16);
+    v[1] = __uint_as_float(a.x & 0xffff0000u);
+    v[2] = __uint_as_float(a.y << 16);
+    v[3] = __uint_as_float(a.y & 0xffff0000u);
+}
+
+// One row of a SELL-32 chunk: the lane's fma chain over its entries in CRS
+// order. Entry j of the lane sits at element voff + 32 (j - j % 4) + j % 4
+// (voff = the chunk's offset + 4 lane), its column at the same place from
+// coff: every group of four entries is one or two vector loads of values
+// and one of columns. A last partial group computes only the row's entries
+// (its padding slots are loaded, never used). AT is the accumulation type:
+// FP64 for FP64 values, FP32 otherwise.
+template <typename VT, typename AT, bool C16, bool POL>
+__device__ __forceinline__ AT sellRowAcc(const VT *__restrict__ val, long long voff, const void *col, long long coff,
+                                         int4 b, int len, const AT *x, unsigned long long pol) {
+    AT t = AT(0);
+    for (int j = 0; j < len; j += 4) {
+        AT v[4];
+        groupVals<POL>(val, voff + 32LL * j, v, pol);
+        const int4 c = groupCols<C16, POL>(col, coff + 32LL * j, b, pol);
+        if (len - j >= 4) {
+            const AT x0 = x[c.x], x1 = x[c.y], x2 = x[c.z], x3 = x[c.w];
+            t = fma(v[0], x0, t);
+            t = fma(v[1], x1, t);
+            t = fma(v[2], x2, t);
+            t = fma(v[3], x3, t);
+        } else {
+            t = fma(v[0], x[c.x], t);
+            if (len - j > 1) t = fma(v[1], x[c.y], t);
+            if (len - j > 2) t = fma(v[2], x[c.z], t);
         }
     }
-#pragma unroll 4
-    for (; j < len; ++j)
-        t = fmaf(toF<VT>(ldEntry<POL>(val + voff + 32LL * j, pol)), x[sellColumn<C16, POL>(col, coff, j, b, pol)],
-                 t);
     return t;
 }
 
 // Row r at power k -> k+1 from its SELL entries; FP32/BF16 results also go
 // to the FP64 powers through the exact conversion.
-template <typename VT, bool C16, bool POL, int B>
+template <typename VT, bool C16, bool POL>
 __device__ __forceinline__ void sellRow(const SellView &m, const void *col, long long voff, long long coff, int4 b,
                                         int len, int r, int k, int n, double *x, float *xf,
                                         unsigned long long pol) {
     if constexpr (sizeof(VT) == 8) {
-        x[(size_t)(k + 1) * n + r] =
-            sellRowD<C16, POL, B>((const double *)m.val, voff, col, coff, b, len, x + (size_t)k * n, pol);
+        x[(size_t)(k + 1) * n + r] = sellRowAcc<double, double, C16, POL>((const double *)m.val, voff, col, coff, b,
+                                                                          len, x + (size_t)k * n, pol);
     } else {
-        const float v = sellRowF<VT, C16, POL, B>((const VT *)m.val, voff, col, coff, b, len, xf + (size_t)k * n, pol);
+        const float v =
+            sellRowAcc<VT, float, C16, POL>((const VT *)m.val, voff, col, coff, b, len, xf + (size_t)k * n, pol);
         xf[(size_t)(k + 1) * n + r] = v;
         x[(size_t)(k + 1) * n + r] = floatToDoubleExact(v);
     }
@@ -280,23 +293,23 @@ __device__ __forceinline__ AT hubSum(const SellView &m, int h, const AT *x) {
 // lanes of a warp. HUBS = false compiles the plain SELL row only (plans
 // without hub rows keep the register count, hence the occupancy, of that);
 // C16 reads the 16-bit column layout.
-template <typename VT, bool HUBS, bool C16, bool POL = false, int B = 0>
+template <typename VT, bool HUBS, bool C16, bool POL = false>
 __device__ __forceinline__ void chunkRow(const SellView &m, int c, int k, int n, double *x, float *xf,
                                          unsigned long long pol) {
     const int lane = threadIdx.x & 31;
     const int r = m.chunkRow[c] + lane;
     if (r < m.chunkRow[c + 1]) {
         const int len = m.rowLen[r];
-        const long long off = m.chunkOff[c] + lane;
+        const long long off = m.chunkOff[c] + 4 * lane;
         if (len >= 0) {
             if constexpr (C16) {
                 const int4 b = m.chunkBase[c];
                 if (b.x >= 0)
-                    sellRow<VT, true, POL, B>(m, m.col16, off, off, b, len, r, k, n, x, xf, pol);
+                    sellRow<VT, true, POL>(m, m.col16, off, off, b, len, r, k, n, x, xf, pol);
                 else
-                    sellRow<VT, false, POL, B>(m, m.wideCol, off, (long long)b.y + lane, b, len, r, k, n, x, xf, pol);
+                    sellRow<VT, false, POL>(m, m.wideCol, off, (long long)b.y + 4 * lane, b, len, r, k, n, x, xf, pol);
             } else {
-                sellRow<VT, false, POL, B>(m, m.col, off, off, make_int4(0, 0, 0, 0), len, r, k, n, x, xf, pol);
+                sellRow<VT, false, POL>(m, m.col, off, off, make_int4(0, 0, 0, 0), len, r, k, n, x, xf, pol);
             }
         }
     }
@@ -321,10 +334,13 @@ struct MpkArgs {
     double *x;      // caller's (p+1)*n powers
     float *xf;      // internal FP32 powers (reduced-precision storage only)
     int n;
-    const int4 *runHead;       // numRuns: first chunk, end chunk, power k, flags (bit 0: last power of the segment)
-    const int4 *runDep;        // 2 per run: four chunk intervals [lo,hi] read at power k-1
-    int numChunks;
-    int *done;                 // power * numChunks completion flags
+    // numRuns: first chunk, end chunk, power k, flags (bit 0: last power of
+    // the segment; bits 1-31: the completion block of the first chunk)
+    const int4 *runHead;
+    const int4 *runDep;        // 2 per run: four block intervals [lo,hi] read at power k-1
+    int numBlocks;
+    const int *blockStart;     // numBlocks+1: first chunk of each completion block
+    int *done;                 // power * numBlocks: chunks complete per block
     int *ticket;               // one per die queue
     int *status;
     int hints;                 // L2 eviction hints on the matrix
@@ -334,36 +350,31 @@ struct MpkArgs {
 };
 
 // Persistent warps: one run (up to 32 consecutive chunks at one power) per
-// ticket. A run waits until every chunk in its intervals is complete at the
-// previous power; those chunks belong to runs earlier in the global order,
-// taken by running warps, so the wait always ends (bounded anyway: a
-// timeout goes to the status word). The polls are relaxed loads and one
-// acquire fence follows the successful poll (a flag read by a relaxed load
-// and a later fence.acq_rel form an acquire of the writer's release).
-// A warp takes the runs of its own die's queue, so each chunk's matrix
-// block is cached by one die's L2 only; an empty queue sends it to the
-// other one. A warp releases its previous run's flags only after fetching
-// the next run, when the stores they publish have drained; the release
-// still comes before any wait, so a warp never waits on itself.
-// Code shape of kMpk per value type, the fastest measured on the 128^3
-// 27-point stencil (p = 8): with 16-bit columns FP64 in batches of 4
-// entries with at least 6 resident blocks per SM (38 registers), FP32
-// unbatched with 6, BF16 in batches of 8 with 8 (32 registers); with 32-bit
-// columns unbatched with 8.
-template <typename VT>
-constexpr int kMpkBatch = sizeof(VT) == 8 ? 4 : sizeof(VT) == 4 ? 0 : 8;
-template <typename VT, bool C16>
-constexpr int kMpkMinBlocks = C16 && sizeof(VT) != 2 ? 6 : 8;
+// ticket. A run waits until every completion block in its intervals is
+// complete at the previous power (its counter equals its chunk count);
+// those chunks belong to runs earlier in the global order (the order is
+// built from dependency ranges widened to whole blocks), taken by running
+// warps, so the wait always ends (bounded anyway: a timeout goes to the
+// status word). The polls are relaxed loads and one acquire fence follows
+// the successful poll (a counter read by a relaxed load and a later
+// fence.acq_rel form an acquire of the writers' releases). A warp takes the
+// runs of its own die's queue, so each chunk's matrix block is cached by
+// one die's L2 only; an empty queue sends it to the other one. A warp adds
+// its previous run's chunks to their block counters (release reductions)
+// only after fetching the next run, when the stores they publish have
+// drained; that comes before any wait, so a warp never waits on itself.
+// At least 6 resident blocks per SM (up to 40 registers a thread).
+constexpr int kMpkMinBlocks = 6;
 
 template <typename VT, bool HUBS, bool C16>
-__global__ void __launch_bounds__(kWarpThreads, (kMpkMinBlocks<VT, C16>)) kMpk(MpkArgs a) {
+__global__ void __launch_bounds__(kWarpThreads, kMpkMinBlocks) kMpk(MpkArgs a) {
     const int lane = threadIdx.x & 31;
     const unsigned long long polKeep = l2Policy(a.hints ? 1 : 0), polDrop = l2Policy(a.hints ? 2 : 0);
     const int myDie = a.numDies > 1 ? a.smDie[smIndex()] : 0;
     int q = myDie;
-    int pc0 = 0, pc1 = 0, pk = 0;  // run whose flags are still to be released
+    int pc0 = 0, pc1 = 0, pk = 0, pb = 0;  // run still to be counted, its first block
+    int it = 0;
     for (;;) {
-        int it = 0;
         if (lane == 0) it = atomicAdd(a.ticket + q, 1);
         it = __shfl_sync(0xffffffffu, it, 0);
         const int qStart = q == 0 ? a.dieStart[0] : a.dieStart[1];
@@ -375,13 +386,19 @@ __global__ void __launch_bounds__(kWarpThreads, (kMpkMinBlocks<VT, C16>)) kMpk(M
             d0 = a.runDep[2 * (qStart + it)];
             d1 = a.runDep[2 * (qStart + it) + 1];
         }
-        // release the previous run; __syncwarp orders all lanes' stores
-        // before the release stores
+        // count the previous run; __syncwarp orders all lanes' stores before
+        // the release reductions (lane i: the run's i-th block)
         __syncwarp();
-        if (lane < pc1 - pc0)
-            asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(a.done + (size_t)pk * a.numChunks + pc0 + lane),
-                         "r"(1)
-                         : "memory");
+        if (pc1 > pc0 && pb + lane < a.numBlocks) {
+            const int bs = a.blockStart[pb + lane];
+            if (bs < pc1) {
+                const int cnt = min(pc1, a.blockStart[pb + lane + 1]) - max(pc0, bs);
+                asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(a.done + (size_t)pk * a.numBlocks + pb +
+                                                                              lane),
+                             "r"(cnt)
+                             : "memory");
+            }
+        }
         pc0 = pc1 = 0;
         if (!have) {
             if (a.numDies > 1 && q == myDie) {
@@ -392,14 +409,15 @@ __global__ void __launch_bounds__(kWarpThreads, (kMpkMinBlocks<VT, C16>)) kMpk(M
         }
         const int k = h.z;  // computes x_{k+1} from x_k
         if (k > 0) {
-            const int *done = a.done + (size_t)(k - 1) * a.numChunks;
+            const int *done = a.done + (size_t)(k - 1) * a.numBlocks;
+            const int *bs = a.blockStart;
             long long spins = 0;
             for (;;) {
                 bool ok = true;
-                for (int i = d0.x + lane; i <= d0.y; i += 32) ok &= ldRelaxed(done + i) != 0;
-                for (int i = d0.z + lane; i <= d0.w; i += 32) ok &= ldRelaxed(done + i) != 0;
-                for (int i = d1.x + lane; i <= d1.y; i += 32) ok &= ldRelaxed(done + i) != 0;
-                for (int i = d1.z + lane; i <= d1.w; i += 32) ok &= ldRelaxed(done + i) != 0;
+                for (int i = d0.x + lane; i <= d0.y; i += 32) ok &= ldRelaxed(done + i) == bs[i + 1] - bs[i];
+                for (int i = d0.z + lane; i <= d0.w; i += 32) ok &= ldRelaxed(done + i) == bs[i + 1] - bs[i];
+                for (int i = d1.x + lane; i <= d1.y; i += 32) ok &= ldRelaxed(done + i) == bs[i + 1] - bs[i];
+                for (int i = d1.z + lane; i <= d1.w; i += 32) ok &= ldRelaxed(done + i) == bs[i + 1] - bs[i];
                 if (__all_sync(0xffffffffu, ok)) break;
                 if (++spins > kSpinLimit || ldAcquire(a.status) != DEV_OK) {
                     if (lane == 0) atomicCAS(a.status, DEV_OK, DEV_WAIT_TIMEOUT);
@@ -410,10 +428,11 @@ __global__ void __launch_bounds__(kWarpThreads, (kMpkMinBlocks<VT, C16>)) kMpk(M
             asm volatile("fence.acq_rel.gpu;" ::: "memory");
         }
         const unsigned long long pol = (h.w & 1) ? polDrop : polKeep;
-        for (int c = h.x; c < h.y; ++c) chunkRow<VT, HUBS, C16, true, kMpkBatch<VT>>(a.m, c, k, a.n, a.x, a.xf, pol);
+        for (int c = h.x; c < h.y; ++c) chunkRow<VT, HUBS, C16, true>(a.m, c, k, a.n, a.x, a.xf, pol);
         pc0 = h.x;
         pc1 = h.y;
         pk = k;
+        pb = h.w >> 1;
     }
 }
 
@@ -469,6 +488,12 @@ __global__ void kGatherHubs(const int *__restrict__ rowPtr, const int *__restric
     }
 }
 
+// Element offset of entry j of a lane's row inside its chunk: entries in
+// groups of four consecutive slots per lane (SELL-32 with 4-entry groups).
+__device__ __forceinline__ long long sellSlot(int j, int lane) {
+    return 32LL * (j & ~3) + 4 * lane + (j & 3);
+}
+
 // CRS -> SELL-32 copy; padding slots get value 0 and the row's own column.
 // Hub rows are longer than the chunk width L: their first L entries are
 // copied and never read.
@@ -484,7 +509,7 @@ __global__ void kToSell(const int *__restrict__ rowPtr, const int *__restrict__ 
     const int s = live ? rowPtr[r] : 0, len = live ? rowPtr[r + 1] - s : 0;
     const int L = chunkLen[c];
     for (int j = 0; j < L; ++j) {
-        long long o = chunkOff[c] + 32LL * j + lane;
+        const long long o = chunkOff[c] + sellSlot(j, lane);
         if (j < len) {
             sval[o] = val[s + j];
             scol[o] = col[s + j];
@@ -551,7 +576,7 @@ __global__ void kToSell16(const int *__restrict__ rowPtr, const int *__restrict_
     const int L = chunkLen[c];
     const int4 b = chunkBase[c];
     for (int j = 0; j < L; ++j) {
-        const long long o = chunkOff[c] + 32LL * j + lane;
+        const long long o = chunkOff[c] + sellSlot(j, lane);
         unsigned short v = 0;
         if (j < len) {
             sval[o] = val[s + j];
@@ -561,11 +586,11 @@ __global__ void kToSell16(const int *__restrict__ rowPtr, const int *__restrict_
                 const int bs = sel == 0 ? b.x : sel == 1 ? b.y : sel == 2 ? b.z : b.w;
                 v = (unsigned short)((sel << 14) | (cc - bs));
             } else {
-                wideCol[b.y + 32 * j + lane] = cc;
+                wideCol[b.y + sellSlot(j, lane)] = cc;
             }
         } else {
             sval[o] = VT(0);
-            if (b.x < 0) wideCol[b.y + 32 * j + lane] = live ? r : chunkRowP[c];
+            if (b.x < 0) wideCol[b.y + sellSlot(j, lane)] = live ? r : chunkRowP[c];
         }
         col16[o] = v;
     }
@@ -683,6 +708,7 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
             int r1 = std::min(gp[g + 1], r + 32);
             int L = 0;
             for (int q = r; q < r1; ++q) L = std::max(L, rowLen[q]);
+            L = (L + 3) & ~3;  // whole entry groups
             chunkOff.push_back(off);
             chunkLen.push_back(L);
             chunkRowH.push_back(r1);
@@ -753,8 +779,8 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     }
     RACE_CUDA(cudaGetLastError());
     plan->stepped = e.powerLevelsType == "L" || e.powerLevelsType == "U";
+    plan->schedule = e.mpkSchedule;
     plan->depRange.alloc((size_t)std::max(C, 1) * 6);
-    plan->done.alloc((size_t)std::max(C, 1) * power);
     plan->ticket.alloc(2);
     plan->status.alloc(1);
     DevBuf<int> dChunkGroup, dBad(1);
@@ -819,15 +845,34 @@ std::unique_ptr<MpkPlan> buildMpkPlan(Engine &e, const race_operands &ops, int p
     const bool twoDies = dies.numDies == 2 && e.mpkOrder == 0 && e.mpkDieQueues;
     const std::vector<int> chunkDie =
         twoDies ? chunkDies(C, dies.smsPerDie[0], dies.smsPerDie[1]) : std::vector<int>();
+    // Completion is counted per block of chunks; the order is built from the
+    // dependency ranges widened to whole blocks, and the kernel's tables
+    // name blocks: each interval as a block range, each run's first block
+    // in the flags.
+    const std::vector<int> blockStart = mpkFlagBlocks(C, chunkGroup);
+    const int NB = (int)blockStart.size() - 1;
+    std::vector<int> blockOf(C);
+    for (int b = 0; b < NB; ++b)
+        for (int c = blockStart[b]; c < blockStart[b + 1]; ++c) blockOf[c] = b;
+    const std::vector<int> widened = widenDepsToBlocks(depRange, blockStart);
     const MpkOrder order = e.mpkOrder == 1
-                               ? mpkGroupOrder(depRange, chunkGroup, G, power, e.mpkStride == 1 ? 1 : 2, segLen)
-                               : mpkRunOrder(depRange, C, power, segLen, e.mpkRun, e.mpkLag, chunkDie);
+                               ? mpkGroupOrder(widened, chunkGroup, G, power, e.mpkStride == 1 ? 1 : 2, segLen)
+                               : mpkRunOrder(widened, C, power, segLen, e.mpkRun, e.mpkLag, chunkDie);
     plan->numItems = (int)((size_t)C * power);
     plan->numRuns = order.numRuns();
     plan->numDies = twoDies ? 2 : 1;
     for (int d = 0; d < 3; ++d) plan->dieStart[d] = order.dieStart[d];
     plan->smDie = dies.smDieDev.p;
+    plan->numBlocks = NB;
+    plan->blockStart.upload(blockStart.data(), blockStart.size(), s);
+    plan->done.alloc((size_t)std::max(NB, 1) * power);
     std::vector<int> head(order.head), dep(order.dep);
+    for (int r = 0; r < plan->numRuns; ++r) head[4 * (size_t)r + 3] |= blockOf[head[4 * (size_t)r]] << 1;
+    for (size_t i = 0; i + 1 < dep.size(); i += 2)
+        if (dep[i + 1] >= dep[i]) {
+            dep[i] = blockOf[dep[i]];
+            dep[i + 1] = blockOf[dep[i + 1]];
+        }
     if (plan->numRuns == 0) {
         head.assign(4, 0);
         dep.assign(8, 0);
@@ -928,11 +973,83 @@ void launchSpmvSell(const MpkPlan &p, int n, int k, double *x, cudaStream_t s) {
 }
 }  // namespace
 
+namespace {
+// The persistent wavefront kernel over all powers.
+void runWavefront(MpkPlan &plan, const race_operands &ops, cudaStream_t s) {
+    RACE_CUDA(cudaMemsetAsync(plan.done.p, 0, sizeof(int) * (size_t)plan.numBlocks * plan.power, s));
+    RACE_CUDA(cudaMemsetAsync(plan.ticket.p, 0, sizeof(int) * 2, s));
+    MpkArgs a{viewOf(plan),
+              (double *)ops.x,
+              plan.xf.p,
+              ops.n,
+              plan.runHead.p,
+              plan.runDep.p,
+              plan.numBlocks,
+              plan.blockStart.p,
+              plan.done.p,
+              plan.ticket.p,
+              plan.status.p,
+              plan.hints,
+              plan.smDie,
+              plan.numDies,
+              {plan.dieStart[0], plan.dieStart[1], plan.dieStart[2]}};
+    switch (plan.valType) {
+    case RACE_VAL_F64: launchMpk<double>(a, plan, s); break;
+    case RACE_VAL_F32: launchMpk<float>(a, plan, s); break;
+    case RACE_VAL_BF16: launchMpk<__nv_bfloat16>(a, plan, s); break;
+    default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
+    }
+    RACE_CUDA(cudaGetLastError());
+}
+
+// p plain SpMV launches on the same layout.
+void runSweeps(MpkPlan &plan, const race_operands &ops, cudaStream_t s) {
+    for (int k = 0; k < plan.power; ++k) {
+        switch (plan.valType) {
+        case RACE_VAL_F64: launchSpmvSell<double>(plan, ops.n, k, (double *)ops.x, s); break;
+        case RACE_VAL_F32: launchSpmvSell<float>(plan, ops.n, k, (double *)ops.x, s); break;
+        case RACE_VAL_BF16: launchSpmvSell<__nv_bfloat16>(plan, ops.n, k, (double *)ops.x, s); break;
+        default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
+        }
+        RACE_CUDA(cudaGetLastError());
+    }
+}
+
+// RACE_MPK_AUTO's choice: each schedule timed on its second run (the first
+// warms the code and the caches), the faster kept. Both compute the same
+// powers, so the call's result is complete either way; the wavefront's
+// status word is cleared afterwards, as the sweeps would leave it.
+int chooseSchedule(MpkPlan &plan, const race_operands &ops, cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    RACE_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return plan.valType == RACE_VAL_F64 ? RACE_MPK_WAVEFRONT : RACE_MPK_SWEEPS;
+    cudaEvent_t ev[2];
+    RACE_CUDA(cudaEventCreate(&ev[0]));
+    RACE_CUDA(cudaEventCreate(&ev[1]));
+    float ms[2] = {0.f, 0.f};
+    for (int rep = 0; rep < 2; ++rep)
+        for (int sc = 0; sc < 2; ++sc) {
+            RACE_CUDA(cudaEventRecord(ev[0], s));
+            if (sc == 0) runWavefront(plan, ops, s);
+            else runSweeps(plan, ops, s);
+            RACE_CUDA(cudaEventRecord(ev[1], s));
+            RACE_CUDA(cudaEventSynchronize(ev[1]));
+            RACE_CUDA(cudaEventElapsedTime(&ms[sc], ev[0], ev[1]));
+        }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    int st = DEV_OK;
+    RACE_CUDA(cudaMemcpyAsync(&st, plan.status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    RACE_CUDA(cudaStreamSynchronize(s));
+    RACE_CUDA(cudaMemsetAsync(plan.status.p, 0, sizeof(int), s));
+    plan.chosen = (st == DEV_OK && ms[0] <= ms[1]) ? RACE_MPK_WAVEFRONT : RACE_MPK_SWEEPS;
+    return plan.chosen;
+}
+}  // namespace
+
 void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
     if (power != plan.power) throw Error(RACE_ERR_INVALID_ARG, "power differs from the planned power");
     cudaStream_t s = e.stream;
-    RACE_CUDA(cudaMemsetAsync(plan.done.p, 0, sizeof(int) * (size_t)plan.numChunks * plan.power, s));
-    RACE_CUDA(cudaMemsetAsync(plan.ticket.p, 0, sizeof(int) * 2, s));
     RACE_CUDA(cudaMemsetAsync(plan.status.p, 0, sizeof(int), s));
     if (plan.valType != RACE_VAL_F64) kToFloat<<<ceilDiv(ops.n, 256), 256, 0, s>>>((const double *)ops.x, plan.xf.p, ops.n);
     if (plan.stepped) {
@@ -945,16 +1062,16 @@ void runMpk(Engine &e, MpkPlan &plan, const race_operands &ops, int power) {
         RACE_CUDA(cudaGetLastError());
         return;
     }
-    MpkArgs a{viewOf(plan), (double *)ops.x, plan.xf.p, ops.n, plan.runHead.p, plan.runDep.p,
-              plan.numChunks, plan.done.p, plan.ticket.p, plan.status.p, plan.hints, plan.smDie, plan.numDies,
-              {plan.dieStart[0], plan.dieStart[1], plan.dieStart[2]}};
-    switch (plan.valType) {
-    case RACE_VAL_F64: launchMpk<double>(a, plan, s); break;
-    case RACE_VAL_F32: launchMpk<float>(a, plan, s); break;
-    case RACE_VAL_BF16: launchMpk<__nv_bfloat16>(a, plan, s); break;
-    default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
+    const int sched = plan.schedule != RACE_MPK_AUTO ? plan.schedule : plan.chosen;
+    if (sched == RACE_MPK_WAVEFRONT) runWavefront(plan, ops, s);
+    else if (sched == RACE_MPK_SWEEPS) runSweeps(plan, ops, s);
+    else {
+        const int c = chooseSchedule(plan, ops, s);
+        if (plan.chosen == 0) {  // not timed (stream capture): run the default
+            if (c == RACE_MPK_WAVEFRONT) runWavefront(plan, ops, s);
+            else runSweeps(plan, ops, s);
+        }
     }
-    RACE_CUDA(cudaGetLastError());
 }
 
 // One plain SpMV x_{k+1} = A x_k on the registered SELL layout (the p-SpMV

@@ -168,4 +168,31 @@ std::vector<int> chunkDies(int numChunks, int smsDie0, int smsDie1) {
     return die;
 }
 
+std::vector<int> mpkFlagBlocks(int numChunks, const std::vector<int> &chunkGroup) {
+    if (!chunkGroup.empty() && (int)chunkGroup.size() != numChunks)
+        throw std::invalid_argument("mpkFlagBlocks: sizes");
+    std::vector<int> start;
+    for (int c = 0; c < numChunks; ++c)
+        if (c % kDieBlockChunks == 0 || (!chunkGroup.empty() && chunkGroup[c] != chunkGroup[c - 1]))
+            start.push_back(c);
+    start.push_back(std::max(numChunks, 0));
+    return start;
+}
+
+std::vector<int> widenDepsToBlocks(const std::vector<int> &depRange, const std::vector<int> &blockStart) {
+    std::vector<int> out(depRange);
+    const int C = blockStart.empty() ? 0 : blockStart.back();
+    for (size_t i = 0; i + 1 < out.size(); i += 2) {
+        const int lo = out[i], hi = out[i + 1];
+        if (hi < lo) continue;
+        if (lo < 0 || hi >= C) throw std::invalid_argument("widenDepsToBlocks: interval outside the chunks");
+        // block of a chunk: the last start <= it
+        const size_t bl = std::upper_bound(blockStart.begin(), blockStart.end() - 1, lo) - blockStart.begin() - 1;
+        const size_t bh = std::upper_bound(blockStart.begin(), blockStart.end() - 1, hi) - blockStart.begin() - 1;
+        out[i] = blockStart[bl];
+        out[i + 1] = blockStart[bh + 1] - 1;
+    }
+    return out;
+}
+
 }  // namespace race

@@ -56,4 +56,18 @@ MpkOrder mpkGroupOrder(const std::vector<int> &depRange, const std::vector<int> 
 constexpr int kDieBlockChunks = 16;
 std::vector<int> chunkDies(int numChunks, int smsDie0, int smsDie1);
 
+// Completion blocks of the persistent kernel: it counts finished chunks per
+// block and power instead of flagging every chunk, so a run polls one
+// counter per block it reads. A block is a maximal stretch of consecutive
+// chunks inside one die block (kDieBlockChunks) and one level group
+// (chunkGroup; empty: no groups). Returns the block starts (numBlocks + 1
+// entries, the last = numChunks).
+std::vector<int> mpkFlagBlocks(int numChunks, const std::vector<int> &chunkGroup);
+
+// depRange with every non-empty interval widened to whole blocks. An order
+// built from the widened ranges has every chunk of every block a run polls
+// complete before the run in the order; as blocks stay inside level groups,
+// the widened ranges still lie in the previous, own and next group.
+std::vector<int> widenDepsToBlocks(const std::vector<int> &depRange, const std::vector<int> &blockStart);
+
 }  // namespace race

@@ -28,6 +28,8 @@ ROW, NNZ = 0, 1
 FILL, SCATTER = 0, 1
 SPMV, SPMTV, SYMMSPMV, GS, KACZ, MPK = 0, 1, 2, 3, 4, 5
 SWEEP_AUTO, SWEEP_WAVE, SWEEP_LEAF, SWEEP_GATHER = 0, 1, 2, 3
+# RACE_MPK_AUTO / WAVEFRONT / SWEEPS
+MPK_SCHEDULES = ("auto", "wavefront", "sweeps")
 VAL_F64, VAL_F32, VAL_BF16 = 0, 1, 2
 _VAL_TYPE = {torch.float64: VAL_F64, torch.float32: VAL_F32, torch.bfloat16: VAL_BF16}
 
@@ -328,12 +330,18 @@ class Interface:
         self._check(lib().race_set_sweep_mode(self._h, int(mode)))
 
     def getMpkLayout(self, funcId: int) -> dict:
-        """Device layout of a registered MPK function (race_get_mpk_layout)."""
+        """Device layout and schedule of a registered MPK function
+        (race_get_mpk_layout)."""
         v = [C.c_int() for _ in range(3)]
         w = [C.c_longlong() for _ in range(2)]
-        self._check(lib().race_get_mpk_layout(self._h, int(funcId), *[C.byref(a) for a in v + w]))
+        sch = C.c_int()
+        self._check(lib().race_get_mpk_layout(self._h, int(funcId), *[C.byref(a) for a in v + w], C.byref(sch)))
         return dict(chunks=v[0].value, col_bits=v[1].value, wide_chunks=v[2].value, sell_slots=w[0].value,
-                    matrix_bytes=w[1].value)
+                    matrix_bytes=w[1].value, schedule=MPK_SCHEDULES[sch.value])
+
+    def setMpkSchedule(self, funcId: int, schedule: str):
+        """race_set_mpk_schedule: "auto", "wavefront" or "sweeps"."""
+        self._check(lib().race_set_mpk_schedule(self._h, int(funcId), MPK_SCHEDULES.index(schedule)))
 
     def getSweepInfo(self, funcId: int, rev: bool = False) -> dict:
         v = [C.c_int() for _ in range(5)]

@@ -11,6 +11,7 @@ from race_gb300 import matgen
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
+from race_gb300 import _lib  # noqa: E402
 from race_gb300 import interface as ri  # noqa: E402
 
 
@@ -412,6 +413,38 @@ def test_mpk_column_layouts(monkeypatch):
             ref32 = outs[1]
         np.testing.assert_array_equal(outs[1], ref32)
     assert mixed
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32, torch.bfloat16])
+def test_mpk_schedules_agree(mats, dtype):
+    """The wavefront kernel, the p plain sweeps and the automatic choice
+    (timed at the first call) give bit-identical powers; FP64 equals the
+    oracle's p sequential fma SpMVs. The layout query reports the schedule
+    that ran."""
+    A = mats["st27_24"]
+    p = 5
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
+    assert rc.RACEColor(p, 2e6) == 0
+    P = A.permuted(rc.getPerm(), rc.getInvPerm())
+    x0 = matgen.uniform_vector(A.n, 3)
+    x = torch.zeros((p + 1) * A.n, dtype=torch.float64, device="cuda")
+    x[: A.n] = torch.tensor(x0, device="cuda")
+    fid = rc.registerFunction(ri.MPK, ri.Operands(_upload(P, dtype), x), power=p)
+    assert rc.getMpkLayout(fid)["schedule"] == "auto"
+    outs = {}
+    for sc in ("wavefront", "sweeps", "auto"):
+        rc.setMpkSchedule(fid, sc)
+        x[A.n:] = 0
+        for _ in range(2):
+            assert rc.executeFunction(fid) == 0
+        outs[sc] = x.cpu().numpy()
+    assert rc.getMpkLayout(fid)["schedule"] in ("wavefront", "sweeps")
+    np.testing.assert_array_equal(outs["wavefront"], outs["sweeps"])
+    np.testing.assert_array_equal(outs["auto"], outs["sweeps"])
+    if dtype == torch.float64:
+        np.testing.assert_array_equal(outs["auto"].reshape(p + 1, A.n), orc.mpk_plain(P, x0, p))
+    with pytest.raises(_lib.RaceError):
+        rc.setMpkSchedule(fid + 1, "sweeps")
 
 
 @pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-5), (torch.bfloat16, 5e-2)])
