@@ -8,29 +8,37 @@
 //
 // Layout. At registration the permuted CRS is copied into SELL-32: rows are
 // cut into chunks of at most 32 consecutive rows that never cross a level
-// group, and each chunk stores entry j of its rows contiguously
-// (val[off + 32 j + lane]). A warp reads 32 consecutive values per load, and
-// each lane still owns one row and walks it as a sequential fma chain in CRS
-// order (MAT_SPMV_KERNEL's order, examples/src/helpers/kernels.cpp:749-777):
-// FP64 output is bit-identical to p sequential SpMVs with fused
-// multiply-adds. Padding slots are never computed (lanes stop at their row
-// length). One lane per row keeps GB300's FP64 pipe (1/64 of the FP32 rate)
-// busy with useful fmas only. Rows of more than kHubRowLen entries (hubs of
-// power-law graphs) would stall their lane and pad their whole chunk: they
-// are kept out of the SELL width, copied contiguously and summed by the
-// whole warp (32 ordered partial chains and a fixed butterfly), which
-// matches the sequential sum to rounding rather than bit for bit.
+// group; each lane owns one row and its entries sit in groups of four
+// consecutive slots (entry j at off + 32 (j - j % 4) + 4 lane + j % 4), so a
+// lane fetches four values and four columns with one or two vector loads
+// and a warp's load covers 256-1024 contiguous bytes. Columns are stored in
+// 16 bits where a chunk's columns fit four windows of 2^14 rows (a 2-bit
+// window and the offset from that window's per-chunk base; the other
+// chunks keep 32-bit columns). Each lane walks its row as a sequential fma
+// chain in CRS order (MAT_SPMV_KERNEL's order,
+// examples/src/helpers/kernels.cpp:749-777): FP64 output is bit-identical
+// to p sequential SpMVs with fused multiply-adds. Padding slots are loaded
+// as part of a last partial group but never computed. One lane per row
+// keeps GB300's FP64 pipe (1/64 of the FP32 rate) busy with useful fmas
+// only. Rows of more than kHubRowLen entries (hubs of power-law graphs)
+// would stall their lane and pad their whole chunk: they are kept out of
+// the SELL width, copied contiguously and summed by the whole warp (32
+// ordered partial chains and a fixed butterfly), which matches the
+// sequential sum to rounding rather than bit for bit.
 //
-// Schedule. A work item is (power, chunk). Items are listed in wavefront
-// order and taken by persistent warps from a global ticket; each warp is an
-// independent worker (no CTA barriers). An item waits until, at the previous
-// power, the chunks holding its columns are complete: per chunk the engine
-// records one chunk range in each of the previous, own and next group
-// (narrow: a row's neighbours sit near the same position of the adjacent
-// levels), and the warp checks their completion flags in parallel. Items
-// wait only on earlier tickets, held by running warps, so the schedule
-// cannot deadlock; every wait is bounded anyway and reports a timeout
-// through the status word.
+// Schedule (RACE_MPK_WAVEFRONT). A work item is (power, chunk). Items are
+// listed in the chunk-level wavefront order (mpk_order.cpp), grouped into
+// runs of consecutive chunks, one queue per L2 die, and taken by persistent
+// warps from per-queue tickets; each warp is an independent worker (no CTA
+// barriers). A run waits until, at the previous power, the chunks holding
+// its columns are complete: per chunk the engine records one chunk range in
+// each of the previous, own and next group (narrow: a row's neighbours sit
+// near the same position of the adjacent levels), widened to blocks of at
+// most 16 chunks whose completions are counted, and the warp checks those
+// counters in parallel. Runs wait only on earlier runs, held by running
+// warps, so the schedule cannot deadlock; every wait is bounded anyway and
+// reports a timeout through the status word. RACE_MPK_SWEEPS runs p plain
+// SpMV launches on the same layout instead; RACE_MPK_AUTO keeps the faster.
 //
 // Reduced precision (FP32/BF16 values): the powers are kept in an internal
 // FP32 copy of x and accumulated in FP32; each result is also written to the
