@@ -799,13 +799,17 @@ def bench_c1(ri, matgen, torch, reps: int = 100, gather: bool = True):
             "cpu_sequential_body_ms_per_call": seq_ms}
 
 
-def bench_tuner(torch):
-    """The MLP cost model (32 features -> 3 x 128 ReLU -> log time), trained
-    by the engine's CUDA kernels on committed search timings and evaluated on
-    the held-out fifth against the searched optimum and against the best
-    single config. Tasks: A^8 x over power per block x cache budget (300
-    matrices, 13 configs) and a symmetric GS sweep over requested threads x
-    efficiency threshold (9 configs)."""
+def bench_tuner(torch, retime: int = 8):
+    """The MLP cost model (matrix and config features -> 3 x 128 ReLU -> log
+    time), trained by the engine's CUDA kernels on committed search timings
+    and evaluated on the held-out matrices against the searched optimum and
+    against the best single config. Tasks: A^8 x over power per block x
+    cache budget x recursion depth (tuner_search.npz) and a symmetric GS
+    sweep over requested threads x efficiency threshold
+    (tuner_search_symmgs.npz). For up to `retime` held-out matrices of the
+    MPK set (the smallest, up to 200k rows), the MLP's pick and the
+    searched optimum are timed again here on fresh engines and the regret
+    is recomputed from those times."""
     from race_gb300 import tuner
     out = {}
     for name, fname in [("mpk", "tuner_search.npz"), ("symmgs", "tuner_search_symmgs.npz")]:
@@ -813,7 +817,9 @@ def bench_tuner(torch):
         if not path.exists():
             continue
         ds = tuner.Dataset.load(path)
-        held = np.arange(len(ds.times)) % 5 == 4
+        # held out: every tenth matrix of the MPK set (200 of 2,000), every
+        # fifth of the coloring set
+        held = np.arange(len(ds.times)) % (10 if name == "mpk" else 5) == (9 if name == "mpk" else 4)
         train, test = ds.subset(~held), ds.subset(held)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -823,6 +829,24 @@ def bench_tuner(torch):
         res = tuner.evaluate(model, test, tuner.best_fixed_config(train))
         res.update({"train_matrices": len(train.times), "train_seconds": time.perf_counter() - t0,
                     "final_train_loss": hist[-1]})
+        if name == "mpk" and retime > 0:
+            rows = [i for i in np.flatnonzero(held) if ds.sizes[i][0] <= 200_000]
+            rows = sorted(rows, key=lambda i: ds.sizes[i][0])[:retime]
+            regrets, details = [], []
+            for i in rows:
+                fam, A = tuner.dataset_matrix(int(i))
+                feas = np.isfinite(ds.times[i])
+                pick = model.choose(ds.features[i], feas)
+                best = int(np.argmin(ds.times[i]))
+                t_pick = tuner.time_config(A, tuner.CONFIGS[pick])
+                t_best = t_pick if best == pick else tuner.time_config(A, tuner.CONFIGS[best])
+                regrets.append(t_pick / min(t_pick, t_best) - 1.0)
+                details.append({"matrix": int(i), "family": fam, "n": A.n, "pick": list(tuner.CONFIGS[pick]),
+                                "searched_best": list(tuner.CONFIGS[best]), "t_pick_ms": t_pick * 1e3,
+                                "t_best_ms": t_best * 1e3})
+            res["retimed_here"] = {"matrices": len(regrets), "mean_regret": float(np.mean(regrets)) if regrets else None,
+                                   "within_10pct": float(np.mean(np.asarray(regrets) <= 0.10)) if regrets else None,
+                                   "cases": details}
         out[name] = res
     return out or None
 

@@ -130,6 +130,18 @@ struct DevWaves {
     DevBuf<unsigned char> waveHuge;
     DevBuf<int> segFirst, segPos, segBeg, segEnd;
     DevBuf<double> segScratch;
+    // SELL copy of the rows a thread runs (up to midRow entries), in plan
+    // order: the rows of a wave sorted by length, cut into chunks of 32
+    // positions; each position's entries in groups of four slots (entry k
+    // of chunk lane l at off + 32 (k - k % 4) + 4 l + k % 4). Per wave its
+    // first chunk (numWaves+1), per chunk its first slot.
+    bool sell = false;
+    int sellMidRow = 0;
+    long long sellSlots = 0;
+    DevBuf<int> waveChunk;
+    DevBuf<long long> chunkOff;
+    DevBuf<unsigned char> sellVal;  // sellSlots values (the operands' value type)
+    DevBuf<int> sellCol;
 };
 
 // Device copy of a gather plan (waves.h) of one sweep direction, built at
@@ -190,6 +202,14 @@ class Engine {
     // or leaf by cost), SWEEP_WAVE (bit-exact wave plans), SWEEP_LEAF (warp
     // per leaf), SWEEP_GATHER
     int sweepMode = SWEEP_AUTO;
+    // wave mode: rows of up to this many entries run one thread each, longer
+    // ones (up to 512) one warp each; both keep the sequential order. With
+    // sweepSell the thread rows read a SELL copy in plan order (coalesced
+    // vector loads) instead of the caller's CRS. 16 and SELL were the
+    // fastest measured (4.2M-row power-law GS, FP32: 43.7 ms per symmetric
+    // sweep against 50.5 ms with 32 and CRS).
+    int sweepMidRow = 16;
+    bool sweepSell = true;
 
     // coloring results
     std::unique_ptr<ZoneTree> tree;

@@ -23,6 +23,7 @@
 //
 // Neither mode needs atomics on the transpose scatter: the coloring (leaf
 // mode) or the wave plan (wave mode) gives every written entry one writer.
+#include <algorithm>
 #include <cstdlib>
 
 #include <cuda_bf16.h>
@@ -34,6 +35,9 @@ namespace {
 
 constexpr int kSweepThreads = 256;
 constexpr int kWarps = kSweepThreads / 32;
+// Wave mode: one block per SM; the grid barrier costs one arrival per block,
+// so the threads a wave can use grow with the block size at no barrier cost.
+constexpr int kWaveThreads = 256;
 constexpr int kWaveBlocksPerSm = 1;
 
 __device__ __forceinline__ unsigned ldAcquireU(const unsigned *p) {
@@ -104,37 +108,137 @@ struct SweepArgs {
     const int *segFirst, *segPos, *segBeg, *segEnd;
     double *segScratch;
     int numSegs;
+    int midRow;  // wave mode: rows of up to midRow entries run one thread each, longer ones a warp
+    // wave mode: SELL copy of the thread rows (DevWaves), or null
+    const int *waveChunk;
+    const long long *chunkOff;
+    const void *sellVal;
+    const int *sellCol;
+};
+
+// Entries [jb, e) of a row in order, one thread: columns and values in
+// batches of 8, then the batch's gathers of x, then f(value, x[col]) in the
+// row's order (the loads of a batch are in flight together; the chain of f
+// is the sequential one).
+template <typename VT, typename XT, typename F>
+__device__ __forceinline__ void serialRow(const SweepArgs &a, int jb, int e, F &&f) {
+    const VT *val = (const VT *)a.val;
+    const XT *x = (const XT *)a.x;
+    int j = jb;
+    for (; j + 8 <= e; j += 8) {
+        int c[8];
+        XT v[8], xv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            c[k] = a.col[j + k];
+            v[k] = ld<VT, XT>(val, j + k);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) xv[k] = x[c[k]];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) f(v[k], xv[k]);
+    }
+    for (; j < e; ++j) f(ld<VT, XT>(val, j), x[a.col[j]]);
+}
+
+// The four values of an entry group of the SELL copy (16-byte aligned).
+__device__ __forceinline__ void groupVals(const double *v, double out[4]) {
+    const double2 a = *(const double2 *)v, b = *(const double2 *)(v + 2);
+    out[0] = a.x;
+    out[1] = a.y;
+    out[2] = b.x;
+    out[3] = b.y;
+}
+__device__ __forceinline__ void groupVals(const float *v, float out[4]) {
+    const float4 a = *(const float4 *)v;
+    out[0] = a.x;
+    out[1] = a.y;
+    out[2] = a.z;
+    out[3] = a.w;
+}
+__device__ __forceinline__ void groupVals(const __nv_bfloat16 *v, float out[4]) {
+    const uint2 a = *(const uint2 *)v;
+    out[0] = __uint_as_float(a.x << 16);
+    out[1] = __uint_as_float(a.x & 0xffff0000u);
+    out[2] = __uint_as_float(a.y << 16);
+    out[3] = __uint_as_float(a.y & 0xffff0000u);
+}
+__device__ __forceinline__ int comp(const int4 &c, int q) { return q == 0 ? c.x : q == 1 ? c.y : q == 2 ? c.z : c.w; }
+
+// The entries of one row, as the row bodies below see them: entry k
+// (0-based, CRS order) and an in-order walk sum(x, k0, f) calling
+// f(value, x[col]) for entries k0..len-1. CrsRow reads the caller's CRS
+// (loads in batches of 8, serialRow); SellRow reads the SELL copy, one
+// group of four entries per vector load of values and columns.
+template <typename VT, typename XT>
+struct CrsRow {
+    const int *col;
+    const VT *val;
+    int s, len;
+    __device__ XT v(int k) const { return ld<VT, XT>(val, s + k); }
+    __device__ int c(int k) const { return col[s + k]; }
+    template <typename F>
+    __device__ void sum(const SweepArgs &a, int k0, F &&f) const {
+        serialRow<VT, XT>(a, s + k0, s + len, f);
+    }
+};
+
+template <typename VT, typename XT>
+struct SellRow {
+    const int *col;
+    const VT *val;
+    long long off;  // the chunk's first slot
+    int lane, len;
+    __device__ long long slot(int k) const { return off + 32LL * (k & ~3) + 4 * lane + (k & 3); }
+    __device__ XT v(int k) const { return ld<VT, XT>(val, slot(k)); }
+    __device__ int c(int k) const { return col[slot(k)]; }
+    template <typename F>
+    __device__ void sum(const SweepArgs &a, int k0, F &&f) const {
+        const XT *x = (const XT *)a.x;
+        for (int g = k0 & ~3; g < len; g += 4) {
+            const long long o = off + 32LL * g + 4 * lane;
+            const int4 cc = *(const int4 *)(col + o);
+            XT vv[4], xv[4];
+            groupVals(val + o, vv);
+            const int lo = max(g, k0) - g, hi = min(len - g, 4);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (q >= lo && q < hi) xv[q] = x[comp(cc, q)];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (q >= lo && q < hi) f(vv[q], xv[q]);
+        }
+    }
 };
 
 // One row with the kernel body's own operation order (thread per row).
-template <typename VT, typename XT>
-__device__ __forceinline__ void rowSerial(const SweepArgs &a, int r) {
-    const VT *val = (const VT *)a.val;
+template <typename VT, typename XT, typename Row>
+__device__ __forceinline__ void rowSerial(const SweepArgs &a, int r, const Row &row) {
     XT *x = (XT *)a.x;
     XT *b = (XT *)a.b;
-    const int s = a.rowPtr[r], e = a.rowPtr[r + 1];
+    const int len = row.len;
     switch (a.kernel) {
     case RACE_K_SPMV: {  // kernels.cpp:5-15
         XT t = XT(0);
-        for (int j = s; j < e; ++j) t = mac(ld<VT, XT>(val, j), x[a.col[j]], t);
+        row.sum(a, 0, [&](XT v, XT xv) { t = mac(v, xv, t); });
         b[r] = t;
         break;
     }
     case RACE_K_SPMTV: {  // kernels.cpp:107-115
         const XT xr = x[r];
-        for (int j = s; j < e; ++j) {
-            const int c = a.col[j];
-            b[c] = mac(ld<VT, XT>(val, j), xr, b[c]);
+        for (int k = 0; k < len; ++k) {
+            const int c = row.c(k);
+            b[c] = mac(row.v(k), xr, b[c]);
         }
         break;
     }
     case RACE_K_SYMMSPMV: {  // kernels.cpp:403-417
         const XT xr = x[r];
-        b[r] = mac(ld<VT, XT>(val, s), xr, b[r]);
+        b[r] = mac(row.v(0), xr, b[r]);
         XT t = XT(0);
-        for (int j = s + 1; j < e; ++j) {
-            const int c = a.col[j];
-            const XT v = ld<VT, XT>(val, j);
+        for (int k = 1; k < len; ++k) {
+            const int c = row.c(k);
+            const XT v = row.v(k);
             t = mac(v, x[c], t);
             b[c] = mac(v, xr, b[c]);
         }
@@ -143,21 +247,20 @@ __device__ __forceinline__ void rowSerial(const SweepArgs &a, int r) {
     }
     case RACE_K_GS: {  // kernels.cpp:174-186
         XT t = b[r];
-        for (int j = s + 1; j < e; ++j) t = mac(-ld<VT, XT>(val, j), x[a.col[j]], t);
-        x[r] = t / ld<VT, XT>(val, s);
+        row.sum(a, 1, [&](XT v, XT xv) { t = mac(-v, xv, t); });
+        x[r] = t / row.v(0);
         break;
     }
     case RACE_K_KACZ: {  // kernels.cpp:285-302
         XT nrm = XT(0), sc = -b[r];
-        for (int j = s; j < e; ++j) {
-            const XT v = ld<VT, XT>(val, j);
-            sc = mac(v, x[a.col[j]], sc);
+        row.sum(a, 0, [&](XT v, XT xv) {
+            sc = mac(v, xv, sc);
             nrm = mac(v, v, nrm);
-        }
+        });
         sc /= nrm;
-        for (int j = s; j < e; ++j) {
-            const int c = a.col[j];
-            x[c] = mac(-sc, ld<VT, XT>(val, j), x[c]);
+        for (int k = 0; k < len; ++k) {
+            const int c = row.c(k);
+            x[c] = mac(-sc, row.v(k), x[c]);
         }
         break;
     }
@@ -166,13 +269,10 @@ __device__ __forceinline__ void rowSerial(const SweepArgs &a, int r) {
 }
 
 // Wave mode keeps the sequential order (bit-exact) for rows of up to
-// kHugeRow entries: up to kMidRow one thread, above that one warp
-// (rowWarpExact). Longer rows are reassociated (hugeWave).
-// Rows longer than this (and up to kHugeRow) are run by a whole warp that
-// keeps the sequential order (rowWarpExact): one thread walking a few hundred
-// entries would pay a dependent gather per few entries and make its row the
-// wave's critical path.
-constexpr int kMidRow = 32;
+// kHugeRow entries: up to SweepArgs::midRow (the engine's sweepMidRow) one
+// thread, above that one warp (rowWarpExact): one thread walking a few
+// hundred entries would pay a dependent gather per few entries and make its
+// row the wave's critical path. Longer rows are reassociated (hugeWave).
 
 template <typename VT, typename XT>
 __device__ __forceinline__ void rowWarp(const SweepArgs &a, int row, int lane);
@@ -218,7 +318,7 @@ __device__ __forceinline__ void foldRow(const SweepArgs &a, int jb, int e, int l
 }
 
 // A row with the kernel body's own operation order, run by a warp (rows of
-// kMidRow+1..kHugeRow entries): sums through foldRow, identical bit for bit
+// midRow+1..kHugeRow entries): sums through foldRow, identical bit for bit
 // to rowSerial; scatters (one distinct column per entry) run lane-parallel
 // with the same per-entry arithmetic.
 template <typename VT, typename XT>
@@ -283,7 +383,7 @@ __device__ __forceinline__ void rowWarpExact(const SweepArgs &a, int r, int lane
 }
 
 template <typename VT, typename XT>
-__global__ void __launch_bounds__(kSweepThreads) kWaveSweep(SweepArgs a) {
+__global__ void __launch_bounds__(kWaveThreads, 1) kWaveSweep(SweepArgs a) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int nt = gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31;
@@ -297,7 +397,14 @@ __global__ void __launch_bounds__(kSweepThreads) kWaveSweep(SweepArgs a) {
         }
         for (int i = r0 + tid; i < r1; i += nt) {
             const int r = a.rows[i];
-            if (a.rowPtr[r + 1] - a.rowPtr[r] <= kMidRow) rowSerial<VT, XT>(a, r);
+            const int rs = a.rowPtr[r], len = a.rowPtr[r + 1] - rs;
+            if (len > a.midRow) continue;
+            if (a.sellCol)  // position i - r0 of the wave: chunk (i - r0) / 32, lane (i - r0) % 32
+                rowSerial<VT, XT>(a, r,
+                                  SellRow<VT, XT>{a.sellCol, (const VT *)a.sellVal,
+                                                  a.chunkOff[a.waveChunk[w] + ((i - r0) >> 5)], (i - r0) & 31, len});
+            else
+                rowSerial<VT, XT>(a, r, CrsRow<VT, XT>{a.col, (const VT *)a.val, rs, len});
         }
         // longer rows of this wave: one warp each, distributed over all warps
         // of the grid (rows of a wave are independent, so the passes may
@@ -307,7 +414,7 @@ __global__ void __launch_bounds__(kSweepThreads) kWaveSweep(SweepArgs a) {
             const int len = a.rowPtr[r + 1] - a.rowPtr[r];
             if (len > kHugeRow)
                 rowWarp<VT, XT>(a, r, lane);  // not reached: the plan gives such rows huge waves
-            else if (len > kMidRow)
+            else if (len > a.midRow)
                 rowWarpExact<VT, XT>(a, r, lane);
         }
         if (w + 1 < a.num && !gridBarrier(a.bar, a.status)) return;
@@ -502,14 +609,40 @@ __global__ void __launch_bounds__(kSweepThreads) kLeafSweep(SweepArgs a) {
 }
 
 template <typename K>
-int coopBlocks(K kernel, int want, int capPerSm = 0) {
+int coopBlocks(K kernel, int want, int capPerSm = 0, int threads = kSweepThreads) {
     int dev = 0, sms = 0, occ = 0;
     RACE_CUDA(cudaGetDevice(&dev));
     RACE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    RACE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kSweepThreads, 0));
+    RACE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, 0));
     occ = std::max(occ, 1);
     if (capPerSm > 0) occ = std::min(occ, capPerSm);
     return std::max(1, std::min(sms * occ, want));
+}
+
+// CRS -> SELL copy of the thread rows of a wave plan (DevWaves): one warp
+// per chunk, lane l the chunk's l-th position; rows above midRow entries
+// (run by a warp from the CRS) and positions past the wave are padding
+// (value 0, column the row itself or 0).
+template <typename VT>
+__global__ void kWaveToSell(const int *__restrict__ rowPtr, const int *__restrict__ col, const VT *__restrict__ val,
+                            const int *__restrict__ rows, const int *__restrict__ chunkPos,
+                            const int *__restrict__ chunkEnd, const int *__restrict__ chunkLen,
+                            const long long *__restrict__ chunkOff, int numChunks, int midRow, VT *__restrict__ sval,
+                            int *__restrict__ scol) {
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= numChunks) return;
+    const int lane = threadIdx.x & 31;
+    const int p = chunkPos[c] + lane;
+    const bool live = p < chunkEnd[c];
+    const int r = live ? rows[p] : 0;
+    const int s = live ? rowPtr[r] : 0;
+    int len = live ? rowPtr[r + 1] - s : 0;
+    if (len > midRow) len = 0;
+    for (int k = 0; k < chunkLen[c]; ++k) {
+        const long long o = chunkOff[c] + 32LL * (k & ~3) + 4 * lane + (k & 3);
+        sval[o] = k < len ? val[s + k] : VT(0);
+        scol[o] = k < len ? col[s + k] : r;
+    }
 }
 
 // Blocks per SM of the wave-mode grid. Every wave ends with a grid barrier
@@ -528,8 +661,8 @@ template <typename VT, typename XT>
 void launch(bool waveMode, SweepArgs &a, int maxWork, cudaStream_t s) {
     void *args[] = {&a};
     if (waveMode) {
-        int blocks = coopBlocks(kWaveSweep<VT, XT>, ceilDiv(maxWork, kSweepThreads), waveBlocksPerSm());
-        RACE_CUDA(cudaLaunchCooperativeKernel((void *)kWaveSweep<VT, XT>, blocks, kSweepThreads, args, 0, s));
+        int blocks = coopBlocks(kWaveSweep<VT, XT>, ceilDiv(maxWork, kWaveThreads), waveBlocksPerSm(), kWaveThreads);
+        RACE_CUDA(cudaLaunchCooperativeKernel((void *)kWaveSweep<VT, XT>, blocks, kWaveThreads, args, 0, s));
     } else {
         int blocks = coopBlocks(kLeafSweep<VT, XT>, ceilDiv(maxWork, kWarps));
         RACE_CUDA(cudaLaunchCooperativeKernel((void *)kLeafSweep<VT, XT>, blocks, kSweepThreads, args, 0, s));
@@ -693,6 +826,37 @@ void buildSweepWaves(Engine &e, FuncEntry &f) {
             }
         }
         DevWaves &w = f.waves[dir];
+        // SELL copy of the thread rows: a wave's rows are independent, so
+        // they are sorted by length (longest first, then by row) and cut
+        // into chunks of 32 positions whose width is their longest thread
+        // row (SELL-C-sigma with sigma = the wave)
+        const int mid = std::min(std::max(e.sweepMidRow, 0), kHugeRow);
+        std::vector<int> waveChunk{0}, cPos, cEnd, cLen;
+        std::vector<long long> cOff;
+        long long slots = 0;
+        if (e.sweepSell) {
+            auto rowLen = [&](int r) { return rp[r + 1] - rp[r]; };
+            for (size_t wi = 0; wi < huge.size(); ++wi) {
+                if (!huge[wi]) {
+                    std::sort(rows.begin() + ptr[wi], rows.begin() + ptr[wi + 1], [&](int x, int y) {
+                        return rowLen(x) != rowLen(y) ? rowLen(x) > rowLen(y) : x < y;
+                    });
+                    for (int p0 = ptr[wi]; p0 < ptr[wi + 1]; p0 += 32) {
+                        const int p1 = std::min(p0 + 32, ptr[wi + 1]);
+                        int L = 0;
+                        for (int q = p0; q < p1; ++q)
+                            if (rowLen(rows[q]) <= mid) L = std::max(L, rowLen(rows[q]));
+                        L = (L + 3) & ~3;
+                        cPos.push_back(p0);
+                        cEnd.push_back(p1);
+                        cLen.push_back(L);
+                        cOff.push_back(slots);
+                        slots += 32LL * L;
+                    }
+                }
+                waveChunk.push_back((int)cPos.size());
+            }
+        }
         w.numWaves = (int)huge.size();
         w.maxRows = 0;
         for (int i = 0; i < w.numWaves; ++i) w.maxRows = std::max(w.maxRows, ptr[i + 1] - ptr[i]);
@@ -705,6 +869,44 @@ void buildSweepWaves(Engine &e, FuncEntry &f) {
         w.segBeg.upload(segBeg.empty() ? nullptr : segBeg.data(), std::max<size_t>(segBeg.size(), 1), e.stream);
         w.segEnd.upload(segEnd.empty() ? nullptr : segEnd.data(), std::max<size_t>(segEnd.size(), 1), e.stream);
         w.segScratch.alloc(std::max<size_t>(3 * segPos.size(), 1));
+        w.sell = e.sweepSell;
+        w.sellMidRow = mid;
+        w.sellSlots = slots;
+        if (w.sell) {
+            const int C = (int)cPos.size();
+            w.waveChunk.upload(waveChunk.data(), waveChunk.size(), e.stream);
+            w.chunkOff.upload(cOff.empty() ? nullptr : cOff.data(), std::max(C, 1), e.stream);
+            DevBuf<int> dPos, dEnd, dLen;
+            dPos.upload(cPos.empty() ? nullptr : cPos.data(), std::max(C, 1), e.stream);
+            dEnd.upload(cEnd.empty() ? nullptr : cEnd.data(), std::max(C, 1), e.stream);
+            dLen.upload(cLen.empty() ? nullptr : cLen.data(), std::max(C, 1), e.stream);
+            const size_t vb = f.ops.val_type == RACE_VAL_F64 ? 8 : f.ops.val_type == RACE_VAL_F32 ? 4 : 2;
+            w.sellVal.alloc(std::max<long long>(slots, 4) * vb);
+            w.sellCol.alloc(std::max<long long>(slots, 4));
+            if (C > 0) {
+                const int blocks = ceilDiv(C, 8);
+                switch (f.ops.val_type) {
+                case RACE_VAL_F64:
+                    kWaveToSell<double><<<blocks, 256, 0, e.stream>>>(f.ops.rowPtr, f.ops.col, (const double *)f.ops.val,
+                                                                     w.rows.p, dPos.p, dEnd.p, dLen.p, w.chunkOff.p, C,
+                                                                     mid, (double *)w.sellVal.p, w.sellCol.p);
+                    break;
+                case RACE_VAL_F32:
+                    kWaveToSell<float><<<blocks, 256, 0, e.stream>>>(f.ops.rowPtr, f.ops.col, (const float *)f.ops.val,
+                                                                    w.rows.p, dPos.p, dEnd.p, dLen.p, w.chunkOff.p, C,
+                                                                    mid, (float *)w.sellVal.p, w.sellCol.p);
+                    break;
+                case RACE_VAL_BF16:
+                    kWaveToSell<__nv_bfloat16><<<blocks, 256, 0, e.stream>>>(
+                        f.ops.rowPtr, f.ops.col, (const __nv_bfloat16 *)f.ops.val, w.rows.p, dPos.p, dEnd.p, dLen.p,
+                        w.chunkOff.p, C, mid, (__nv_bfloat16 *)w.sellVal.p, w.sellCol.p);
+                    break;
+                default: throw Error(RACE_ERR_INVALID_ARG, "unknown value type");
+                }
+                RACE_CUDA(cudaGetLastError());
+            }
+            RACE_CUDA(cudaStreamSynchronize(e.stream));  // the temporaries go out of scope
+        }
     }
     RACE_CUDA(cudaStreamSynchronize(e.stream));
 }
@@ -729,6 +931,7 @@ void runSweep(Engine &e, FuncEntry &f, bool rev) {
     const bool waveMode = useWaveMode(e, f, dir);
     SweepArgs a{f.kernel, ops.rowPtr, ops.col, ops.val, ops.x, ops.b, nullptr, nullptr, nullptr, 0,
                 (unsigned *)(e.dStatus.p + 2), e.dStatus.p};
+    a.midRow = std::min(std::max(e.sweepMidRow, 0), kHugeRow);
     int maxWork = 0;
     if (waveMode) {
         DevWaves &w = f.waves[dir];
@@ -742,6 +945,12 @@ void runSweep(Engine &e, FuncEntry &f, bool rev) {
         a.segEnd = w.segEnd.p;
         a.segScratch = w.segScratch.p;
         a.numSegs = w.numSegs;
+        if (w.sell && w.sellMidRow == a.midRow) {
+            a.waveChunk = w.waveChunk.p;
+            a.chunkOff = w.chunkOff.p;
+            a.sellVal = w.sellVal.p;
+            a.sellCol = w.sellCol.p;
+        }
         maxWork = w.maxRows;
     } else {
         DevPhases &d = e.dPhases[dir];

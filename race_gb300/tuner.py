@@ -4,20 +4,23 @@ engine's own parameter search.
 The reference tunes one knob by wall clock: Interface::tuneFunction
 (src/interface.cpp:605-647) runs powers 1..p and keeps the fastest. Its other
 knobs are the cache budget of RACEColor(power, cacheSize, ...)
-(interface.cpp:205) and the power per block. This module searches those
-knobs on the GPU for A^8 x (computed as 8/p chained level-blocked MPK calls
-of power p) and learns from the search:
+(interface.cpp:205), the power per block and the depth of the recursion into
+hopeless regions (RACE_MAX_RECURSION_STAGES, src/matrixPowerRecursive.cpp).
+This module searches those knobs on the GPU for A^8 x (computed as 8/p
+chained MPK calls of power p, each in the engine's default schedule) and
+learns from the search:
 
 * ``CONFIGS``: power per block p in {1, 2, 4, 8} times cache budget in
-  {8, 32, 128, 512} MB (p = 1 takes one budget: it has no blocking);
+  {8, 32, 128, 512} MB times recursion stages in {0, 1, 2} (p = 1 takes one
+  budget and depth: it has no blocking);
 * ``search``: times every config on the engine (median of repetitions);
-  configs whose partition the engine refuses are infeasible (the committed
-  searches predate the partition of hopeless regions: 3 of their 3,900 MPK
-  entries are marked infeasible for that reason);
+  where the default depth's partition has no hopeless region every depth
+  gives the same partition, and the other depths take its time; configs
+  whose partition the engine refuses are infeasible;
 * ``matrix_features`` / ``config_features``: 24 structural features of the
   matrix (sizes, row lengths, index distances, BFS level profile from row 0,
-  RACE's root) and 8 of the config, 32 inputs in total;
-* ``CostModel``: an MLP 32 -> 3 x 128 (ReLU) -> 1 predicting the log time,
+  RACE's root) and 10 of the config, 34 inputs in total;
+* ``CostModel``: an MLP 34 -> 3 x 128 (ReLU) -> 1 predicting the log time,
   trained with the engine's own CUDA kernels (race_mlp_* in the C ABI:
   forward, MSE gradient, Adam); it picks the feasible config with the
   lowest predicted time;
@@ -28,9 +31,11 @@ of power p) and learns from the search:
 A second task, ``SWEEP_TASK``, tunes RACE's coloring for a symmetric
 Gauss-Seidel sweep (forward + backward, FP64, distance-2 coloring): requested
 threads in {64, 256, 1024} times the efficiency threshold RACE_EFFICIENCY in
-{20, 40, 80} (src/level_recursion.cpp:48-70). RACE's other recursion knob,
-RACE_MAX_RECURSION_STAGES, steers the recursive MPK partition, which this
-engine does not build (stage 0 only), so it has nothing to tune here.
+{20, 40, 80} (src/level_recursion.cpp:48-70).
+
+The seeded matrix set (``dataset_matrix``): 3D 7-point and 27-point
+stencils, banded matrices (bandwidth 8-512) with scrambled rows, Chung-Lu
+power-law graphs, n log-uniform in [50k, 2M] rows by default.
 """
 from __future__ import annotations
 
@@ -46,10 +51,11 @@ from . import matgen
 
 TOTAL_POWER = 8
 CACHE_MB = (8, 32, 128, 512)
-CONFIGS = [(1, 512)] + [(p, c) for p in (2, 4, 8) for c in CACHE_MB]
+RECURSION_STAGES = (0, 1, 2)  # RACE_MAX_RECURSION_STAGES; 1 is the default
+CONFIGS = [(1, 512, 1)] + [(p, c, r) for p in (2, 4, 8) for c in CACHE_MB for r in RECURSION_STAGES]
 L2_BYTES = 126.5 * 2 ** 20
 N_MATRIX_FEATURES = 24
-N_CONFIG_FEATURES = 8
+N_CONFIG_FEATURES = 10
 N_FEATURES = N_MATRIX_FEATURES + N_CONFIG_FEATURES
 HIDDEN, HIDDEN_LAYERS = 128, 3
 
@@ -95,7 +101,7 @@ def matrix_features(A) -> np.ndarray:
     return np.asarray(f, np.float32)
 
 
-def config_features(mf: np.ndarray, p: int, cache_mb: float) -> np.ndarray:
+def config_features(mf: np.ndarray, p: int, cache_mb: float, stages: int = 1) -> np.ndarray:
     """Features of one config given the matrix features (log sizes are
     recovered from them)."""
     lp = math.log2(p)
@@ -106,7 +112,9 @@ def config_features(mf: np.ndarray, p: int, cache_mb: float) -> np.ndarray:
     c3 = math.log2(cb / bytes64) / 10 if blocked else 0.0
     f = [lp / 3, 0.0 if blocked else 1.0, (math.log2(cache_mb) / 9) if blocked else 0.0, c3,
          (math.log2(cb / (2 * (p + 1) * maxlev)) / 10) if blocked else 0.0, lp * c3,
-         (math.log2(cb / L2_BYTES) / 5) if blocked else 0.0, TOTAL_POWER / p / 8]
+         (math.log2(cb / L2_BYTES) / 5) if blocked else 0.0, TOTAL_POWER / p / 8,
+         stages / 2 if blocked else 0.0, stages * c3 / 2 if blocked else 0.0]
+    assert len(f) == N_CONFIG_FEATURES
     return np.asarray(f, np.float32)
 
 
@@ -130,31 +138,56 @@ def feature_rows(mf: np.ndarray, task=None) -> np.ndarray:
 
 
 # ---------------------------------------------------------------- search
+def has_hopeless(tree: np.ndarray) -> bool:
+    """Whether an MPK leaf tree (Interface.getPowerTree: count, then per
+    leaf lo, hi, stage, parent, numGroups, groupPtr[numGroups+1],
+    numHopeless, ...) holds hopeless regions: more leaves than the root, or
+    hopeless groups in the root."""
+    if len(tree) == 0:
+        return False
+    if tree[0] > 1:
+        return True
+    ng = int(tree[5])
+    return int(tree[6 + ng + 1]) > 0
+
+
 def search(A, reps: int = 5, warmup: int = 2, stream=None) -> np.ndarray:
     """Seconds of A^8 x per config (np.inf where RACE rejects the
-    partition), timed with CUDA events on the engine's stream."""
+    partition), timed with CUDA events on the engine's stream. One engine
+    per recursion depth; depths other than the default are timed only where
+    the default's partition has hopeless regions."""
     import torch
 
     from . import interface as ri
-    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True)
     times = np.full(len(CONFIGS), np.inf)
-    perm = None
     x0 = torch.tensor(matgen.uniform_vector(A.n, 0), device="cuda")
-    for ci, (p, c) in enumerate(CONFIGS):
+    engines = {}
+
+    def engine(r):
+        if r not in engines:
+            engines[r] = [ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True,
+                                       params={"max_recursion_stages": r}), None, None]
+        return engines[r]
+
+    def timed(r, p, c):
+        """(seconds or inf, whether the partition has hopeless regions)"""
+        eng = engine(r)
+        rc = eng[0]
         if rc.RACEColor(p, c * 1e6) != 0:
-            continue
+            return np.inf, False
+        hopeless = has_hopeless(rc.getPowerTree())
         # The permutation normally stays the one of the first partition; a
         # partition with hopeless regions reorders rows inside groups.
         cur = rc.getPerm()
-        if perm is None or not np.array_equal(cur, perm):
-            perm = cur
-            P = A.permuted(perm, rc.getInvPerm())
-            dm = ri.DeviceCsr.from_csr(P, "cuda", torch.float64)
+        if eng[1] is None or not np.array_equal(cur, eng[1]):
+            eng[1] = cur
+            eng[2] = ri.DeviceCsr.from_csr(A.permuted(cur, rc.getInvPerm()), "cuda", torch.float64)
+        dm = eng[2]
         x = torch.zeros((p + 1) * A.n, dtype=torch.float64, device="cuda")
         fid = rc.registerFunction(ri.MPK, ri.Operands(dm, x), power=p)
         x[: A.n].copy_(x0)
         if rc.executeFunction(fid) != 0:  # also catches an error code returned in place of an id
-            continue
+            return np.inf, hopeless
 
         def run():
             x[: A.n].copy_(x0)
@@ -174,11 +207,63 @@ def search(A, reps: int = 5, warmup: int = 2, stream=None) -> np.ndarray:
             e1.synchronize()
             ts.append(e0.elapsed_time(e1) * 1e-3)
         if rc.getStatus() != 0:
-            continue
-        times[ci] = float(np.median(ts))
-        del x
-    rc.close()
+            return np.inf, hopeless
+        return float(np.median(ts)), hopeless
+
+    index = {cfg: i for i, cfg in enumerate(CONFIGS)}
+    times[index[(1, 512, 1)]] = timed(1, 1, 512)[0]
+    for p in (2, 4, 8):
+        for c in CACHE_MB:
+            t, hopeless = timed(1, p, c)
+            times[index[(p, c, 1)]] = t
+            for r in RECURSION_STAGES:
+                if r != 1:
+                    times[index[(p, c, r)]] = timed(r, p, c)[0] if hopeless else t
+    for eng in engines.values():
+        eng[0].close()
     return times
+
+
+def time_config(A, config, reps: int = 5, warmup: int = 2) -> float:
+    """Seconds of A^8 x in one MPK config (p, cacheMB, recursion stages) on
+    a fresh engine, timed as the search times it (np.inf if refused)."""
+    import torch
+
+    from . import interface as ri
+    p, c, r = config
+    rc = ri.Interface(A.n, 1, ri.POWER, A.row_ptr, A.col, symm_hint=True, params={"max_recursion_stages": r})
+    try:
+        if rc.RACEColor(p, c * 1e6) != 0:
+            return np.inf
+        P = A.permuted(rc.getPerm(), rc.getInvPerm())
+        dm = ri.DeviceCsr.from_csr(P, "cuda", torch.float64)
+        x0 = torch.tensor(matgen.uniform_vector(A.n, 0), device="cuda")
+        x = torch.zeros((p + 1) * A.n, dtype=torch.float64, device="cuda")
+        fid = rc.registerFunction(ri.MPK, ri.Operands(dm, x), power=p)
+        x[: A.n].copy_(x0)
+        if rc.executeFunction(fid) != 0:
+            return np.inf
+
+        def run():
+            x[: A.n].copy_(x0)
+            for j in range(TOTAL_POWER // p):
+                if j:
+                    x[: A.n].copy_(x[p * A.n:])
+                rc.executeFunctionAsync(fid)
+
+        for _ in range(warmup):
+            run()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            run()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return float(np.median(ts)) if rc.getStatus() == 0 else np.inf
+    finally:
+        rc.close()
 
 
 def search_sweep(A, reps: int = 5, warmup: int = 2) -> np.ndarray:
@@ -222,7 +307,7 @@ def search_sweep(A, reps: int = 5, warmup: int = 2) -> np.ndarray:
     return times
 
 
-def dataset_matrix(index: int, seed: int = 0, nmin: int = 20_000, nmax: int = 400_000):
+def dataset_matrix(index: int, seed: int = 0, nmin: int = 50_000, nmax: int = 2_000_000):
     """Matrix `index` of the seeded tuning set: 3D 7-point or 27-point
     stencil, random banded (bandwidth 8-512, rows scrambled) or power-law
     graph, n log-uniform in [nmin, nmax]."""
@@ -380,8 +465,9 @@ class CostModel:
     """MLP regression of log time on (matrix, config) features."""
 
     def __init__(self, seed: int = 0, task: Task = None):
-        self.net = Mlp(seed=seed)
         self.task = task or MPK_TASK
+        n_in = feature_rows(np.zeros(N_MATRIX_FEATURES, np.float32), self.task).shape[1]
+        self.net = Mlp(n_in=n_in, seed=seed)
         self.mu = 0.0
         self.sd = 1.0
 
@@ -395,8 +481,12 @@ class CostModel:
         return np.concatenate(X).astype(np.float32), np.concatenate(T).astype(np.float32)
 
     def fit(self, ds: Dataset, epochs: int = 300, batch: int = 64, lr: float = 1e-3, seed: int = 0):
+        """Adam on the MSE of the normalised log times; the batch grows with
+        the data (at most ~128 steps an epoch) so large searches train in
+        seconds."""
         import torch
         X, T = self._rows(ds)
+        batch = max(batch, len(T) // 128)
         self.mu, self.sd = float(T.mean()), float(T.std() + 1e-6)
         Xt = torch.tensor(X, device="cuda")
         Tt = torch.tensor(((T - self.mu) / self.sd)[:, None], device="cuda")
@@ -466,29 +556,65 @@ class Tuner:
         return self.task.configs[c], {"how": "mlp", "seconds": time.perf_counter() - t0}
 
 
-def build_dataset(count: int, seed: int = 0, nmin: int = 20_000, nmax: int = 400_000, log=None,
-                  out=None, save_every: int = 10, task: str = "mpk") -> Dataset:
-    """Search `count` matrices of the seeded set for one task; with `out`,
-    the partial dataset is saved every `save_every` matrices."""
+def _generate(job):
+    i, seed, nmin, nmax = job
+    fam, A = dataset_matrix(i, seed, nmin, nmax)
+    return i, fam, A, matrix_features(A)
+
+
+def build_dataset(count: int, seed: int = 0, nmin: int = 50_000, nmax: int = 2_000_000, log=None,
+                  out=None, save_every: int = 10, task: str = "mpk", start: int = 0, workers: int = 0,
+                  max_seconds: float = math.inf) -> Dataset:
+    """Search matrices start .. start+count-1 of the seeded set for one task;
+    with `out`, the partial dataset is saved every `save_every` matrices.
+    workers > 0 makes the matrices and their features in that many spawned
+    processes, at most 2 x workers ahead of the GPU search; the search stops
+    after the matrix that passes max_seconds."""
+    import collections
+
     feats, times, fams, sizes = [], [], [], []
     tk = TASKS[task]
+    jobs = [(i, seed, nmin, nmax) for i in range(start, start + count)]
 
     def ds():
         return Dataset(np.stack(feats), np.stack(times), np.asarray(fams), np.asarray(sizes, np.int64), task)
 
-    for i in range(count):
-        fam, A = dataset_matrix(i, seed, nmin, nmax)
+    def made():
+        if workers <= 0:
+            for j in jobs:
+                yield _generate(j)
+            return
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(workers) as pool:
+            it = iter(jobs)
+            pending = collections.deque(pool.apply_async(_generate, (j,)) for j, _ in zip(it, range(2 * workers)))
+            while pending:
+                r = pending.popleft().get()
+                nxt = next(it, None)
+                if nxt is not None:
+                    pending.append(pool.apply_async(_generate, (nxt,)))
+                yield r
+
+    t_start = time.perf_counter()
+    for i, fam, A, mf in made():
         t0 = time.perf_counter()
-        tr = tk.search(A)
-        feats.append(matrix_features(A))
+        try:
+            tr = tk.search(A)
+        except Exception as exc:  # one failing matrix is recorded as infeasible, the search goes on
+            if log:
+                log(f"{i} {fam} n={A.n}: search failed: {exc}")
+            tr = np.full(len(tk.configs), np.inf)
+        feats.append(mf)
         times.append(tr)
         fams.append(fam)
         sizes.append((A.n, A.nnz))
         if log:
             log(f"{i} {fam} n={A.n} nnz={A.nnz} best={tk.configs[int(np.argmin(tr))]} "
                 f"{time.perf_counter() - t0:.1f}s")
-        if out is not None and (i + 1) % save_every == 0:
+        if out is not None and len(times) % save_every == 0:
             ds().save(out)
+        if time.perf_counter() - t_start > max_seconds:
+            break
     d = ds()
     if out is not None:
         d.save(out)
@@ -502,11 +628,14 @@ def main(argv=None):
                     help="search: time every config of --count matrices; merge: concatenate saved datasets "
                          "(the inputs) of one task into --out")
     ap.add_argument("inputs", nargs="*")
-    ap.add_argument("--count", type=int, default=300)
+    ap.add_argument("--count", type=int, default=2000)
+    ap.add_argument("--start", type=int, default=0, help="index of the first matrix of the seeded set")
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--nmin", type=int, default=20_000)
-    ap.add_argument("--nmax", type=int, default=400_000)
+    ap.add_argument("--nmin", type=int, default=50_000)
+    ap.add_argument("--nmax", type=int, default=2_000_000)
     ap.add_argument("--task", choices=sorted(TASKS), default="mpk")
+    ap.add_argument("--workers", type=int, default=0, help="processes that make the matrices ahead of the search")
+    ap.add_argument("--max-seconds", type=float, default=math.inf, help="stop the search after this long")
     ap.add_argument("--out", required=True)
     a = ap.parse_intermixed_args(argv)
     if a.command == "merge":
@@ -516,7 +645,8 @@ def main(argv=None):
                 np.concatenate([d.families for d in parts]), np.concatenate([d.sizes for d in parts]),
                 parts[0].task).save(a.out)
         return
-    build_dataset(a.count, a.seed, a.nmin, a.nmax, log=lambda s: print(s, flush=True), out=a.out, task=a.task)
+    build_dataset(a.count, a.seed, a.nmin, a.nmax, log=lambda s: print(s, flush=True), out=a.out, task=a.task,
+                  start=a.start, workers=a.workers, max_seconds=a.max_seconds)
 
 
 if __name__ == "__main__":

@@ -51,7 +51,7 @@ def test_mlp_adam_training_fits_a_function():
 def test_cost_model_beats_best_fixed_config_on_held_out_matrices():
     ds = tuner.Dataset.load(GOLDEN)
     n = len(ds.times)
-    held = np.arange(n) % 5 == 4           # every fifth matrix is held out
+    held = np.arange(n) % 10 == 9          # every tenth matrix is held out (200 of 2,000)
     train, test = ds.subset(~held), ds.subset(held)
     model = tuner.CostModel(seed=0)
     hist = model.fit(train, epochs=300, seed=0)

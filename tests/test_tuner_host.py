@@ -12,7 +12,9 @@ def test_features_deterministic_and_finite():
     assert f1.shape == (tuner.N_MATRIX_FEATURES,) and np.array_equal(f1, f2)
     for task in (tuner.MPK_TASK, tuner.SWEEP_TASK):
         rows = tuner.feature_rows(f1, task)
-        assert rows.shape == (len(task.configs), tuner.N_FEATURES)
+        assert rows.shape[0] == len(task.configs) and rows.shape[1] > tuner.N_MATRIX_FEATURES
+        if task is tuner.MPK_TASK:
+            assert rows.shape[1] == tuner.N_FEATURES
         assert np.isfinite(rows).all()
         # configs are distinguishable by their features
         assert len({r.tobytes() for r in rows[:, tuner.N_MATRIX_FEATURES:]}) == len(task.configs)
@@ -63,23 +65,35 @@ def test_regret_and_best_fixed_config():
     assert tuner.best_fixed_config(ds) == 2
 
 
-def test_tuning_matrices_have_no_hopeless_regions():
-    """The recursion depth (RACE_MAX_RECURSION_STAGES) changes a partition
-    only where two consecutive levels exceed the budget by more than the
-    cut-off (50). On the seeded tuning matrices none does at any searched
-    power and budget, so the depth is not a tuning knob there (the first
-    matrices up to at least 8 and all four families; the oracle's BFS
-    levels)."""
-    from oracle import oracle as orc
-    families = set()
-    idx = 0
-    while idx < 8 or len(families) < 4:
-        fam, A = tuner.dataset_matrix(idx)
-        idx += 1
-        families.add(fam)
-        _, _, lr, ln, _ = orc.traverse(A, 3, 0, A.n)
-        lp = np.concatenate([[0], np.cumsum(lr)]).astype(np.int32)
-        for p, c in tuner.CONFIGS:
-            part = orc.mpk_partition(p, A.n, A.nnz, c * 1e6, 2.0, 50, lp, ln)
-            assert part is not None and part[1].size == 0, (idx - 1, fam, p, c)
-    assert families == {"lap7", "st27", "band", "plaw"}
+def test_recursion_depth_configs_and_hopeless_trees():
+    """Every blocked (power, budget) pair is searched at recursion depths 0,
+    1 and 2 (RACE_MAX_RECURSION_STAGES), distinguishable by their features;
+    the search times the other depths only where the default depth's leaf
+    tree shows hopeless regions (more than the root, or hopeless groups in
+    it)."""
+    assert (1, 512, 1) in tuner.CONFIGS
+    for p in (2, 4, 8):
+        for c in tuner.CACHE_MB:
+            assert all((p, c, r) in tuner.CONFIGS for r in tuner.RECURSION_STAGES)
+    # trees: count, then lo, hi, stage, parent, numGroups, groupPtr..., numHopeless, hopeless...
+    root_only = np.array([1, 0, 100, 0, -1, 2, 0, 40, 100, 0])
+    root_hopeless = np.array([1, 0, 100, 0, -1, 3, 0, 30, 70, 100, 1, 1])
+    two_leaves = np.array([2, 0, 100, 0, -1, 3, 0, 30, 70, 100, 1, 1, 30, 70, 1, 0, 1, 0, 40, 0])
+    assert not tuner.has_hopeless(root_only)
+    assert tuner.has_hopeless(root_hopeless)
+    assert tuner.has_hopeless(two_leaves)
+    assert not tuner.has_hopeless(np.zeros(0, np.int64))
+
+
+def test_seeded_set_covers_the_configured_sizes_and_families():
+    """The default tuning set: n log-uniform in [50k, 2M] rows, the four
+    families (stencils 7/27-point, scrambled banded, power-law); checked on
+    the seeds alone (no matrix is built)."""
+    import math
+    fams, sizes = set(), []
+    for i in range(400):
+        rng = np.random.Generator(np.random.PCG64([0, i]))
+        fams.add(int(rng.integers(0, 4)))
+        sizes.append(int(math.exp(rng.uniform(math.log(50_000), math.log(2_000_000)))))
+    assert fams == {0, 1, 2, 3}
+    assert 50_000 <= min(sizes) < 60_000 and 1_700_000 < max(sizes) <= 2_000_000
