@@ -834,14 +834,14 @@ def bench_tuner(torch, retime: int = 8):
             rows = sorted(rows, key=lambda i: ds.sizes[i][0])[:retime]
             regrets, details = [], []
             for i in rows:
-                fam, A = tuner.dataset_matrix(int(i))
+                fam, A = tuner.dataset_matrix(int(ds.index[i]))
                 feas = np.isfinite(ds.times[i])
                 pick = model.choose(ds.features[i], feas)
                 best = int(np.argmin(ds.times[i]))
                 t_pick = tuner.time_config(A, tuner.CONFIGS[pick])
                 t_best = t_pick if best == pick else tuner.time_config(A, tuner.CONFIGS[best])
                 regrets.append(t_pick / min(t_pick, t_best) - 1.0)
-                details.append({"matrix": int(i), "family": fam, "n": A.n, "pick": list(tuner.CONFIGS[pick]),
+                details.append({"matrix": int(ds.index[i]), "family": fam, "n": A.n, "pick": list(tuner.CONFIGS[pick]),
                                 "searched_best": list(tuner.CONFIGS[best]), "t_pick_ms": t_pick * 1e3,
                                 "t_best_ms": t_best * 1e3})
             res["retimed_here"] = {"matrices": len(regrets), "mean_regret": float(np.mean(regrets)) if regrets else None,

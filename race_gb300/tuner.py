@@ -440,21 +440,28 @@ class Dataset:
     families: np.ndarray
     sizes: np.ndarray      # (matrices, 2): n, nnz
     task: str = "mpk"      # configs of the times' columns: TASKS[task].configs
+    index: Optional[np.ndarray] = None  # each row's matrix in the seeded set (dataset_matrix)
+
+    def __post_init__(self):
+        if self.index is None:
+            self.index = np.arange(len(self.times), dtype=np.int64)
 
     def save(self, path):
         np.savez_compressed(path, features=self.features, times=self.times, families=self.families,
                             sizes=self.sizes, configs=np.asarray(TASKS[self.task].configs),
-                            task=np.array(self.task))
+                            task=np.array(self.task), index=np.asarray(self.index, np.int64))
 
     @staticmethod
     def load(path) -> "Dataset":
         d = np.load(path)
         task = str(d["task"]) if "task" in d.files else "mpk"
         assert [tuple(c) for c in d["configs"]] == [tuple(c) for c in TASKS[task].configs], "config space changed"
-        return Dataset(d["features"], d["times"], d["families"], d["sizes"], task)
+        return Dataset(d["features"], d["times"], d["families"], d["sizes"], task,
+                       d["index"] if "index" in d.files else None)
 
     def subset(self, idx) -> "Dataset":
-        return Dataset(self.features[idx], self.times[idx], self.families[idx], self.sizes[idx], self.task)
+        return Dataset(self.features[idx], self.times[idx], self.families[idx], self.sizes[idx], self.task,
+                       self.index[idx])
 
 
 def regret(times_row: np.ndarray, choice: int) -> float:
@@ -571,13 +578,15 @@ def build_dataset(count: int, seed: int = 0, nmin: int = 50_000, nmax: int = 2_0
     processes, at most 2 x workers ahead of the GPU search; the search stops
     after the matrix that passes max_seconds."""
     import collections
+    import itertools
 
-    feats, times, fams, sizes = [], [], [], []
+    feats, times, fams, sizes, idx = [], [], [], [], []
     tk = TASKS[task]
     jobs = [(i, seed, nmin, nmax) for i in range(start, start + count)]
 
     def ds():
-        return Dataset(np.stack(feats), np.stack(times), np.asarray(fams), np.asarray(sizes, np.int64), task)
+        return Dataset(np.stack(feats), np.stack(times), np.asarray(fams), np.asarray(sizes, np.int64), task,
+                       np.asarray(idx, np.int64))
 
     def made():
         if workers <= 0:
@@ -587,7 +596,7 @@ def build_dataset(count: int, seed: int = 0, nmin: int = 50_000, nmax: int = 2_0
         import multiprocessing as mp
         with mp.get_context("spawn").Pool(workers) as pool:
             it = iter(jobs)
-            pending = collections.deque(pool.apply_async(_generate, (j,)) for j, _ in zip(it, range(2 * workers)))
+            pending = collections.deque(pool.apply_async(_generate, (j,)) for j in itertools.islice(it, 2 * workers))
             while pending:
                 r = pending.popleft().get()
                 nxt = next(it, None)
@@ -608,6 +617,7 @@ def build_dataset(count: int, seed: int = 0, nmin: int = 50_000, nmax: int = 2_0
         times.append(tr)
         fams.append(fam)
         sizes.append((A.n, A.nnz))
+        idx.append(i)
         if log:
             log(f"{i} {fam} n={A.n} nnz={A.nnz} best={tk.configs[int(np.argmin(tr))]} "
                 f"{time.perf_counter() - t0:.1f}s")
@@ -643,7 +653,7 @@ def main(argv=None):
         assert parts and len({d.task for d in parts}) == 1, "merge needs datasets of one task"
         Dataset(np.concatenate([d.features for d in parts]), np.concatenate([d.times for d in parts]),
                 np.concatenate([d.families for d in parts]), np.concatenate([d.sizes for d in parts]),
-                parts[0].task).save(a.out)
+                parts[0].task, np.concatenate([d.index for d in parts])).save(a.out)
         return
     build_dataset(a.count, a.seed, a.nmin, a.nmax, log=lambda s: print(s, flush=True), out=a.out, task=a.task,
                   start=a.start, workers=a.workers, max_seconds=a.max_seconds)

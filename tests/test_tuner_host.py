@@ -41,6 +41,12 @@ def test_dataset_roundtrip_and_merge(tmp_path):
     m = tuner.Dataset.load(pm)
     assert m.task == "symmgs" and m.times.shape == (7, len(tuner.SWEEP_CONFIGS))
     np.testing.assert_array_equal(m.times[3:], b.times)
+    # each row keeps the index of its matrix in the seeded set
+    c = tuner.Dataset(a.features, a.times, a.families, a.sizes, "symmgs", np.array([4, 9, 11]))
+    c.save(pa)
+    np.testing.assert_array_equal(tuner.Dataset.load(pa).index, [4, 9, 11])
+    np.testing.assert_array_equal(tuner.Dataset.load(pa).subset(np.array([False, True, True])).index, [9, 11])
+    np.testing.assert_array_equal(m.index, [0, 1, 2, 0, 1, 2, 3])
 
 
 def test_committed_search_files_match_config_spaces():
@@ -52,6 +58,7 @@ def test_committed_search_files_match_config_spaces():
         d = tuner.Dataset.load(g / name)
         assert d.task == task and d.times.shape[1] == len(tuner.TASKS[task].configs)
         assert (d.times[np.isfinite(d.times)] > 0).all()
+        assert len(np.unique(d.index)) == len(d.index) and (np.diff(d.index) > 0).all()
 
 
 def test_regret_and_best_fixed_config():
