@@ -817,9 +817,7 @@ def bench_tuner(torch, retime: int = 8):
         if not path.exists():
             continue
         ds = tuner.Dataset.load(path)
-        # held out: every tenth matrix of the MPK set (200 of 2,000), every
-        # fifth of the coloring set
-        held = np.arange(len(ds.times)) % (10 if name == "mpk" else 5) == (9 if name == "mpk" else 4)
+        held = tuner.held_out(len(ds.times), ds.task)
         train, test = ds.subset(~held), ds.subset(held)
         torch.cuda.synchronize()
         t0 = time.perf_counter()

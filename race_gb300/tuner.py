@@ -469,12 +469,16 @@ def regret(times_row: np.ndarray, choice: int) -> float:
 
 
 class CostModel:
-    """MLP regression of log time on (matrix, config) features."""
+    """MLP regression of log time on (matrix, config) features: an ensemble
+    of `members` networks from consecutive seeds, trained alike, whose
+    predictions are averaged (in the normalised log domain), which steadies
+    the choice between seeds."""
 
-    def __init__(self, seed: int = 0, task: Task = None):
+    def __init__(self, seed: int = 0, task: Task = None, members: int = 3):
         self.task = task or MPK_TASK
         n_in = feature_rows(np.zeros(N_MATRIX_FEATURES, np.float32), self.task).shape[1]
-        self.net = Mlp(n_in=n_in, seed=seed)
+        self.seed = seed
+        self.nets = [Mlp(n_in=n_in, seed=seed + m) for m in range(max(1, members))]
         self.mu = 0.0
         self.sd = 1.0
 
@@ -497,12 +501,15 @@ class CostModel:
         self.mu, self.sd = float(T.mean()), float(T.std() + 1e-6)
         Xt = torch.tensor(X, device="cuda")
         Tt = torch.tensor(((T - self.mu) / self.sd)[:, None], device="cuda")
-        return self.net.train(Xt, Tt, epochs=epochs, batch=batch, lr=lr, seed=seed)
+        hists = [net.train(Xt, Tt, epochs=epochs, batch=batch, lr=lr, seed=seed + m)
+                 for m, net in enumerate(self.nets)]
+        return [float(np.mean(h)) for h in zip(*hists)]
 
     def predict(self, mf: np.ndarray) -> np.ndarray:
-        """Predicted seconds of every config."""
+        """Predicted seconds of every config (the members' mean)."""
         import torch
-        y = self.net.forward(torch.tensor(feature_rows(mf, self.task), device="cuda")).cpu().numpy()[:, 0]
+        rows = torch.tensor(feature_rows(mf, self.task), device="cuda")
+        y = np.mean([net.forward(rows).cpu().numpy()[:, 0] for net in self.nets], axis=0)
         return np.exp(y * self.sd + self.mu)
 
     def choose(self, mf: np.ndarray, feasible: Optional[np.ndarray] = None) -> int:
@@ -510,6 +517,15 @@ class CostModel:
         if feasible is not None:
             pred = np.where(feasible, pred, np.inf)
         return int(np.argmin(pred))
+
+
+def held_out(count: int, task: str = "mpk") -> np.ndarray:
+    """The evaluation split: every k-th row is held out, k = count // 200
+    (at least 2) for the MPK task, so that 200 of the configured 2,000
+    matrices (and at least 200 of any set of 400 or more) are held out, and
+    every fifth row for the coloring task."""
+    k = max(2, count // 200) if task == "mpk" else 5
+    return np.arange(count) % k == k - 1
 
 
 def best_fixed_config(ds: Dataset) -> int:
@@ -563,6 +579,16 @@ class Tuner:
         return self.task.configs[c], {"how": "mlp", "seconds": time.perf_counter() - t0}
 
 
+def _lower_priority():
+    """Pool initializer: matrix generation yields the host to the search
+    process, whose launch timing it would otherwise perturb."""
+    import os
+    try:
+        os.nice(19)
+    except OSError:
+        pass
+
+
 def _generate(job):
     i, seed, nmin, nmax = job
     fam, A = dataset_matrix(i, seed, nmin, nmax)
@@ -594,7 +620,7 @@ def build_dataset(count: int, seed: int = 0, nmin: int = 50_000, nmax: int = 2_0
                 yield _generate(j)
             return
         import multiprocessing as mp
-        with mp.get_context("spawn").Pool(workers) as pool:
+        with mp.get_context("spawn").Pool(workers, initializer=_lower_priority) as pool:
             it = iter(jobs)
             pending = collections.deque(pool.apply_async(_generate, (j,)) for j in itertools.islice(it, 2 * workers))
             while pending:
