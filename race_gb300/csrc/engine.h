@@ -203,12 +203,11 @@ class Engine {
     // per leaf), SWEEP_GATHER
     int sweepMode = SWEEP_AUTO;
     // wave mode: rows of up to this many entries run one thread each, longer
-    // ones (up to 512) one warp each; both keep the sequential order. With
-    // sweepSell the thread rows read a SELL copy in plan order (coalesced
-    // vector loads) instead of the caller's CRS. 16 and SELL were the
-    // fastest measured (4.2M-row power-law GS, FP32: 43.7 ms per symmetric
-    // sweep against 50.5 ms with 32 and CRS).
-    int sweepMidRow = 16;
+    // ones (up to 512) one warp each; both keep the sequential order (-1:
+    // 16 for FP64 vectors, 8 for FP32, the fastest measured on the 4.2M-row
+    // power-law GS). With sweepSell the thread rows read a SELL copy in plan
+    // order (coalesced vector loads) instead of the caller's CRS.
+    int sweepMidRow = -1;
     bool sweepSell = true;
 
     // coloring results

@@ -291,15 +291,32 @@ __device__ bool hugeWave(const SweepArgs &a, int r0, int r1, int gw, int nw, int
 
 // Entries [jb, e) of a row, folded in order by every lane of a warp: each
 // round gathers up to kFoldBlocks x 32 entries at once (all loads in
-// flight), then applies f(value, x[col]) to them in the row's order through
-// broadcasts, so every lane runs the same sequential chain.
+// flight), stages the (value, x) pairs in the warp's shared memory, then
+// every lane applies f(value, x[col]) to them in the row's order, reading
+// the pairs as broadcasts (the reads do not depend on the running sum, so
+// they pipeline), so every lane runs the same sequential chain. Called by
+// whole warps of kWaveSweep only.
 constexpr int kFoldBlocks = 8;
+
+template <typename XT>
+struct FoldStage {
+    XT v[kWaveThreads / 32][32 * kFoldBlocks];
+    XT x[kWaveThreads / 32][32 * kFoldBlocks];
+};
+
+// One stage per block and accumulation type, shared by every fold body.
+template <typename XT>
+__device__ __forceinline__ FoldStage<XT> &foldStage() {
+    __shared__ FoldStage<XT> st;
+    return st;
+}
 
 template <typename VT, typename XT, typename F>
 __device__ __forceinline__ void foldRow(const SweepArgs &a, int jb, int e, int lane, F &&f) {
-    constexpr unsigned kFull = 0xffffffffu;
+    FoldStage<XT> &st = foldStage<XT>();
     const VT *val = (const VT *)a.val;
     const XT *x = (const XT *)a.x;
+    const int w = threadIdx.x >> 5;
     for (int jr = jb; jr < e; jr += 32 * kFoldBlocks) {
         XT v[kFoldBlocks], xv[kFoldBlocks];
 #pragma unroll
@@ -309,11 +326,16 @@ __device__ __forceinline__ void foldRow(const SweepArgs &a, int jb, int e, int l
             v[k] = ok ? ld<VT, XT>(val, j) : XT(0);
             xv[k] = ok ? x[a.col[j]] : XT(0);
         }
+        __syncwarp();  // the previous round's reads are done
 #pragma unroll
         for (int k = 0; k < kFoldBlocks; ++k) {
-            const int m = min(32, e - (jr + 32 * k));
-            for (int q = 0; q < m; ++q) f(__shfl_sync(kFull, v[k], q), __shfl_sync(kFull, xv[k], q));
+            st.v[w][32 * k + lane] = v[k];
+            st.x[w][32 * k + lane] = xv[k];
         }
+        __syncwarp();
+        const int m = min(32 * kFoldBlocks, e - jr);
+#pragma unroll 8
+        for (int q = 0; q < m; ++q) f(st.v[w][q], st.x[w][q]);
     }
 }
 
@@ -777,6 +799,12 @@ void uploadPhases(Engine &e, int dir) {
     d.leafHi.upload(pt.leafHi.data(), std::max<size_t>(pt.leafHi.size(), 1), e.stream);
 }
 
+// Thread-row limit of a sweep function (Engine::sweepMidRow).
+static int midRowOf(const Engine &e, const FuncEntry &f) {
+    const int m = e.sweepMidRow >= 0 ? e.sweepMidRow : (f.ops.vec_type == RACE_VAL_F64 ? 16 : 8);
+    return std::min(m, kHugeRow);
+}
+
 // Wave plans of a registered sweep function for both directions.
 void buildSweepWaves(Engine &e, FuncEntry &f) {
     const int n = f.ops.n;
@@ -830,7 +858,7 @@ void buildSweepWaves(Engine &e, FuncEntry &f) {
         // they are sorted by length (longest first, then by row) and cut
         // into chunks of 32 positions whose width is their longest thread
         // row (SELL-C-sigma with sigma = the wave)
-        const int mid = std::min(std::max(e.sweepMidRow, 0), kHugeRow);
+        const int mid = midRowOf(e, f);
         std::vector<int> waveChunk{0}, cPos, cEnd, cLen;
         std::vector<long long> cOff;
         long long slots = 0;
@@ -931,7 +959,7 @@ void runSweep(Engine &e, FuncEntry &f, bool rev) {
     const bool waveMode = useWaveMode(e, f, dir);
     SweepArgs a{f.kernel, ops.rowPtr, ops.col, ops.val, ops.x, ops.b, nullptr, nullptr, nullptr, 0,
                 (unsigned *)(e.dStatus.p + 2), e.dStatus.p};
-    a.midRow = std::min(std::max(e.sweepMidRow, 0), kHugeRow);
+    a.midRow = midRowOf(e, f);
     int maxWork = 0;
     if (waveMode) {
         DevWaves &w = f.waves[dir];

@@ -289,7 +289,7 @@ Engine::Engine(int nrow, int nthreads, int dist_, const int *rowPtr, const int *
     if (const char *d = getenv("RACE_GPU_MPK_DIES")) mpkDieQueues = atoi(d) != 1;
     if (const char *h = getenv("RACE_GPU_MPK_HINTS")) mpkHints = atoi(h) ? 1 : 0;
     if (const char *c16 = getenv("RACE_GPU_MPK_COL16")) mpkCol16 = atoi(c16) != 0;
-    if (const char *mr = getenv("RACE_GPU_SWEEP_MIDROW")) sweepMidRow = std::max(0, atoi(mr));
+    if (const char *mr = getenv("RACE_GPU_SWEEP_MIDROW")) sweepMidRow = std::max(-1, atoi(mr));
     if (const char *ss = getenv("RACE_GPU_SWEEP_SELL")) sweepSell = atoi(ss) != 0;
     if (const char *sc = getenv("RACE_GPU_MPK_SCHEDULE"))
         mpkSchedule = std::string(sc) == "wavefront" ? RACE_MPK_WAVEFRONT
