@@ -110,6 +110,44 @@ def test_sweeps_match_oracle(golden, mats, m, d, t):
             assert _rel_err(out, out_ref) <= 1e-12, (kern, rev, _rel_err(out, out_ref))
 
 
+@pytest.mark.parametrize("m", ["plaw_20k", "band_5k"])
+def test_wave_sweep_layouts_agree(mats, monkeypatch, m):
+    """Wave-mode sweeps hand a row to one thread or to a warp by its length
+    (RACE_GPU_SWEEP_MIDROW) and read thread rows from the SELL copy of the
+    wave plan or from the caller's CRS (RACE_GPU_SWEEP_SELL); every
+    combination keeps each row's operation order, so GS, Kaczmarz and SpMV
+    give the same vectors bit for bit, with FP64 and FP32 values."""
+    A = mats[m]
+    x0 = matgen.uniform_vector(A.n, 0)
+    b0 = matgen.uniform_vector(A.n, 1)
+    ref = {}
+    for sell in ("1", "0"):
+        for mid in ("0", "8", "32", "-1"):
+            monkeypatch.setenv("RACE_GPU_SWEEP_SELL", sell)
+            monkeypatch.setenv("RACE_GPU_SWEEP_MIDROW", mid)
+            rc = ri.Interface(A.n, 64, ri.TWO, A.row_ptr, A.col, symm_hint=True)
+            assert rc.RACEColor() == 0
+            rc.setSweepMode(ri.SWEEP_WAVE)
+            P = A.permuted(rc.getPerm(), rc.getInvPerm())
+            for vdt in (torch.float64, torch.float32):
+                xdt = torch.float64 if vdt == torch.float64 else torch.float32
+                for kern in (ri.GS, ri.KACZ, ri.SPMV):
+                    x = torch.tensor(x0, dtype=xdt, device="cuda")
+                    b = torch.zeros(A.n, dtype=xdt, device="cuda") if kern == ri.SPMV else \
+                        torch.tensor(b0, dtype=xdt, device="cuda")
+                    fid = rc.registerFunction(kern, ri.Operands(_upload(P, vdt), x, b))
+                    assert fid >= 0 and rc.getSweepInfo(fid)["wave_mode"]
+                    assert rc.executeFunction(fid) == 0
+                    if kern != ri.SPMV:
+                        assert rc.executeFunction(fid, True) == 0
+                    out = (b if kern == ri.SPMV else x).cpu().numpy()
+                    key = (str(vdt), kern)
+                    if key not in ref:
+                        ref[key] = out
+                    assert np.array_equal(out, ref[key]), (sell, mid, key)
+            rc.close()
+
+
 @pytest.mark.parametrize("m,d,t", [("lap7_32", 2, 1024), ("aniso9_100x80", 1, 16), ("plaw_3k", 1, 32)])
 def test_leaf_mode_sweeps(golden, mats, m, d, t):
     """Leaf mode (warp per RACE leaf, shuffle reductions): within 1e-12 of
