@@ -27,8 +27,9 @@ struct DevPhases {
 };
 
 // Schedule and layout of one registered matrix-power function: the
-// permuted matrix in SELL-32 chunks inside RACE's level groups, the chunks'
-// dependency ranges, and the (power, chunk) work items in wavefront order.
+// permuted matrix in SELL-32 chunks inside RACE's level groups (4-entry
+// groups, 16- or 32-bit columns), the chunks' dependency ranges, and the
+// runs of (power, chunk) items in wavefront order, one queue per L2 die.
 struct MpkPlan {
     int numChunks = 0;          // SELL-32 chunks (<= 32 rows, inside one level group)
     int power = 0;
