@@ -104,3 +104,24 @@ def test_seeded_set_covers_the_configured_sizes_and_families():
         sizes.append(int(math.exp(rng.uniform(math.log(50_000), math.log(2_000_000)))))
     assert fams == {0, 1, 2, 3}
     assert 50_000 <= min(sizes) < 60_000 and 1_700_000 < max(sizes) <= 2_000_000
+
+
+def test_build_dataset_keeps_every_matrix_in_order(monkeypatch):
+    """The search over spawned matrix-making processes (workers > 0) sees
+    matrices start .. start+count-1, each once and in order, and records
+    their indices; the GPU search is replaced by a stand-in here."""
+    calls = []
+
+    def fake_search(A):
+        calls.append(A.n)
+        return np.full(len(tuner.SWEEP_CONFIGS), 1e-3)
+
+    monkeypatch.setitem(tuner.TASKS, "fake", tuner.Task("fake", tuner.SWEEP_CONFIGS, tuner.sweep_config_features,
+                                                        fake_search))
+    monkeypatch.setitem(tuner.TASKS, "symmgs", tuner.TASKS["fake"])
+    for workers in (0, 2):
+        calls.clear()
+        ds = tuner.build_dataset(7, seed=3, nmin=2000, nmax=4000, task="symmgs", start=5, workers=workers)
+        np.testing.assert_array_equal(ds.index, np.arange(5, 12))
+        want = [tuner.dataset_matrix(i, 3, 2000, 4000)[1].n for i in range(5, 12)]
+        assert calls == want and list(ds.sizes[:, 0]) == want
