@@ -57,23 +57,25 @@ def chunk_tables(P, gp):
     return dep, groups, reads, starts
 
 
-def issue_order(dep, groups, power, order=0, stride=2, seg=0, run=2, lag=0, dies=None):
+def issue_order(dep, groups, power, order=0, stride=2, seg=0, run=2, lag=0, dies=None, pass_groups=True):
     """Runs in queue order (die 0's queue, then die 1's), their global ranks
-    and the queue bounds."""
+    and the queue bounds (pass_groups False: no chunk groups, so completion
+    blocks follow the chunk index alone)."""
     L = _lib.lib()
     C_ = len(groups)
     dep = np.ascontiguousarray(dep, np.int32)
     groups = np.ascontiguousarray(groups, np.int32)
+    gptr = groups.ctypes.data if pass_groups else None
     dies_a = None if dies is None else np.ascontiguousarray(dies, np.int32)
     dp = None if dies_a is None else dies_a.ctypes.data
     nr = C.c_int(0)
-    _lib.check(L.race_mpk_issue_order(dep.ctypes.data, groups.ctypes.data, dp, C_, power, order, stride, seg, run,
+    _lib.check(L.race_mpk_issue_order(dep.ctypes.data, gptr, dp, C_, power, order, stride, seg, run,
                                       lag, None, None, None, None, 0, C.byref(nr)))
     head = np.zeros((nr.value, 4), np.int32)
     deps = np.zeros((nr.value, 8), np.int32)
     rank = np.zeros(nr.value, np.int32)
     ds = np.zeros(3, np.int32)
-    _lib.check(L.race_mpk_issue_order(dep.ctypes.data, groups.ctypes.data, dp, C_, power, order, stride, seg, run,
+    _lib.check(L.race_mpk_issue_order(dep.ctypes.data, gptr, dp, C_, power, order, stride, seg, run,
                                       lag, head.ctypes.data, deps.ctypes.data, rank.ctypes.data, ds.ctypes.data,
                                       nr.value, C.byref(nr)))
     return head, deps, rank, ds
@@ -153,6 +155,33 @@ def test_issue_orders_are_valid(name, gen, power, cache):
     for stride in (1, 2):
         head, deps, rank, ds = issue_order(dep, groups, power, 1, stride=stride)
         check_order(head, deps, reads, power, 1, rank, ds)
+
+
+def test_completion_blocks_widen_dependencies():
+    """The kernel counts finished chunks per completion block (at most 16
+    consecutive chunks, inside one level group when groups are given), so
+    every dependency interval is widened to whole blocks; the widened
+    orders stay valid (every chunk of every polled block comes earlier),
+    with groups and by chunk index alone."""
+    power = 4
+    A = matgen.stencil3d_27pt(20)
+    P, gp = partition(A, power, 1e6)
+    dep, groups, reads, _ = chunk_tables(P, gp)
+    dies = two_dies(len(groups), 72, 80)
+    starts = np.flatnonzero((np.arange(len(groups)) % 16 == 0) | np.r_[True, groups[1:] != groups[:-1]])
+    for pass_groups in (True, False):
+        for run, lag in ((1, 0), (4, 0), (4, 300)):
+            head, deps, rank, ds = issue_order(dep, groups, power, 0, run=run, lag=lag, dies=dies,
+                                               pass_groups=pass_groups)
+            check_order(head, deps, reads, power, run, rank, ds, dies)
+            iv = deps.reshape(-1, 2)
+            iv = iv[iv[:, 1] >= iv[:, 0]]
+            block_starts = starts if pass_groups else np.arange(0, len(groups), 16)
+            assert np.isin(iv[:, 0], block_starts).all()  # every interval begins a block
+            ends = np.r_[block_starts[1:], len(groups)] - 1
+            assert np.isin(iv[:, 1], ends).all()  # and ends one
+    head, deps, rank, ds = issue_order(dep, groups, power, 1, stride=1)
+    check_order(head, deps, reads, power, 1, rank, ds)
 
 
 def test_chunk_wavefront_live_window():
