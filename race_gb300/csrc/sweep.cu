@@ -233,6 +233,7 @@ __device__ __forceinline__ void rowSerial(const SweepArgs &a, int r, const Row &
         break;
     }
     case RACE_K_SYMMSPMV: {  // kernels.cpp:403-417
+        if (len == 0) break;  // no diagonal entry to read (the bodies assume one)
         const XT xr = x[r];
         b[r] = mac(row.v(0), xr, b[r]);
         XT t = XT(0);
@@ -246,6 +247,7 @@ __device__ __forceinline__ void rowSerial(const SweepArgs &a, int r, const Row &
         break;
     }
     case RACE_K_GS: {  // kernels.cpp:174-186
+        if (len == 0) break;  // no diagonal entry to divide by
         XT t = b[r];
         row.sum(a, 1, [&](XT v, XT xv) { t = mac(-v, xv, t); });
         x[r] = t / row.v(0);
@@ -572,6 +574,7 @@ __device__ __forceinline__ void rowWarp(const SweepArgs &a, int row, int lane) {
         break;
     }
     case RACE_K_SYMMSPMV: {
+        if (e == s) break;  // no diagonal entry to read
         const XT xr = x[row];
         XT t = XT(0);
         for (int j = s + 1 + lane; j < e; j += 32) {
@@ -585,6 +588,7 @@ __device__ __forceinline__ void rowWarp(const SweepArgs &a, int row, int lane) {
         break;
     }
     case RACE_K_GS: {
+        if (e == s) break;  // no diagonal entry to divide by
         XT t = XT(0);
         for (int j = s + 1 + lane; j < e; j += 32) t = mac(-ld<VT, XT>(val, j), x[a.col[j]], t);
         t = warpSum(t);
@@ -715,6 +719,7 @@ __global__ void kGather(int kernel, int n, const int *__restrict__ ptr, const in
                 acc = mac(ld<VT, XT>(val, e), x[src[k]], acc);
             } else {  // row y's own SymmSpMV update: diagonal, then its off-diagonal dot product
                 const int s = rowPtr[y], end = rowPtr[y + 1];
+                if (end == s) continue;  // no diagonal entry to read
                 acc = mac(ld<VT, XT>(val, s), x[y], acc);
                 XT t = XT(0);
                 for (int j = s + 1; j < end; ++j) t = mac(ld<VT, XT>(val, j), x[col[j]], t);
